@@ -1,0 +1,375 @@
+"""Benchmark: batched self-adjoint eigensolver on GB300 (one JSON line).
+
+Workload (batched configuration of the headline metric): 4096 real symmetric
+GOE matrices A = (B + B')/2, B iid N(0, 1), orders n drawn uniform in
+[8, 128] from numpy PCG64 seed 2; all eigenpairs (eigen!(Hermitian(A))).
+A step = one solve of the whole batch. Synthetic data (the reference
+publishes no benchmark dataset). The packed FP64 input arena is ~191 MB,
+larger than the 129 MB L2, so every step streams it from HBM.
+
+Paths timed: plain FP64 (the reference's arithmetic), plain FP32, and FP32 +
+FP64 Ogita-Aishima refinement (the headline `value`, eigh/s, when it meets
+residual and eigenvalue error <= 1e-13 ||A|| on the checked sample).
+
+--impl reference times the reference algorithm on the host cores instead:
+the CPU restatement of GenericLinearAlgebra.jl's eigen!(Hermitian)
+(oracle/, one matrix per OpenMP thread) — Julia itself is not installed.
+Multi-GPU: the batch shards per rank with no collective ("replicas only");
+value = matrices solved by all ranks / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "genericlinearalgebra.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "eigh/s (batch n≤128) & n=4096 time at 1e-13 resid: FP32+refine vs FP64 GPU"
+BATCH = 4096
+NLO, NHI = 8, 128
+SEED = 2
+
+
+def workload(batch=BATCH, seed=SEED):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = rng.integers(NLO, NHI + 1, size=batch)
+    mats = []
+    for n in ns:
+        B = rng.standard_normal((n, n))
+        mats.append((B + B.T) / 2)
+    return ns.astype(np.int64), mats
+
+
+def pack_f(mats, dtype=np.float64):
+    return np.concatenate([np.asarray(m, dtype=dtype).ravel(order="F") for m in mats])
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def start_clock_sampler():
+    path = tempfile.mktemp(suffix=".csv")
+    try:
+        f = open(path, "w")
+        p = subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+             "--format=csv,noheader,nounits", "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL)
+        return p, f, path
+    except Exception:
+        return None, None, path
+
+
+def stop_clock_sampler(handle, gpu_index=0):
+    p, f, path = handle
+    if p is None:
+        return None
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except Exception:
+        p.kill()
+    f.close()
+    sm, mx, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open(path):
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9 or parts[0] != str(gpu_index):
+            continue
+        try:
+            sm.append(float(parts[1]))
+            mx = max(mx, float(parts[2]))
+        except ValueError:
+            continue
+        for nm, v in zip(names, parts[5:9]):
+            if v.lower() in ("active", "1"):
+                reasons.add(nm)
+    os.unlink(path)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_dgemm_tflops(torch):
+    """FP64 peak measured in this run: cuBLAS DGEMM 4096^3 (best of 3)."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def check_sample(ns, mats, w, V, woff, aoff, idx, dtype):
+    """Max residual ||AV - VW||/||A||, orthogonality and eigenvalue error vs the
+    CPU oracle over the sampled matrices."""
+    from oracle import oracle as O
+    res = orth = ev = 0.0
+    for b in idx:
+        n = int(ns[b])
+        A = mats[b]
+        wb = w[woff[b]: woff[b] + n].astype(np.float64)
+        Vb = V[aoff[b]: aoff[b] + n * n].reshape(n, n, order="F").astype(np.float64)
+        nA = np.linalg.norm(A, 2)
+        res = max(res, np.linalg.norm(A @ Vb - Vb * wb, 2) / nA)
+        orth = max(orth, np.linalg.norm(Vb.T @ Vb - np.eye(n), 2))
+        wo = O.syev(A, "N" if dtype == np.float64 else "N")[0]
+        ev = max(ev, np.abs(wb - wo).max() / nA)
+    return {"max_residual": res, "max_orthogonality": orth, "max_eig_err_vs_oracle": ev}
+
+
+def run_ours(args):
+    import torch
+
+    import glagpu
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    ns, mats = workload(seed=SEED + 1000 * rank)
+    aoff = np.concatenate([[0], np.cumsum(ns * ns)[:-1]]).astype(np.int64)
+    woff = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    A64 = pack_f(mats)
+    A32 = A64.astype(np.float32)
+    nA = len(A64)
+    nW = int(ns.sum())
+    dA64 = torch.from_numpy(A64).to(dev)
+    dA32 = torch.from_numpy(A32).to(dev)
+    sample = np.random.Generator(np.random.PCG64(99)).choice(len(ns), size=48, replace=False)
+    sample = np.unique(np.concatenate([sample, np.argsort(-ns)[:8]]))
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    results = {}
+    for path in ("f64", "f32", "f32_refined"):
+        plan = glagpu.Plan(ns, precision=path, timing=True)
+        dt = torch.float32 if path == "f32" else torch.float64
+        A = dA32 if path == "f32" else dA64
+        w = torch.empty(nW, dtype=dt, device=dev)
+        V = torch.empty(nA, dtype=dt, device=dev)
+        info = torch.zeros(len(ns), dtype=torch.int32, device=dev)
+        for _ in range(args.warmup):
+            plan.execute(A, w, V, info)
+        torch.cuda.synchronize()
+        phases = {k: 0.0 for k in ("tridiag", "chase", "apply", "refine")}
+        counters = None
+        clk = start_clock_sampler() if path == "f32_refined" and rank == 0 else (None, None, "")
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            plan.execute(A, w, V, info)
+            for k, v in plan.phase_times().items():
+                phases[k] += v
+        torch.cuda.synchronize()
+        barrier()
+        el = time.perf_counter() - t0
+        clocks = stop_clock_sampler(clk, local) if clk[0] is not None else None
+        if ws > 1:
+            t = torch.tensor([el], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        counters = plan.stats()
+        wh = w.cpu().numpy()
+        Vh = V.cpu().numpy()
+        acc = check_sample(ns, mats, wh, Vh, woff, aoff, sample, np.float64 if path != "f32" else np.float32)
+        n_bad = int((info.cpu().numpy() != 0).sum())
+        results[path] = {
+            "eigh_per_s": ws * len(ns) * args.steps / el,
+            "ms_per_step": 1e3 * el / args.steps,
+            "phase_ms_per_step": {k: v / args.steps for k, v in phases.items()},
+            "counters": counters,
+            "accuracy": acc,
+            "info_nonzero": n_bad,
+            "clocks": clocks,
+            "launches_per_step": None,
+        }
+        nb = len(plan_buckets(ns))
+        passes = counters["passes"]
+        results[path]["launches_per_step"] = nb + passes * (1 + nb) + (nb if path == "f32_refined" else 0)
+        plan.close()
+    # ---- end to end through the C ABI with host buffers (headline path)
+    plan = glagpu.Plan(ns, precision="f32_refined")
+    hA = torch.from_numpy(A64).pin_memory()
+    hw = torch.empty(nW, dtype=torch.float64).pin_memory()
+    hV = torch.empty(nA, dtype=torch.float64).pin_memory()
+    hinfo = torch.zeros(len(ns), dtype=torch.int32).pin_memory()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.execute_host(hA.numpy(), hw.numpy(), hV.numpy(), hinfo.numpy(), stream)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.execute_host(hA.numpy(), hw.numpy(), hV.numpy(), hinfo.numpy(), stream)
+    barrier()
+    el_e2e = time.perf_counter() - t0
+    plan.close()
+    if ws > 1:
+        t = torch.tensor([el_e2e], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el_e2e = float(t.item())
+    peak = measured_dgemm_tflops(torch) if rank == 0 else None
+
+    if rank == 0:
+        head = results["f32_refined"]
+        ok = head["accuracy"]["max_residual"] <= 1e-13 and head["accuracy"]["max_eig_err_vs_oracle"] <= 1e-13
+        hp = "f32_refined" if ok else "f64"
+        H = results[hp]
+        ph = H["phase_ms_per_step"]
+        dom = max(ph, key=lambda k: ph[k])
+        c = H["counters"]
+        # algorithmic flops of the dominant phase per execute
+        ns3 = float((ns.astype(np.float64) ** 3).sum())
+        flops = {"tridiag": (4.0 / 3.0 + 4.0 / 3.0) * ns3,  # symtri! + explicit Q (structure exploited)
+                 "apply": 6.0 * c["row_rotations"],          # 6 flops per row per rotation
+                 "refine": 6.0 * c["refine_n3"],             # AX 2n^3 + X'Y n^3 + X'X n^3 + XE 2n^3 per iteration
+                 "chase": 0.0}
+        achieved = flops[dom] / (ph[dom] * 1e-3) / 1e12 if ph[dom] > 0 else 0.0
+        cpu = cpu_baseline(ns, mats)
+        line = {
+            "metric": METRIC,
+            "value": H["eigh_per_s"],
+            "unit": "eigh/s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": H["ms_per_step"],
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 solve + f64 refinement" if hp == "f32_refined" else "f64",
+            "data": "synthetic (seeded GOE)",
+            "config": {"workload": f"batched eigen!(Hermitian): {len(ns)} GOE matrices, n~U[{NLO},{NHI}], seed {SEED}",
+                       "path": hp, "batch": len(ns), "sum_n": int(ns.sum()), "sum_n3": ns3,
+                       "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}"},
+            "roofline": {"kernel": dom, "bound": "fp64" if dom != "chase" else "latency",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if peak else None, "traffic": None,
+                         "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (FP64 pipe)"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": ws * len(ns) * args.steps / el_e2e, "unit": "eigh/s",
+                    "h2d_bytes_per_step": int(A64.nbytes),
+                    "d2h_bytes_per_step": int(8 * nA + 8 * nW + 4 * len(ns))},
+            "clocks": results["f32_refined"]["clocks"],
+            "gpu_launches": int(H["launches_per_step"] * args.steps),
+            "paths": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} for k, v in results.items()},
+            "speedup_f32refined_vs_f64": results["f32_refined"]["eigh_per_s"] / results["f64"]["eigh_per_s"],
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def plan_buckets(ns):
+    edges = [0, 32, 64, 96, 128]
+    return [i for i in range(4) if ((ns > edges[i]) & (ns <= edges[i + 1])).any()]
+
+
+def cpu_baseline(ns, mats, budget_s=15.0):
+    """The reference algorithm (CPU restatement, oracle/) on all host cores,
+    one matrix per OpenMP thread, over a bounded sample of the workload."""
+    from oracle import oracle as O
+    nth = os.cpu_count() or 1
+    # sample the first m matrices so that the run takes about budget_s
+    m = min(len(ns), 256)
+    t = time_oracle(ns[:m], mats[:m], nth)
+    per = t / m
+    m2 = int(min(len(ns), max(m, budget_s / max(per, 1e-9))))
+    if m2 > m:
+        t = time_oracle(ns[:m2], mats[:m2], nth)
+        m = m2
+    return {"value": m / t, "unit": "eigh/s", "cores": nth, "kind": "port",
+            "sample": f"first {m} of the {len(ns)} workload matrices, eigen!(Hermitian) FP64, "
+                      f"{nth} OpenMP threads (one matrix per thread)"}
+
+
+def time_oracle(ns, mats, nth):
+    from oracle import oracle as O
+    aoff = np.concatenate([[0], np.cumsum(ns * ns)[:-1]]).astype(np.int64)
+    woff = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    A = pack_f(mats)
+    w = np.zeros(int(ns.sum()))
+    V = np.zeros(len(A))
+    info = np.zeros(len(ns), np.int32)
+    Ac = A.copy()
+    O.batched_raw("V", "L", np.ascontiguousarray(ns), aoff, Ac, w, woff, V, info, nthreads=nth)  # warm
+    Ac = A.copy()
+    t0 = time.perf_counter()
+    O.batched_raw("V", "L", np.ascontiguousarray(ns), aoff, Ac, w, woff, V, info, nthreads=nth)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    ns, mats = workload()
+    nth = os.cpu_count() or 1
+    # each step: a bounded sample (the first 512 matrices) of the workload
+    m = 512
+    for _ in range(args.warmup):
+        time_oracle(ns[:m], mats[:m], nth)
+    tot = 0.0
+    for _ in range(args.steps):
+        tot += time_oracle(ns[:m], mats[:m], nth)
+    val = m * args.steps / tot
+    line = {
+        "metric": METRIC, "value": val, "unit": "eigh/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded GOE)", "impl": "reference",
+        "config": {"workload": f"batched eigen!(Hermitian): {len(ns)} GOE matrices, n~U[{NLO},{NHI}], seed {SEED}",
+                   "path": "reference CPU", "batch": len(ns)},
+        "cpu_baseline": {"value": val, "unit": "eigh/s", "cores": nth, "kind": "port",
+                         "sample": f"first {m} matrices of the workload per step; CPU restatement of "
+                                   "GenericLinearAlgebra.jl eigen!(Hermitian) (Julia not installed), "
+                                   f"{nth} OpenMP threads"},
+        "e2e": {"value": val, "unit": "eigh/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,623 @@
+// C-ABI entry points (include/glagpu.h): plans, workspace, launch sequence.
+//
+// A plan fixes the matrix orders of a batch, so all host-side planning
+// (offsets, size buckets, chase lane order, workspace carving) happens once
+// in gla_plan_create and gla_plan_execute only enqueues kernels.
+//
+// Launch sequence for jobz 'V' (eigen!):
+//   k_tridiag  per size bucket   symtri! + Array(Q)      (one CTA per matrix)
+//   repeat per pass (normally one):
+//     k_chase                     eigQL!/eigQR! scalars   (one lane per matrix)
+//     k_apply  per size bucket    rotations on Q, sorteig!
+//   [F32_REFINED] refinement kernels (refine.cu)
+// jobz 'N' (eigvals!): k_tridiag (no Q), k_chase<PWK>, k_sort_values.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#include "../../include/glagpu.h"
+#include "gla_launch.h"
+#include "gla_refine.h"
+
+using namespace gla;
+
+namespace gla {
+cudaError_t tridiag_kernels_init();
+cudaError_t chase_kernels_init();
+cudaError_t apply_kernels_init();
+}  // namespace gla
+
+namespace {
+
+constexpr int kRotPerN2 = 2;    // rotation-log capacity per pass, in units of n^2
+constexpr int kHdrPerN = 3;     // header-log capacity per pass, in units of n
+constexpr int kMaxSweepsPerN = 30;  // chase cap per matrix (src/eigenGeneral.jl:52 uses 30n)
+constexpr int kMaxPasses = 64;
+
+#define GLA_CUDA(x)                                  \
+  do {                                               \
+    cudaError_t e_ = (x);                            \
+    if (e_ != cudaSuccess) return -1000 - (int)e_;   \
+  } while (0)
+
+struct Bucket {
+  int nmax;   // largest order in the bucket
+  int nt;     // threads per CTA
+  int start;  // first index into perm_bucket
+  int count;
+};
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+std::once_flag g_init_flag;
+cudaError_t g_init_err = cudaSuccess;
+
+cudaError_t ensure_init() {
+  std::call_once(g_init_flag, [] {
+    cudaError_t e;
+    if ((e = tridiag_kernels_init()) != cudaSuccess) g_init_err = e;
+    if ((e = chase_kernels_init()) != cudaSuccess) g_init_err = e;
+    if ((e = apply_kernels_init()) != cudaSuccess) g_init_err = e;
+    if ((e = refine_kernels_init()) != cudaSuccess) g_init_err = e;
+  });
+  return g_init_err;
+}
+
+}  // namespace
+
+struct gla_plan_s {
+  int prec = GLA_PREC_F64;
+  char jobz = 'V', uplo = 'L';
+  int algo = kAlgoQL;
+  int64_t batch = 0;
+  double tol = 0;
+  std::vector<int64_t> n;
+  int64_t a_elems = 0, w_elems = 0;
+  int nwork = 0;  // matrices with n >= 1
+  std::vector<Bucket> buckets;
+  int chase_count = 0;
+  int chase_nmax = 0;
+  int nmax = 0;
+  // device workspace
+  char* ws = nullptr;
+  size_t ws_bytes = 0;
+  SmallDesc* d_desc = nullptr;
+  int* d_perm_bucket = nullptr;
+  int* d_perm_chase = nullptr;
+  void* d_d = nullptr;
+  void* d_e = nullptr;
+  void* d_rot = nullptr;
+  unsigned* d_hdr = nullptr;
+  ChaseState* d_cst = nullptr;
+  int* d_pending = nullptr;
+  unsigned long long* d_stats = nullptr;
+  int* d_scale = nullptr;
+  void* d_x32 = nullptr;  // FP32 eigenvectors (refined runs, or 'N' refined)
+  void* d_w32 = nullptr;
+  RefineWork rw;          // refinement scratch
+  void* d_vtmp = nullptr; // V target when the caller passes none
+  // host-execute buffers
+  void* h_A = nullptr;
+  void* h_w = nullptr;
+  void* h_V = nullptr;
+  int* h_info = nullptr;
+  int* pin_pending = nullptr;
+  cudaStream_t last_stream = nullptr;
+  int last_passes = 0;
+  // phase timing (GLA_FLAG_TIMING): events[phase][0/1] per chase pass
+  bool timing = false;
+  static constexpr int kEv = 2 * GLA_NUM_PHASES * (kMaxPasses + 1);
+  cudaEvent_t ev[kEv] = {};
+  int nev[GLA_NUM_PHASES] = {};
+  void mark(int phase, int end, cudaStream_t st) {
+    if (!timing) return;
+    const int slot = nev[phase] / 2;
+    if (slot > kMaxPasses) return;
+    cudaEventRecord(ev[(phase * (kMaxPasses + 1) + slot) * 2 + end], st);
+    nev[phase]++;
+  }
+  int tcode() const { return prec == GLA_PREC_F64 ? kF64 : (prec == GLA_PREC_F32 ? kF32 : kF32FromF64); }
+  size_t elem() const { return prec == GLA_PREC_F64 ? 8 : 4; }          // working element size
+  size_t io_elem() const { return prec == GLA_PREC_F32 ? 4 : 8; }       // caller element size
+};
+
+extern "C" {
+
+int gla_version(void) { return GLA_VERSION; }
+
+const char* gla_status_string(int status) {
+  if (status == 0) return "success";
+  if (status > 0) return "some matrices did not converge or held non-finite values (see info)";
+  if (status <= -1000) return cudaGetErrorString((cudaError_t)(-1000 - status));
+  switch (status) {
+    case -1: return "invalid argument 1";
+    case -2: return "invalid argument 2";
+    case -3: return "invalid argument 3";
+    case -4: return "invalid argument 4";
+    case -5: return "invalid argument 5";
+    case -6: return "invalid argument 6";
+    case -7: return "invalid argument 7";
+    case -8: return "invalid argument 8";
+    case -9: return "invalid argument 9";
+    case -10: return "invalid argument 10";
+    default: return "invalid argument";
+  }
+}
+
+int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, int64_t batch, const int64_t* n,
+                    double tol, int flags) {
+  if (!plan_out) return -1;
+  *plan_out = nullptr;
+  if (precision != GLA_PREC_F64 && precision != GLA_PREC_F32 && precision != GLA_PREC_F32_REFINED) return -2;
+  if (jobz != 'V' && jobz != 'N') return -3;
+  if (uplo != 'L' && uplo != 'U') return -4;
+  if (batch < 0) return -5;
+  if (batch > 0 && !n) return -6;
+  for (int64_t b = 0; b < batch; b++)
+    if (n[b] < 0 || n[b] > GLA_MAX_SMALL_N) return -6;
+  if (!(tol == tol)) return -7;
+  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING)) != 0 || (flags & 3) > GLA_ALG_QR) return -8;
+  GLA_CUDA(ensure_init());
+
+  gla_plan_s* p = new (std::nothrow) gla_plan_s();
+  if (!p) return -1;
+  p->prec = precision;
+  p->jobz = jobz;
+  p->uplo = uplo;
+  p->algo = (flags & 3) == GLA_ALG_QR ? kAlgoQR : kAlgoQL;
+  p->batch = batch;
+  p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? 0x1p-52 : (double)0x1p-23f);
+  p->timing = (flags & GLA_FLAG_TIMING) != 0;
+  if (p->timing)
+    for (int i = 0; i < gla_plan_s::kEv; i++) {
+      cudaError_t e = cudaEventCreate(&p->ev[i]);
+      if (e != cudaSuccess) {
+        delete p;
+        return -1000 - (int)e;
+      }
+    }
+  p->n.assign(n, n + batch);
+
+  // ---- descriptors and offsets
+  std::vector<SmallDesc> desc(batch);
+  int64_t aoff = 0, woff = 0, roff = 0, hoff = 0;
+  for (int64_t b = 0; b < batch; b++) {
+    const int nb = (int)n[b];
+    SmallDesc& d = desc[b];
+    d.n = nb;
+    d.pad = 0;
+    d.a_off = aoff;
+    d.w_off = woff;
+    d.rot_off = roff;
+    d.hdr_off = hoff;
+    d.rot_cap = (flags & GLA_FLAG_SMALL_LOG) ? nb * nb / 8 + nb : kRotPerN2 * nb * nb + 4;
+    d.hdr_cap = (flags & GLA_FLAG_SMALL_LOG) ? nb / 4 + 2 : kHdrPerN * nb + 4;
+    aoff += (int64_t)nb * nb;
+    woff += nb;
+    roff += d.rot_cap;
+    hoff += d.hdr_cap;
+    p->nmax = std::max(p->nmax, nb);
+  }
+  p->a_elems = aoff;
+  p->w_elems = woff;
+
+  // ---- size buckets (descending order inside each bucket), chase order
+  std::vector<int> idx;
+  for (int64_t b = 0; b < batch; b++)
+    if (n[b] >= 1) idx.push_back((int)b);
+  p->nwork = (int)idx.size();
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return n[a] > n[b]; });
+  std::vector<int> perm_bucket;
+  const int edges[4] = {32, 64, 96, 128};
+  int lo = 0;
+  for (int ei = 0; ei < 4; ei++) {
+    Bucket bk;
+    bk.nmax = 0;
+    bk.start = (int)perm_bucket.size();
+    bk.count = 0;
+    for (int b : idx) {
+      if (n[b] > lo && n[b] <= edges[ei]) {
+        perm_bucket.push_back(b);
+        bk.count++;
+        bk.nmax = std::max(bk.nmax, (int)n[b]);
+      }
+    }
+    bk.nt = std::max(32, (bk.nmax + 31) / 32 * 32);
+    if (bk.count) p->buckets.push_back(bk);
+    lo = edges[ei];
+  }
+  std::vector<int> perm_chase = idx;  // n >= 2 only need a chase, n == 1 too (trivially done)
+  p->chase_count = (int)perm_chase.size();
+  p->chase_nmax = p->nmax;
+
+  // ---- workspace carve-up
+  const size_t el = p->elem();
+  size_t off = 0;
+  auto carve = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + std::max<size_t>(bytes, 1), 256);
+    return o;
+  };
+  const size_t o_desc = carve(sizeof(SmallDesc) * batch);
+  const size_t o_pb = carve(sizeof(int) * perm_bucket.size());
+  const size_t o_pc = carve(sizeof(int) * perm_chase.size());
+  const size_t o_d = carve(el * woff);
+  const size_t o_e = carve(el * woff);
+  const bool wantvec = jobz == 'V' || precision == GLA_PREC_F32_REFINED;
+  const size_t o_rot = carve(wantvec ? 2 * el * roff : 0);
+  const size_t o_hdr = carve(wantvec ? sizeof(unsigned) * hoff : 0);
+  const size_t o_cst = carve(sizeof(ChaseState) * batch);
+  const size_t o_pend = carve(sizeof(int) * 4);
+  const size_t o_stats = carve(sizeof(unsigned long long) * 4);
+  const size_t o_scale = carve(sizeof(int) * batch);
+  const bool refined = precision == GLA_PREC_F32_REFINED;
+  const size_t o_x32 = carve(refined ? 4 * aoff : 0);
+  const size_t o_w32 = carve(refined ? 4 * woff : 0);
+  const size_t o_vtmp = carve((jobz == 'N' && refined) ? 8 * aoff : 0);
+  size_t refine_bytes = refined ? refine_workspace_bytes(aoff, woff, batch) : 0;
+  const size_t o_ref = carve(refine_bytes);
+  p->ws_bytes = off;
+  cudaError_t err = cudaMalloc((void**)&p->ws, p->ws_bytes);
+  if (err != cudaSuccess) {
+    delete p;
+    return -1000 - (int)err;
+  }
+  char* w = p->ws;
+  p->d_desc = (SmallDesc*)(w + o_desc);
+  p->d_perm_bucket = (int*)(w + o_pb);
+  p->d_perm_chase = (int*)(w + o_pc);
+  p->d_d = w + o_d;
+  p->d_e = w + o_e;
+  p->d_rot = w + o_rot;
+  p->d_hdr = (unsigned*)(w + o_hdr);
+  p->d_cst = (ChaseState*)(w + o_cst);
+  p->d_pending = (int*)(w + o_pend);
+  p->d_stats = (unsigned long long*)(w + o_stats);
+  p->d_scale = (int*)(w + o_scale);
+  p->d_x32 = refined ? (void*)(w + o_x32) : nullptr;
+  p->d_w32 = refined ? (void*)(w + o_w32) : nullptr;
+  p->d_vtmp = (jobz == 'N' && refined) ? (void*)(w + o_vtmp) : nullptr;
+  if (refined) refine_carve(&p->rw, w + o_ref, aoff, woff, batch);
+  if (batch) err = cudaMemcpy(p->d_desc, desc.data(), sizeof(SmallDesc) * batch, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && !perm_bucket.empty())
+    err = cudaMemcpy(p->d_perm_bucket, perm_bucket.data(), sizeof(int) * perm_bucket.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && !perm_chase.empty())
+    err = cudaMemcpy(p->d_perm_chase, perm_chase.data(), sizeof(int) * perm_chase.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemset(p->d_scale, 0, sizeof(int) * std::max<int64_t>(batch, 1));
+  if (err == cudaSuccess) err = cudaMallocHost((void**)&p->pin_pending, sizeof(int) * 4);
+  if (err != cudaSuccess) {
+    cudaFree(p->ws);
+    delete p;
+    return -1000 - (int)err;
+  }
+  *plan_out = p;
+  return 0;
+}
+
+int gla_plan_destroy(gla_plan_t p) {
+  if (!p) return -1;
+  if (p->timing)
+    for (int i = 0; i < gla_plan_s::kEv; i++) cudaEventDestroy(p->ev[i]);
+  cudaFree(p->ws);
+  cudaFree(p->h_A);
+  cudaFree(p->h_w);
+  cudaFree(p->h_V);
+  cudaFree(p->h_info);
+  cudaFreeHost(p->pin_pending);
+  delete p;
+  return 0;
+}
+
+int gla_plan_workspace_size(gla_plan_t p, size_t* bytes) {
+  if (!p) return -1;
+  if (!bytes) return -2;
+  *bytes = p->ws_bytes;
+  return 0;
+}
+
+int gla_plan_arena_sizes(gla_plan_t p, int64_t* a_elems, int64_t* w_elems) {
+  if (!p) return -1;
+  if (a_elems) *a_elems = p->a_elems;
+  if (w_elems) *w_elems = p->w_elems;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Chase passes + apply (vectors) for the working type; V holds Q on entry.
+int run_chase_apply(gla_plan_t p, int tcode, void* V, void* wout, int* info, const int* scale, cudaStream_t st) {
+  const size_t el = tcode == kF64 ? 8 : 4;
+  const int work_t = tcode == kF64 ? kF64 : kF32;
+  const size_t chase_smem = chase_smem_bytes(p->chase_nmax, (int)el);
+  int passes = 0;
+  for (;;) {
+    GLA_CUDA(cudaMemsetAsync(p->d_pending, 0, sizeof(int), st));
+    p->mark(GLA_PHASE_CHASE, 0, st);
+    GLA_CUDA(launch_chase(work_t, p->algo, p->chase_count, chase_smem, st, p->d_desc, p->d_perm_chase, p->d_d,
+                          p->d_e, p->d_cst, p->d_rot, p->d_hdr, info, p->tol, kMaxSweepsPerN, p->d_pending,
+                          p->d_stats));
+    p->mark(GLA_PHASE_CHASE, 1, st);
+    p->mark(GLA_PHASE_APPLY, 0, st);
+    for (const Bucket& bk : p->buckets)
+      GLA_CUDA(launch_apply(work_t, bk.count, bk.nt, apply_smem_bytes(bk.nmax, (int)el), st, p->d_desc,
+                            p->d_perm_bucket + bk.start, V, p->d_d, wout, p->d_cst, p->d_rot, p->d_hdr, info,
+                            scale));
+    p->mark(GLA_PHASE_APPLY, 1, st);
+    passes++;
+    GLA_CUDA(cudaMemcpyAsync(p->pin_pending, p->d_pending, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GLA_CUDA(cudaStreamSynchronize(st));
+    if (*p->pin_pending == 0 || passes >= kMaxPasses) break;
+  }
+  p->last_passes = passes;
+  return 0;
+}
+
+int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaStream_t st) {
+  p->last_stream = st;
+  for (int i = 0; i < GLA_NUM_PHASES; i++) p->nev[i] = 0;
+  GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
+  if (p->batch) GLA_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * p->batch, st));
+  if (p->nwork == 0) return 0;
+  const int lower = p->uplo == 'L';
+  const int tc = p->tcode();
+  const size_t el = p->elem();
+  if (p->prec != GLA_PREC_F32_REFINED) {
+    const bool wantq = p->jobz == 'V';
+    p->mark(GLA_PHASE_TRIDIAG, 0, st);
+    for (const Bucket& bk : p->buckets)
+      GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt, tridiag_smem_bytes(bk.nmax, bk.nt, (int)el), st,
+                              p->d_desc, p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, V, info, p->d_cst,
+                              nullptr));
+    p->mark(GLA_PHASE_TRIDIAG, 1, st);
+    if (wantq) {
+      int rc = run_chase_apply(p, tc, V, w, info, nullptr, st);
+      if (rc) return rc;
+    } else {
+      p->mark(GLA_PHASE_CHASE, 0, st);
+      GLA_CUDA(launch_chase(tc, kAlgoPWK, p->chase_count, chase_smem_bytes(p->chase_nmax, (int)el), st, p->d_desc,
+                            p->d_perm_chase, p->d_d, p->d_e, p->d_cst, nullptr, nullptr, info, p->tol,
+                            kMaxSweepsPerN, p->d_pending, p->d_stats));
+      p->mark(GLA_PHASE_CHASE, 1, st);
+      p->mark(GLA_PHASE_APPLY, 0, st);
+      for (const Bucket& bk : p->buckets)
+        GLA_CUDA(launch_sort_values(tc, bk.count, st, p->d_desc, p->d_perm_bucket + bk.start, p->d_d, w, info,
+                                    nullptr));
+      p->mark(GLA_PHASE_APPLY, 1, st);
+      p->last_passes = 1;
+    }
+    return 0;
+  }
+  // ---- FP32 solve on the 2^-s scaled matrix, then FP64 refinement
+  p->mark(GLA_PHASE_TRIDIAG, 0, st);
+  for (const Bucket& bk : p->buckets)
+    GLA_CUDA(launch_tridiag(kF32FromF64, true, bk.count, bk.nt, tridiag_smem_bytes(bk.nmax, bk.nt, 4), st,
+                            p->d_desc, p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, p->d_x32, info,
+                            p->d_cst, p->d_scale));
+  p->mark(GLA_PHASE_TRIDIAG, 1, st);
+  int rc = run_chase_apply(p, kF32FromF64, p->d_x32, p->d_w32, info, p->d_scale, st);
+  if (rc) return rc;
+  void* Vout = p->jobz == 'V' ? V : p->d_vtmp;
+  p->mark(GLA_PHASE_REFINE, 0, st);
+  for (const Bucket& bk : p->buckets)
+    GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
+                           lower, (const float*)p->d_x32, (const float*)p->d_w32, (double*)Vout, (double*)w, info,
+                           p->d_stats));
+  p->mark(GLA_PHASE_REFINE, 1, st);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gla_plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, void* stream) {
+  if (!p) return -1;
+  if (!A && p->a_elems) return -2;
+  if (!w && p->w_elems) return -3;
+  if (p->jobz == 'V' && !V && p->a_elems) return -4;
+  if (!info && p->batch) return -5;
+  return plan_execute(p, A, w, V, info, (cudaStream_t)stream);
+}
+
+int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host,
+                          void* stream) {
+  if (!p) return -1;
+  if (!A_host && p->a_elems) return -2;
+  if (!w_host && p->w_elems) return -3;
+  if (p->jobz == 'V' && !V_host && p->a_elems) return -4;
+  if (!info_host && p->batch) return -5;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t ioe = p->io_elem();
+  const size_t abytes = ioe * std::max<int64_t>(p->a_elems, 1), wbytes = ioe * std::max<int64_t>(p->w_elems, 1);
+  if (!p->h_A) {
+    GLA_CUDA(cudaMalloc(&p->h_A, abytes));
+    GLA_CUDA(cudaMalloc(&p->h_w, wbytes));
+    GLA_CUDA(cudaMalloc(&p->h_V, p->jobz == 'V' ? abytes : 16));
+    GLA_CUDA(cudaMalloc((void**)&p->h_info, sizeof(int) * std::max<int64_t>(p->batch, 1)));
+  }
+  GLA_CUDA(cudaMemcpyAsync(p->h_A, A_host, ioe * p->a_elems, cudaMemcpyHostToDevice, st));
+  int rc = plan_execute(p, p->h_A, p->h_w, p->h_V, p->h_info, st);
+  if (rc) return rc;
+  GLA_CUDA(cudaMemcpyAsync(w_host, p->h_w, ioe * p->w_elems, cudaMemcpyDeviceToHost, st));
+  if (p->jobz == 'V') GLA_CUDA(cudaMemcpyAsync(V_host, p->h_V, ioe * p->a_elems, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaMemcpyAsync(info_host, p->h_info, sizeof(int) * p->batch, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaStreamSynchronize(st));
+  int bad = 0;
+  for (int64_t b = 0; b < p->batch; b++) bad += info_host[b] != 0;
+  return bad;
+}
+
+int gla_plan_phase_times(gla_plan_t p, float* ms) {
+  if (!p) return -1;
+  if (!ms) return -2;
+  for (int ph = 0; ph < GLA_NUM_PHASES; ph++) ms[ph] = 0.f;
+  if (!p->timing) return 0;
+  GLA_CUDA(cudaStreamSynchronize(p->last_stream));
+  for (int ph = 0; ph < GLA_NUM_PHASES; ph++) {
+    for (int slot = 0; slot < p->nev[ph] / 2; slot++) {
+      float t = 0.f;
+      const int base = (ph * (kMaxPasses + 1) + slot) * 2;
+      GLA_CUDA(cudaEventElapsedTime(&t, p->ev[base], p->ev[base + 1]));
+      ms[ph] += t;
+    }
+  }
+  return 0;
+}
+
+int gla_plan_stats(gla_plan_t p, int64_t* rotations, int64_t* sweeps, int* passes) {
+  int64_t c[GLA_NUM_COUNTERS];
+  int rc = gla_plan_counters(p, c);
+  if (rc) return rc;
+  if (rotations) *rotations = c[GLA_COUNTER_ROTATIONS];
+  if (sweeps) *sweeps = c[GLA_COUNTER_SWEEPS];
+  if (passes) *passes = (int)c[GLA_COUNTER_PASSES];
+  return 0;
+}
+
+int gla_plan_counters(gla_plan_t p, int64_t* c) {
+  if (!p) return -1;
+  if (!c) return -2;
+  unsigned long long h[4] = {0, 0, 0, 0};
+  GLA_CUDA(cudaStreamSynchronize(p->last_stream));
+  GLA_CUDA(cudaMemcpy(h, p->d_stats, sizeof(h), cudaMemcpyDeviceToHost));
+  c[GLA_COUNTER_ROTATIONS] = (int64_t)h[0];
+  c[GLA_COUNTER_SWEEPS] = (int64_t)h[1];
+  c[GLA_COUNTER_ROW_ROTATIONS] = (int64_t)h[2];
+  c[GLA_COUNTER_REFINE_N3] = (int64_t)h[3];
+  c[GLA_COUNTER_PASSES] = p->last_passes;
+  return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- single-matrix drivers
+namespace {
+
+struct SingleKey {
+  int prec;
+  char jobz, uplo;
+  int64_t n;
+  int flags;
+  bool operator<(const SingleKey& o) const {
+    return std::tie(prec, jobz, uplo, n, flags) < std::tie(o.prec, o.jobz, o.uplo, o.n, o.flags);
+  }
+};
+struct SingleEntry {
+  gla_plan_t plan = nullptr;
+  void* buf = nullptr;  // packed n*n matrix + n values
+  int* dinfo = nullptr;
+};
+std::mutex g_single_mu;
+std::map<SingleKey, SingleEntry> g_single;
+
+int single_entry(int prec, char jobz, char uplo, int64_t n, int flags, SingleEntry** out) {
+  SingleKey k{prec, jobz, uplo, n, flags};
+  auto it = g_single.find(k);
+  if (it != g_single.end()) {
+    *out = &it->second;
+    return 0;
+  }
+  SingleEntry e;
+  int rc = gla_plan_create(&e.plan, prec, jobz, uplo, 1, &n, 0.0, flags);
+  if (rc) return rc;
+  const size_t el = prec == GLA_PREC_F32 ? 4 : 8;
+  GLA_CUDA(cudaMalloc(&e.buf, el * (size_t)(n * n + 2 * n + 2)));
+  GLA_CUDA(cudaMalloc((void**)&e.dinfo, sizeof(int)));
+  auto r = g_single.emplace(k, e);
+  *out = &r.first->second;
+  return 0;
+}
+
+template <class T>
+int syev_single(int prec, char jobz, char uplo, int64_t n, T* A, int64_t lda, T* w, int* info, void* stream) {
+  if (jobz != 'V' && jobz != 'N') return -1;
+  if (uplo != 'L' && uplo != 'U') return -2;
+  if (n < 0 || n > GLA_MAX_SMALL_N) return -3;
+  if (!A && n) return -4;
+  if (lda < std::max<int64_t>(1, n)) return -5;
+  if (!w && n) return -6;
+  if (!info) return -7;
+  *info = 0;
+  if (n == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_single_mu);
+  SingleEntry* e;
+  int rc = single_entry(prec, jobz, uplo, n, 0, &e);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  T* buf = (T*)e->buf;
+  GLA_CUDA(cudaMemcpy2DAsync(buf, sizeof(T) * n, A, sizeof(T) * lda, sizeof(T) * n, n, cudaMemcpyDeviceToDevice, st));
+  rc = gla_plan_execute(e->plan, buf, w, buf, e->dinfo, stream);
+  if (rc) return rc;
+  if (jobz == 'V')
+    GLA_CUDA(cudaMemcpy2DAsync(A, sizeof(T) * lda, buf, sizeof(T) * n, sizeof(T) * n, n, cudaMemcpyDeviceToDevice, st));
+  GLA_CUDA(cudaMemcpyAsync(info, e->dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaStreamSynchronize(st));
+  return *info != 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gla_dsyev(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, int* info, void* stream) {
+  return syev_single<double>(GLA_PREC_F64, jobz, uplo, n, A, lda, w, info, stream);
+}
+
+int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, int* info, void* stream) {
+  return syev_single<float>(GLA_PREC_F32, jobz, uplo, n, A, lda, w, info, stream);
+}
+
+int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz, int flags, int* info,
+              void* stream) {
+  if (jobz != 'V' && jobz != 'N') return -1;
+  if (n < 0 || n > GLA_MAX_SMALL_N) return -2;
+  if (!d && n) return -3;
+  if (!e && n > 1) return -4;
+  if (jobz == 'V' && !Z && n) return -5;
+  if (jobz == 'V' && ldz < std::max<int64_t>(1, n)) return -6;
+  if ((flags & ~3) != 0 || (flags & 3) > GLA_ALG_QR) return -7;
+  if (!info) return -8;
+  *info = 0;
+  if (n == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_single_mu);
+  SingleEntry* ent;
+  int rc = single_entry(GLA_PREC_F64, jobz, 'L', n, flags, &ent);
+  if (rc) return rc;
+  gla_plan_t p = ent->plan;
+  cudaStream_t st = (cudaStream_t)stream;
+  double* buf = (double*)ent->buf;   // Q (n*n) | e padded (n)
+  double* epad = buf + n * n;
+  GLA_CUDA(cudaMemsetAsync(epad, 0, sizeof(double) * n, st));
+  if (n > 1) GLA_CUDA(cudaMemcpyAsync(epad, e, sizeof(double) * (n - 1), cudaMemcpyDeviceToDevice, st));
+  GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
+  p->last_stream = st;
+  GLA_CUDA(launch_init_tridiagonal(kF64, 1, st, p->d_desc, p->d_perm_bucket, d, epad, p->d_d, p->d_e, buf,
+                                   ent->dinfo, p->d_cst, jobz == 'V'));
+  if (jobz == 'V') {
+    rc = run_chase_apply(p, kF64, buf, d, ent->dinfo, nullptr, st);
+    if (rc) return rc;
+    GLA_CUDA(cudaMemcpy2DAsync(Z, sizeof(double) * ldz, buf, sizeof(double) * n, sizeof(double) * n, n,
+                               cudaMemcpyDeviceToDevice, st));
+  } else {
+    GLA_CUDA(launch_chase(kF64, kAlgoPWK, 1, chase_smem_bytes((int)n, 8), st, p->d_desc, p->d_perm_chase, p->d_d,
+                          p->d_e, p->d_cst, nullptr, nullptr, ent->dinfo, p->tol, kMaxSweepsPerN, p->d_pending,
+                          p->d_stats));
+    GLA_CUDA(launch_sort_values(kF64, 1, st, p->d_desc, p->d_perm_bucket, p->d_d, d, ent->dinfo, nullptr));
+  }
+  if (n > 1) GLA_CUDA(cudaMemcpyAsync(e, p->d_e, sizeof(double) * (n - 1), cudaMemcpyDeviceToDevice, st));
+  GLA_CUDA(cudaMemcpyAsync(info, ent->dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaStreamSynchronize(st));
+  return *info != 0;
+}
+
+}  // extern "C"

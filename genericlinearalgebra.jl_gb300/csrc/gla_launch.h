@@ -1,0 +1,41 @@
+// Host-side launchers of the small-matrix kernels (one per kernel family;
+// each returns the launch error). Element type codes: kF64 = double,
+// kF32 = float, kF32FromF64 = float work type loading double input.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "gla_small.cuh"
+
+namespace gla {
+
+enum TypeCode { kF64 = 0, kF32 = 1, kF32FromF64 = 2 };
+
+size_t tridiag_smem_bytes(int n, int nt, int elem);
+size_t chase_smem_bytes(int nmax, int elem);
+size_t apply_smem_bytes(int n, int elem);
+
+// Raise the dynamic shared-memory limit of every kernel instantiation once.
+cudaError_t small_kernels_init();
+
+cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
+                           const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
+                           void* Q, int* info, ChaseState* cst, int* scale_exp);
+
+cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
+                         const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,
+                         double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats);
+
+cudaError_t launch_apply(int tcode, int nblocks, int nt, size_t smem, cudaStream_t st, const SmallDesc* descs,
+                         const int* perm, void* V, const void* d, void* w, ChaseState* cst, const void* rot,
+                         const unsigned* hdr, const int* info, const int* scale_exp);
+
+cudaError_t launch_sort_values(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
+                               const void* d, void* w, const int* info, const int* scale_exp);
+
+// SymTridiagonal input: copy (d, e) into the working arrays, Q := I, reset state.
+cudaError_t launch_init_tridiagonal(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs,
+                                    const int* perm, const void* din, const void* ein, void* d, void* e, void* Q,
+                                    int* info, ChaseState* cst, bool wantq);
+
+}  // namespace gla

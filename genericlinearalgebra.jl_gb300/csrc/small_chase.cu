@@ -1,0 +1,402 @@
+// Implicit-shift QL / QR / root-free PWK iterations on the tridiagonal,
+// one matrix per lane (32 matrices per warp, matrices sorted by size so the
+// lanes of a warp run similar-length loops).
+//
+// Replaces, per matrix:
+//   eigQL!          (GenericLinearAlgebra.jl src/eigenSelfAdjoint.jl:221-288)
+//   singleShiftQL!  (:377-409)
+//   eigQR!          (:290-340), singleShiftQR! (:412-444)
+//   eigvalsPWK!     (:163-219), singleShiftQLPWK! (:343-374)
+//   eig2x2! / eigvals2x2 (:131-161)
+//   givensAlgorithm for Float64/Float32 (LinearAlgebra's LAPACK-dlartg port).
+//
+// The scalar recurrence of a chase is serial, and on GB300 an FP64 warp
+// instruction costs the FP64 unit ~64 cycles whatever the active-lane count,
+// so running one matrix per lane is 32x cheaper than one per warp. The
+// rotations (c, s) are not applied here: they are appended to a per-matrix
+// log (plus one header per sweep) that the apply kernel replays on the rows
+// of Q in parallel. When a matrix's log is full the lane stops between
+// sweeps, saves its state and is resumed by the next pass.
+//
+// Differences from the reference, all rounding-level: the Givens radius
+// uses a Newton-refined hardware rsqrt seed instead of sqrt and two
+// divisions; gamma/c uses a refined reciprocal; the deflation test
+// |e| <= tol*sqrt|d_i|*sqrt|d_i+1| (:250-256) is decided on exponents when
+// the two sides are more than a factor 4 apart and evaluated exactly
+// otherwise (identical decisions on identical data). Each chase is capped at
+// max_sweeps_per_n * n sweeps (the reference has no cap and loops forever on
+// e.g. NaN input); hitting the cap reports the unconverged count as info.
+#include "gla_launch.h"
+#include "gla_small.cuh"
+
+namespace gla {
+
+template <class T> GLA_DEV bool is_zero(T x) { return (prec<T>::bits(x) << 1) == 0; }
+
+// Deflation test of :250-256 (and of :177 with e holding e^2).
+template <class T> GLA_DEV bool negligible(T ev, T d1, T d2, T tol, int tol_e) {
+  const int maxe = sizeof(T) == 8 ? 0x7ff : 0xff;
+  const int xe = prec<T>::biased_exp(ev), x1 = prec<T>::biased_exp(d1), x2 = prec<T>::biased_exp(d2);
+  if (xe != 0 && xe != maxe && x1 != 0 && x1 != maxe && x2 != 0 && x2 != maxe) {
+    // q = 2log2|e| - log2|d1| - log2|d2| - 2log2(tol) lies in (L-4, L+2)
+    const int L = 2 * xe - x1 - x2 - 2 * tol_e;
+    if (L + 2 <= 0) return true;
+    if (L - 4 >= 0) return false;
+  }
+  return tabs(ev) <= tol * prec<T>::sqrt_ieee(tabs(d1)) * prec<T>::sqrt_ieee(tabs(d2));
+}
+
+// LAPACK 3.x dlartg convention (as in LinearAlgebra.givensAlgorithm for
+// AbstractFloat): r = +-sqrt(f^2+g^2), (c,s,r) negated when |f|>|g| and c<0.
+template <class T> GLA_DEV void givens_exact(T f, T g, T& cs, T& sn, T& r) {
+  const T safmn2 = sizeof(T) == 8 ? (T)0x1p-485 : (T)0x1p-51f;
+  const T safmx2 = T(1) / safmn2;
+  T f1 = f, g1 = g;
+  T scale = fmax(tabs(f1), tabs(g1));
+  int count = 0;
+  if (scale >= safmx2) {
+    do {
+      count++;
+      f1 *= safmn2;
+      g1 *= safmn2;
+      scale = fmax(tabs(f1), tabs(g1));
+    } while (scale >= safmx2 && count < 20);
+    r = prec<T>::sqrt_ieee(f1 * f1 + g1 * g1);
+    cs = prec<T>::div_ieee(f1, r);
+    sn = prec<T>::div_ieee(g1, r);
+    for (int i = 0; i < count; i++) r *= safmx2;
+  } else if (scale <= safmn2) {
+    do {
+      count++;
+      f1 *= safmx2;
+      g1 *= safmx2;
+      scale = fmax(tabs(f1), tabs(g1));
+    } while (scale <= safmn2 && count < 4000);
+    r = prec<T>::sqrt_ieee(f1 * f1 + g1 * g1);
+    cs = prec<T>::div_ieee(f1, r);
+    sn = prec<T>::div_ieee(g1, r);
+    for (int i = 0; i < count; i++) r *= safmn2;
+  } else {
+    r = prec<T>::sqrt_ieee(f1 * f1 + g1 * g1);
+    cs = prec<T>::div_ieee(f1, r);
+    sn = prec<T>::div_ieee(g1, r);
+  }
+}
+
+template <class T> GLA_DEV void givens(T f, T g, T& c, T& s, T& r) {
+  if (is_zero(g)) {
+    c = 1;
+    s = 0;
+    r = f;
+    return;
+  }
+  if (is_zero(f)) {
+    c = 0;
+    s = 1;
+    r = g;
+    return;
+  }
+  if (prec<T>::tame(f) && prec<T>::tame(g)) {
+    const T r2 = fma(f, f, g * g);
+    const T y = prec<T>::rsqrt(r2);
+    r = r2 * y;
+    c = f * y;
+    s = g * y;
+  } else {
+    givens_exact(f, g, c, s, r);
+  }
+  // |f| > |g| and c < 0 (c has the sign of f)
+  if (!abs_le(f, g) && (prec<T>::bits(c) >> (sizeof(T) * 8 - 1))) {
+    c = -c;
+    s = -s;
+    r = -r;
+  }
+}
+
+template <class T> GLA_DEV T div_fast(T a, T b) {
+  return prec<T>::tame(b) ? a * prec<T>::rcp(b) : prec<T>::div_ieee(a, b);
+}
+
+size_t chase_smem_bytes(int nmax, int elem) { return (size_t)2 * nmax * 32 * elem; }
+
+// ALGO: kAlgoQL (eigQL!, logs rotations), kAlgoQR (eigQR!, logs), kAlgoPWK
+// (eigvalsPWK!, values only). d, e: per-matrix diagonals at w_off (e padded
+// to n entries). rot: 2 values per rotation; hdr: one word per sweep.
+template <class T, int ALGO>
+__global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
+                                              int count, T* __restrict__ dg_all, T* __restrict__ eg_all,
+                                              ChaseState* __restrict__ cst, T* __restrict__ rot,
+                                              unsigned* __restrict__ hdr, int* __restrict__ info, T tol,
+                                              int max_sweeps_per_n, int* __restrict__ pending,
+                                              unsigned long long* __restrict__ stats) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x;
+  const int slot = blockIdx.x * 32 + lane;
+  const bool have = slot < count;
+  const int mid = have ? perm[slot] : 0;
+  SmallDesc dsc;
+  dsc.n = 0;
+  if (have) dsc = descs[mid];
+  const int n = dsc.n;
+  int nmax = n;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+  T* D = reinterpret_cast<T*>(smem_raw) + lane;
+  T* E = reinterpret_cast<T*>(smem_raw) + (size_t)nmax * 32 + lane;
+#define DD(i) D[(size_t)(i) * 32]
+#define EE(i) E[(size_t)(i) * 32]
+
+  ChaseState st;
+  st.status = kChaseDone;
+  if (have) st = cst[mid];
+  const bool was_running = have && st.status == kChaseRunning;
+  bool active = was_running;
+  T* dg = dg_all + dsc.w_off;
+  T* eg = eg_all + dsc.w_off;
+  if (active) {
+    for (int i = 0; i < n; i++) {
+      DD(i) = dg[i];
+      const T e = eg[i];
+      // eigvalsPWK! squares the off-diagonal first (:171-173)
+      EE(i) = (ALGO == kAlgoPWK && st.nsweeps == 0 && st.bs == 0) ? e * e : e;
+    }
+  }
+  const int tol_e = prec<T>::biased_exp(tol) - prec<T>::expbias;
+  const int cap = max_sweeps_per_n * n;
+  int bs = st.bs, nsw = st.nsweeps;
+  int nrot = 0, nhdr = 0;
+  T* myrot = rot + 2 * dsc.rot_off;
+  unsigned* myhdr = hdr + dsc.hdr_off;
+  bool insweep = false, stopped_full = false;
+  int i = 0, be = 0;
+  T mu = 0, gam = 0, p = 0, c = 1, s = 0;
+  int iters = 0;
+  const int iter_cap = (max_sweeps_per_n + 4) * 4 * nmax * nmax + 64;  // hard bound on loop trips
+
+  while (__any_sync(0xffffffffu, active)) {
+    if (++iters > iter_cap) {  // defensive: never reached when the sweep cap works
+      if (active) {
+        info[mid] = max(1, n - 1);
+        active = false;
+        st.status = kChaseDone;
+      }
+      continue;
+    }
+    if (active && !insweep) {
+      if (bs >= n - 1) {
+        active = false;
+        st.status = kChaseDone;
+      } else {
+        be = n - 1;
+        for (int b = bs + 1; b <= n - 1; b++) {
+          if (negligible(EE(b - 1), DD(b - 1), DD(b), tol, tol_e)) {
+            be = b - 1;
+            break;
+          }
+        }
+        if (bs == be) {
+          bs += 1;
+        } else if (bs + 1 == be) {
+          if (ALGO == kAlgoPWK) {
+            const T d1 = DD(bs), d2 = DD(be), ee = prec<T>::sqrt_ieee(EE(bs));
+            const T r1 = (d1 + d2) / 2;
+            const T r2 = hypot_borges(d1 - d2, 2 * ee) / 2;
+            DD(bs) = r1 + r2;
+            DD(be) = r1 - r2;
+            EE(bs) = 0;
+            bs += 1;
+          } else if (nrot + 1 > dsc.rot_cap || nhdr + 1 > dsc.hdr_cap) {
+            active = false;
+            stopped_full = true;
+          } else {
+            // eig2x2! (:136-161)
+            const T dj = DD(bs), dj1 = DD(be), ej = EE(bs);
+            const T r1 = (dj + dj1) / 2;
+            const T r2 = hypot_borges(dj - dj1, 2 * ej) / 2;
+            const T lp = r1 + r2, lm = r1 - r2;
+            DD(bs) = lp;
+            DD(be) = lm;
+            EE(bs) = 0;
+            T cc, ss;
+            if (is_zero(ej)) {
+              cc = 1;
+              ss = 0;
+            } else if (tabs(lp - dj) > tabs(lm - dj)) {
+              cc = prec<T>::div_ieee(-ej, hypot_borges(ej, lp - dj));
+              ss = prec<T>::sqrt_ieee(1 - cc * cc);
+            } else {
+              ss = prec<T>::div_ieee(tabs(ej), hypot_borges(ej, lm - dj));
+              cc = tcopysign(prec<T>::sqrt_ieee(1 - ss * ss), -ej);
+            }
+            myhdr[nhdr++] = pack_hdr(bs, 1, 0);
+            myrot[2 * nrot] = cc;
+            myrot[2 * nrot + 1] = ss;
+            nrot++;
+            bs += 2;
+          }
+        } else if (nsw >= cap) {
+          int cnt = 0;
+          for (int b = 0; b + 1 < n; b++) cnt += !negligible(EE(b), DD(b), DD(b + 1), tol, tol_e);
+          info[mid] = max(cnt, 1);
+          active = false;
+          st.status = kChaseDone;
+        } else if (ALGO != kAlgoPWK && (nrot + (be - bs) > dsc.rot_cap || nhdr + 1 > dsc.hdr_cap)) {
+          active = false;
+          stopped_full = true;
+        } else {
+          // shift (:199-202 PWK, :271-273 QL, :324-326 QR) and start a chase
+          if (ALGO == kAlgoPWK) {
+            const T sqrte = prec<T>::sqrt_ieee(EE(bs));
+            T m = (DD(bs + 1) - DD(bs)) / (2 * sqrte);
+            const T r = hypot_borges(m, T(1));
+            mu = DD(bs) - sqrte / (m + tcopysign(r, m));
+            gam = DD(be) - mu;
+            p = gam * gam;
+            i = be - 1;
+          } else if (ALGO == kAlgoQL) {
+            T m = (DD(bs + 1) - DD(bs)) / (2 * EE(bs));
+            const T r = hypot_borges(m, T(1));
+            mu = DD(bs) - (EE(bs) / (m + tcopysign(r, m)));
+            gam = DD(be) - mu;
+            p = gam;
+            i = be - 1;
+            myhdr[nhdr++] = pack_hdr(be - 1, be - bs, 0);
+          } else {
+            T m = (DD(be - 1) - DD(be)) / (2 * EE(be - 1));
+            const T r = hypot_borges(m, T(1));
+            mu = DD(be) - (EE(be - 1) / (m + tcopysign(r, m)));
+            gam = DD(bs) - mu;
+            p = gam;
+            i = bs + 1;
+            myhdr[nhdr++] = pack_hdr(bs + 1, be - bs, 1);
+          }
+          c = 1;
+          s = 0;
+          insweep = true;
+          nsw++;
+        }
+      }
+    }
+    if (active && insweep) {
+      if (ALGO == kAlgoQL) {
+        // singleShiftQL! step at i (:389-405)
+        const T ei = EE(i);
+        const T c1 = c, s1 = s;
+        T zeta;
+        givens(p, ei, c, s, zeta);
+        if (i < be - 1) EE(i + 1) = s1 * zeta;
+        const T di = DD(i);
+        const T g1 = gam;
+        gam = c * c * (di - mu) - s * s * g1;
+        DD(i + 1) = g1 + di - gam;
+        p = is_zero(c) ? -ei * c1 : div_fast(gam, c);
+        myrot[2 * nrot] = c;
+        myrot[2 * nrot + 1] = s;
+        nrot++;
+        i--;
+        if (i < bs) {
+          EE(bs) = s * p;
+          DD(bs) = mu + gam;
+          insweep = false;
+        }
+      } else if (ALGO == kAlgoQR) {
+        // singleShiftQR! step at i (:424-440)
+        const T ei = EE(i - 1);
+        const T c1 = c, s1 = s;
+        T zeta;
+        givens(p, ei, c, s, zeta);
+        if (i > bs + 1) EE(i - 2) = s1 * zeta;
+        const T di = DD(i);
+        const T g1 = gam;
+        gam = c * c * (di - mu) - s * s * g1;
+        DD(i - 1) = g1 + di - gam;
+        p = is_zero(c) ? -ei * c1 : div_fast(gam, c);
+        myrot[2 * nrot] = c;
+        myrot[2 * nrot + 1] = s;
+        nrot++;
+        i++;
+        if (i > be) {
+          EE(be - 1) = s * p;
+          DD(be) = mu + gam;
+          insweep = false;
+        }
+      } else {
+        // singleShiftQLPWK! step at i (:356-370); e holds squares
+        const T ei = EE(i);
+        const T zeta = p + ei;
+        if (i < be - 1) EE(i + 1) = s * zeta;
+        const T c1 = c;
+        const T rz = prec<T>::tame(zeta) ? prec<T>::rcp(zeta) : prec<T>::div_ieee(T(1), zeta);
+        c = p * rz;
+        s = ei * rz;
+        const T di = DD(i);
+        const T g1 = gam;
+        gam = c * (di - mu) - s * g1;
+        DD(i + 1) = g1 + di - gam;
+        p = is_zero(c) ? ei * c1 : div_fast(gam * gam, c);
+        i--;
+        if (i < bs) {
+          EE(bs) = s * p;
+          DD(bs) = mu + gam;
+          insweep = false;
+        }
+      }
+    }
+  }
+  if (was_running) {
+    for (int k = 0; k < n; k++) {
+      dg[k] = DD(k);
+      eg[k] = EE(k);
+    }
+    const int sweeps_this_pass = nsw - st.nsweeps;
+    st.bs = bs;
+    st.nsweeps = nsw;
+    st.nrot = nrot;
+    st.nhdr = nhdr;
+    cst[mid] = st;
+    if (stopped_full) atomicAdd(pending, 1);
+    atomicAdd(&stats[0], (unsigned long long)(ALGO == kAlgoPWK ? 0 : nrot));
+    atomicAdd(&stats[1], (unsigned long long)sweeps_this_pass);
+    atomicAdd(&stats[2], (unsigned long long)(ALGO == kAlgoPWK ? 0 : nrot) * (unsigned long long)n);
+  }
+#undef DD
+#undef EE
+}
+
+
+template <class T, int ALGO> static void set_chase_attr() {
+  cudaFuncSetAttribute(k_chase<T, ALGO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 128 * 32 * (int)sizeof(T));
+}
+
+cudaError_t chase_kernels_init() {
+  set_chase_attr<double, kAlgoQL>();
+  set_chase_attr<double, kAlgoQR>();
+  set_chase_attr<double, kAlgoPWK>();
+  set_chase_attr<float, kAlgoQL>();
+  set_chase_attr<float, kAlgoQR>();
+  set_chase_attr<float, kAlgoPWK>();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
+                         const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,
+                         double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats) {
+  if (count <= 0) return cudaSuccess;
+  const int nb = (count + 31) / 32;
+#define GLA_CH(T, A)                                                                                             \
+  k_chase<T, A><<<nb, 32, smem, st>>>(descs, perm, count, (T*)d, (T*)e, cst, (T*)rot, hdr, info, (T)tol,        \
+                                      max_sweeps_per_n, pending, stats)
+  if (tcode == kF64) {
+    if (algo == kAlgoQL) GLA_CH(double, kAlgoQL);
+    else if (algo == kAlgoQR) GLA_CH(double, kAlgoQR);
+    else GLA_CH(double, kAlgoPWK);
+  } else {
+    if (algo == kAlgoQL) GLA_CH(float, kAlgoQL);
+    else if (algo == kAlgoQR) GLA_CH(float, kAlgoQR);
+    else GLA_CH(float, kAlgoPWK);
+  }
+#undef GLA_CH
+  return cudaGetLastError();
+}
+
+}  // namespace gla

@@ -1,0 +1,285 @@
+"""glagpu — Python host mirror of GenericLinearAlgebra.jl's self-adjoint
+eigensolver API, running on the GB300 kernels of libglagpu.so.
+
+Reference interface (GenericLinearAlgebra.jl v0.4.0, src/eigenSelfAdjoint.jl)
+and the functions here that mirror it:
+
+  eigen!(Hermitian/Symmetric)   :626-630   -> eigen(A, uplo=...)       (copying)
+  eigvals!(Hermitian/Symmetric) :584-588   -> eigvals(A, uplo=...)
+  eigen!(SymTridiagonal)        :623       -> eigen(SymTridiagonal(dv, ev))
+  eigvals!(SymTridiagonal)      :581       -> eigvals(SymTridiagonal(dv, ev))
+  eigQR!                        :290-340   -> alg="QR"
+  keyword tol = eps(T)          :566-630   -> tol=None (eps of the precision)
+  sortby = eigsortby (ascending)           -> always ascending (the default)
+  LinearAlgebra.Eigen                      -> Eigen(values, vectors)
+
+Beside the reference's plain path, precision="f32_refined" runs the FP32
+solve plus FP64 Ogita-Aishima refinement, and Plan / eigen_batched solve
+thousands of matrices per launch sequence.
+
+Inputs are torch CUDA tensors (results stay on the device) or numpy arrays
+(host buffers: copied in and out by the library, results as numpy). Errors:
+DimensionMismatch for shape errors (as the reference raises at :230-243),
+NonConvergenceError(info) when a chase hits its sweep cap (the reference
+would loop forever; LAPACK-style info as in src/lapack.jl:62) and
+NonFiniteError for NaN/Inf input.
+"""
+import ctypes as C
+from collections import namedtuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import GLA_ALG_QL, GLA_ALG_QR, GLA_MAX_SMALL_N, GLAError
+
+Eigen = namedtuple("Eigen", ["values", "vectors"])
+
+PRECISIONS = {"f64": _lib.GLA_PREC_F64, "f32": _lib.GLA_PREC_F32, "f32_refined": _lib.GLA_PREC_F32_REFINED}
+
+
+class DimensionMismatch(ValueError):
+    pass
+
+
+class NonConvergenceError(RuntimeError):
+    """Raised when info > 0 for some matrix (sweep cap reached)."""
+
+    def __init__(self, info):
+        self.info = info
+        super().__init__(f"eigensolver did not converge (info = {info})")
+
+
+class NonFiniteError(ValueError):
+    """Raised when the referenced triangle holds NaN or Inf (info == -1)."""
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _is_torch(x):
+    try:
+        import torch
+    except ImportError:
+        return False
+    return isinstance(x, torch.Tensor)
+
+
+def _stream_ptr(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class SymTridiagonal:
+    """SymTridiagonal(dv, ev): diagonal (n) and off-diagonal (n-1)."""
+
+    def __init__(self, dv, ev):
+        self.dv = dv
+        self.ev = ev
+        n = len(dv)
+        if len(ev) != max(n - 1, 0):
+            raise DimensionMismatch(f"off-diagonal has length {len(ev)}, expected {max(n - 1, 0)}")
+
+
+def _raise_for_info(info):
+    info = np.asarray(info)
+    if (info == -1).any():
+        raise NonFiniteError("input contains NaN or Inf")
+    if (info > 0).any():
+        raise NonConvergenceError(int(info[info > 0][0]))
+
+
+class Plan:
+    """Batched solver plan over matrices of orders `ns` (each <= 128).
+
+    Arena layout: matrix b is column-major n_b x n_b at offset sum(n_c^2, c<b);
+    its eigenvalues at sum(n_c, c<b). precision: "f64", "f32", "f32_refined".
+    """
+
+    def __init__(self, ns, precision="f64", jobz="V", uplo="L", tol=None, alg="QL", small_log=False,
+                 timing=False):
+        L = _lib.load()
+        ns = np.ascontiguousarray(np.asarray(ns, dtype=np.int64))
+        if (ns < 0).any() or (ns > GLA_MAX_SMALL_N).any():
+            raise DimensionMismatch(f"orders must lie in [0, {GLA_MAX_SMALL_N}]")
+        self.ns = ns
+        self.precision = precision
+        self.jobz = jobz
+        self.uplo = uplo
+        self.dtype = np.float32 if precision == "f32" else np.float64
+        flags = (GLA_ALG_QR if alg == "QR" else GLA_ALG_QL) | (_lib.GLA_FLAG_SMALL_LOG if small_log else 0) | \
+            (_lib.GLA_FLAG_TIMING if timing else 0)
+        h = C.c_void_p()
+        _lib.check(L.gla_plan_create(C.byref(h), PRECISIONS[precision], jobz.encode(), uplo.encode(), len(ns),
+                                     ns.ctypes.data_as(C.POINTER(C.c_int64)), float(tol or 0.0), flags),
+                   "gla_plan_create")
+        self._h = h
+        a = C.c_int64()
+        w = C.c_int64()
+        L.gla_plan_arena_sizes(h, C.byref(a), C.byref(w))
+        self.a_elems = a.value
+        self.w_elems = w.value
+        self.a_off = np.zeros(len(ns), np.int64)
+        self.w_off = np.zeros(len(ns), np.int64)
+        if len(ns) > 1:
+            self.a_off[1:] = np.cumsum(ns * ns)[:-1]
+            self.w_off[1:] = np.cumsum(ns)[:-1]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().gla_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def workspace_bytes(self):
+        b = C.c_size_t()
+        _lib.check(_lib.load().gla_plan_workspace_size(self._h, C.byref(b)))
+        return b.value
+
+    def execute(self, A, w, V, info, stream=None):
+        """Device run: A, w, V (may be None for jobz 'N'), info are torch CUDA
+        tensors holding the packed arenas. Asynchronous on `stream`."""
+        rc = _lib.load().gla_plan_execute(self._h, C.c_void_p(A.data_ptr()), C.c_void_p(w.data_ptr()),
+                                          C.c_void_p(V.data_ptr()) if V is not None else None,
+                                          C.c_void_p(info.data_ptr()), _stream_ptr(stream))
+        return _lib.check(rc, "gla_plan_execute")
+
+    def execute_host(self, A, w, V, info, stream=None):
+        """Host-buffer run (numpy arenas); copies in/out and synchronizes.
+        Returns the number of matrices with nonzero info."""
+        rc = _lib.load().gla_plan_execute_host(self._h, C.c_void_p(A.ctypes.data), C.c_void_p(w.ctypes.data),
+                                               C.c_void_p(V.ctypes.data) if V is not None else None,
+                                               C.c_void_p(info.ctypes.data),
+                                               _stream_ptr(stream) if stream is not None else None)
+        return _lib.check(rc, "gla_plan_execute_host")
+
+    def stats(self):
+        """Work counters of the last execute (rotations, sweeps, row_rotations,
+        refine_n3, passes)."""
+        c = (C.c_int64 * len(_lib.COUNTERS))()
+        _lib.check(_lib.load().gla_plan_counters(self._h, c))
+        return dict(zip(_lib.COUNTERS, [int(x) for x in c]))
+
+    def phase_times(self):
+        """Milliseconds per phase of the last execute (plan made with timing=True)."""
+        ms = (C.c_float * len(_lib.PHASES))()
+        _lib.check(_lib.load().gla_plan_phase_times(self._h, ms))
+        return dict(zip(_lib.PHASES, [float(x) for x in ms]))
+
+    # -- packing helpers (column-major arenas)
+    def pack(self, mats, device=None):
+        """Pack square matrices into the column-major A arena (numpy, or torch on `device`)."""
+        if device is None:
+            return np.concatenate([np.asarray(m, dtype=self.dtype).ravel(order="F") for m in mats]) \
+                if len(mats) else np.zeros(1, self.dtype)
+        torch = _torch()
+        dt = torch.float32 if self.dtype == np.float32 else torch.float64
+        return torch.cat([torch.as_tensor(m, dtype=dt, device=device).t().contiguous().reshape(-1) for m in mats])
+
+    def unpack(self, w, V=None):
+        vals, vecs = [], []
+        for b, n in enumerate(self.ns):
+            vals.append(w[self.w_off[b]: self.w_off[b] + n])
+            if V is not None:
+                seg = V[self.a_off[b]: self.a_off[b] + n * n]
+                vecs.append(seg.reshape(n, n).T if not _is_torch(seg) else seg.reshape(n, n).t())
+        return vals, (vecs if V is not None else None)
+
+
+def _solve_batched(mats, jobz, uplo, tol, precision, alg, check):
+    if len(mats) == 0:
+        return []
+    for m in mats:
+        if m.ndim != 2 or m.shape[0] != m.shape[1]:
+            raise DimensionMismatch(f"matrix is not square: dimensions are {tuple(m.shape)}")
+    ns = [int(m.shape[0]) for m in mats]
+    plan = Plan(ns, precision=precision, jobz=jobz, uplo=uplo, tol=tol, alg=alg)
+    try:
+        if _is_torch(mats[0]):
+            torch = _torch()
+            dev = mats[0].device
+            A = plan.pack(mats, device=dev)
+            dt = A.dtype
+            w = torch.empty(max(plan.w_elems, 1), dtype=dt, device=dev)
+            V = torch.empty(max(plan.a_elems, 1), dtype=dt, device=dev) if jobz == "V" else None
+            info = torch.zeros(len(mats), dtype=torch.int32, device=dev)
+            plan.execute(A, w, V, info)
+            info_h = info.cpu().numpy()
+        else:
+            A = plan.pack(mats)
+            w = np.zeros(max(plan.w_elems, 1), plan.dtype)
+            V = np.zeros(max(plan.a_elems, 1), plan.dtype) if jobz == "V" else None
+            info_h = np.zeros(len(mats), np.int32)
+            plan.execute_host(A, w, V, info_h)
+        if check:
+            _raise_for_info(info_h)
+        vals, vecs = plan.unpack(w, V)
+        if jobz == "V":
+            return [Eigen(v, x) for v, x in zip(vals, vecs)], info_h
+        return vals, info_h
+    finally:
+        plan.close()
+
+
+def eigen_batched(mats, uplo="L", tol=None, precision="f64", alg="QL", check=True):
+    """[eigen(Hermitian(A, uplo)) for A in mats] in one batched launch sequence."""
+    r = _solve_batched(list(mats), "V", uplo, tol, precision, alg, check)
+    return r[0] if r else []
+
+
+def eigvals_batched(mats, uplo="L", tol=None, precision="f64", check=True):
+    r = _solve_batched(list(mats), "N", uplo, tol, precision, "QL", check)
+    return r[0] if r else []
+
+
+def _tridiag(T, jobz, alg, tol):
+    if tol is not None:
+        raise ValueError("tol for SymTridiagonal input: only the default eps(Float64) is supported")
+    L = _lib.load()
+    torch = _torch()
+    on_dev = _is_torch(T.dv)
+    dev = T.dv.device if on_dev else torch.device("cuda")
+    d = torch.as_tensor(T.dv, dtype=torch.float64, device=dev).clone()
+    e = torch.as_tensor(T.ev, dtype=torch.float64, device=dev).clone()
+    n = d.numel()
+    if e.numel() == 0:
+        e = torch.zeros(1, dtype=torch.float64, device=dev)
+    Z = torch.empty((n, n), dtype=torch.float64, device=dev) if jobz == "V" else None
+    info = C.c_int()
+    rc = L.gla_dstev(jobz.encode(), n, C.c_void_p(d.data_ptr()), C.c_void_p(e.data_ptr()),
+                     C.c_void_p(Z.data_ptr()) if Z is not None else None, max(n, 1),
+                     GLA_ALG_QR if alg == "QR" else GLA_ALG_QL, C.byref(info), _stream_ptr())
+    _lib.check(rc, "gla_dstev")
+    _raise_for_info([info.value])
+    if jobz == "V":
+        Zt = Z.t()  # column-major buffer -> row-major view
+        if on_dev:
+            return Eigen(d, Zt)
+        return Eigen(d.cpu().numpy(), Zt.cpu().numpy())
+    return d if on_dev else d.cpu().numpy()
+
+
+def eigen(A, uplo="L", tol=None, precision="f64", alg="QL"):
+    """eigen(Hermitian(A, uplo)) / eigen(SymTridiagonal): ascending values and
+    the matching orthonormal eigenvectors (columns)."""
+    if isinstance(A, SymTridiagonal):
+        return _tridiag(A, "V", alg, tol)
+    return eigen_batched([A], uplo=uplo, tol=tol, precision=precision, alg=alg)[0]
+
+
+def eigvals(A, uplo="L", tol=None, precision="f64"):
+    """eigvals(Hermitian(A, uplo)) / eigvals(SymTridiagonal): ascending values."""
+    if isinstance(A, SymTridiagonal):
+        return _tridiag(A, "N", "QL", tol)
+    return eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
+
+
+__all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigvals", "eigen_batched", "eigvals_batched",
+           "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N"]

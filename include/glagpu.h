@@ -1,0 +1,157 @@
+/*
+ * glagpu.h — C ABI of the GB300 (sm_103a) self-adjoint eigensolver.
+ *
+ * Drop-in for the eigen/eigvals path of GenericLinearAlgebra.jl v0.4.0
+ * (src/eigenSelfAdjoint.jl). Each entry point names the reference
+ * interface it replaces. Conventions follow the reference's own native
+ * boundary (src/lapack.jl:40-62, ccall into LAPACK): plain C types,
+ * column-major storage, character flags, an integer status, no exceptions
+ * across the ABI.
+ *
+ *   status   0  success
+ *           <0  argument -status is invalid (LAPACK xerbla convention)
+ *         -1000 - e  CUDA runtime error e (see gla_status_string)
+ *           >0  number of matrices whose per-matrix info is nonzero
+ *   info[b]  0  converged
+ *           >0  number of off-diagonal entries still above the deflation
+ *               threshold after the sweep cap (30*n chases per matrix;
+ *               the reference has no cap and never returns on such input)
+ *           -1  the referenced triangle held NaN or Inf (outputs are NaN)
+ *
+ * Buffers are caller-owned; the library owns only plans and their
+ * workspace. All pointers passed to *_execute are device pointers unless
+ * the function name ends in _host. Calls are asynchronous on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) except where stated.
+ */
+#ifndef GLAGPU_H
+#define GLAGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLA_VERSION 100
+
+/* Arithmetic of a plan. */
+#define GLA_PREC_F64 0         /* plain FP64 end to end */
+#define GLA_PREC_F32 1         /* plain FP32 end to end (float in/out) */
+#define GLA_PREC_F32_REFINED 2 /* FP32 solve + Ogita-Aishima refinement, FP64 in/out */
+
+/* Chase algorithm (flags bits 0-1). */
+#define GLA_ALG_QL 0 /* eigQL!  (src/eigenSelfAdjoint.jl:221-288), the default */
+#define GLA_ALG_QR 1 /* eigQR!  (src/eigenSelfAdjoint.jl:290-340) */
+
+/* Flag bit: shrink the per-pass rotation log to ~n^2/8 so that the chase
+ * runs in several passes (exercises the resume path; results are identical). */
+#define GLA_FLAG_SMALL_LOG 4
+/* Flag bit: record CUDA events around each phase of every execute (see
+ * gla_plan_phase_times). */
+#define GLA_FLAG_TIMING 8
+
+/* Phases reported by gla_plan_phase_times. */
+#define GLA_PHASE_TRIDIAG 0 /* symtri! + Array(Q)          */
+#define GLA_PHASE_CHASE 1   /* eigQL!/eigQR!/eigvalsPWK! scalar chase */
+#define GLA_PHASE_APPLY 2   /* rotations on Q + sorteig!   */
+#define GLA_PHASE_REFINE 3  /* Ogita-Aishima refinement    */
+#define GLA_NUM_PHASES 4
+
+#define GLA_MAX_SMALL_N 128
+
+typedef struct gla_plan_s* gla_plan_t;
+
+int gla_version(void);
+const char* gla_status_string(int status);
+
+/*
+ * Batched plan over `batch` independent real symmetric matrices of orders
+ * n[0..batch) (host array, 0 <= n[b] <= GLA_MAX_SMALL_N).
+ *
+ * Packed arena layout used by the execute calls: matrix b is n[b] x n[b],
+ * column-major with leading dimension n[b], at element offset
+ * a_off(b) = sum_{c<b} n[c]^2; its eigenvalues at w_off(b) = sum_{c<b} n[c].
+ *
+ * jobz 'V' -> eigen!(Hermitian(A, uplo))  (src/eigenSelfAdjoint.jl:614-630:
+ *             symtri!, Array(Q), eigQL!, sorteig!)
+ * jobz 'N' -> eigvals!(Hermitian(A, uplo)) (:572-588: symtri!, eigvalsPWK!,
+ *             sorteig!)
+ * tol <= 0 selects eps of the working precision, the reference default
+ * (tol = eps(real(eltype(A)))). Allocates the plan's device workspace
+ * (synchronous).
+ */
+int gla_plan_create(gla_plan_t* plan, int precision, char jobz, char uplo, int64_t batch, const int64_t* n,
+                    double tol, int flags);
+int gla_plan_destroy(gla_plan_t plan);
+/* Device workspace held by the plan, in bytes. */
+int gla_plan_workspace_size(gla_plan_t plan, size_t* bytes);
+/* Total arena sizes (elements) of A/V and of w for this plan. */
+int gla_plan_arena_sizes(gla_plan_t plan, int64_t* a_elems, int64_t* w_elems);
+
+/*
+ * Run the plan. A: packed input arena (double for F64 and F32_REFINED,
+ * float for F32), only the uplo triangle of each matrix is read and A is
+ * not modified. w: packed eigenvalues, ascending per matrix. V: packed
+ * eigenvectors (columns in eigenvalue order; unused for jobz 'N'; may be
+ * the same buffer as A). info: one int per matrix (device). Asynchronous.
+ */
+int gla_plan_execute(gla_plan_t plan, const void* A, void* w, void* V, int* info, void* stream);
+
+/*
+ * Same, from and to HOST buffers: copies A in, runs, copies w, V and info
+ * out, and synchronizes `stream` before returning. Uses plan-owned device
+ * buffers (allocated on first use). Pinned host memory is fastest.
+ */
+int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, void* V_host, int* info_host,
+                          void* stream);
+
+/*
+ * Statistics of the last execute: total Givens rotations applied to the
+ * eigenvectors, implicit-shift chases and chase passes. Synchronizes the
+ * plan's last stream.
+ */
+int gla_plan_stats(gla_plan_t plan, int64_t* rotations, int64_t* sweeps, int* passes);
+
+/*
+ * Work counters of the last execute (synchronizes the plan's last stream):
+ * the algorithmic-work figures a roofline needs.
+ */
+#define GLA_COUNTER_ROTATIONS 0     /* Givens rotations applied to eigenvectors */
+#define GLA_COUNTER_SWEEPS 1        /* implicit-shift chases */
+#define GLA_COUNTER_ROW_ROTATIONS 2 /* sum over matrices of n * rotations (rows rotated) */
+#define GLA_COUNTER_REFINE_N3 3     /* sum over matrices of refinement iterations * n^3 */
+#define GLA_COUNTER_PASSES 4        /* chase passes */
+#define GLA_NUM_COUNTERS 5
+int gla_plan_counters(gla_plan_t plan, int64_t* counters);
+
+/*
+ * Milliseconds spent in each phase (GLA_PHASE_*) by the last execute, from
+ * CUDA events recorded on the execute's stream (plan created with
+ * GLA_FLAG_TIMING; otherwise all zero). Synchronizes that stream.
+ */
+int gla_plan_phase_times(gla_plan_t plan, float* ms);
+
+/*
+ * Single-matrix LAPACK-style driver (device pointers), the in-place form of
+ * LinearAlgebra.eigen!(Hermitian(A, uplo)) (src/eigenSelfAdjoint.jl:626):
+ * on return A holds the eigenvectors (jobz 'V') and w the ascending
+ * eigenvalues. lda >= n. *info is written on the host (synchronizes).
+ */
+int gla_dsyev(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, int* info, void* stream);
+int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, int* info, void* stream);
+
+/*
+ * eigen!/eigvals! of SymTridiagonal(d, e) (src/eigenSelfAdjoint.jl:581,
+ * :602-612, :623): d (n), e (n-1) device arrays, overwritten; on return d
+ * holds the ascending eigenvalues and Z (n x n, ldz) the eigenvectors
+ * (jobz 'V'). flags selects QL (default) or QR. Synchronizes.
+ */
+int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz, int flags, int* info,
+              void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLAGPU_H */

@@ -1,0 +1,185 @@
+"""CPU oracle pinned against the reference's own known answers
+(GenericLinearAlgebra.jl test/eigenselfadjoint.jl), LAPACK and the 256-bit
+restatement. No GPU."""
+import mpmath
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+from helpers import from_hex, goe, golden, orth, prescribed, residual, signfix, sym_from, vec_parity
+from oracle import oracle as O
+
+
+def test_one_by_one():
+    # test/eigenselfadjoint.jl:100-105
+    w, _ = O.stev([1.0], [], "N")[:2]
+    assert list(w) == [1.0]
+    w, V, info = O.stev([1.0], [], "V")
+    assert list(w) == [1.0] and V.tolist() == [[1.0]] and info == 0
+    w, V, info = O.syev(np.array([[1.0]]))
+    assert list(w) == [1.0] and V.tolist() == [[1.0]]
+
+
+@pytest.mark.parametrize("pos", [0, 2])
+def test_issue52_zero_diagonal(pos):
+    # test/eigenselfadjoint.jl:108-117: exact equality with LAPACK eigvals
+    M = np.zeros((3, 3))
+    M[pos, pos] = 0.01
+    lap = sl.eigh(M, eigvals_only=True)
+    for jobz in "NV":
+        w = O.syev(M, jobz)[0]
+        assert np.array_equal(w, lap), (jobz, w, lap)
+
+
+def test_issue139_diagonal():
+    # test/eigenselfadjoint.jl:164-170
+    A = np.diag([1.0, 2.0])
+    assert O.syev(A, "N")[0].tolist() == [1.0, 2.0]
+    assert O.syev(A, "V")[0].tolist() == [1.0, 2.0]
+
+
+def test_issue123_against_256bit():
+    # test/eigenselfadjoint.jl:125-133 (matrix read from the test file)
+    g = golden()["issue123"]
+    M = np.array([[float(v) for v in row] for row in g["A"]])
+    w, V, info = O.syev(M)
+    assert info == 0
+    assert residual(M, V, w) < 1e-14
+    w256 = np.array([float(mpmath.mpf(v)) for v in g["w"]])
+    assert np.abs(w - w256).max() <= 1e-14 * np.linalg.norm(M, 2)
+
+
+def test_eig2x2_table():
+    # test/eigenselfadjoint.jl:135-149: hypot(c, s) ≈ 1 for every case
+    for case in golden()["eig2x2_cases"]:
+        d, e, V, c, s = O.eig2x2(case["d"], case["e"])
+        assert np.isclose(np.hypot(c, s), 1.0, rtol=np.sqrt(2.2e-16)), case
+        assert e[0] == 0.0
+
+
+def test_generic_givens():
+    # test/eigenselfadjoint.jl:93-98
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        x, y = rng.standard_normal(2)
+        for generic in (True, False):
+            c, s, r = O.givens(x, y, generic)
+            assert np.isclose(c * x + s * y, r, rtol=1e-14)
+            assert np.isclose(c * y, s * x, rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_prescribed_spectrum(uplo):
+    # test/eigenselfadjoint.jl:54-84 (real version): vals ≈ λ with rtol = 1e-13 n
+    n = 50
+    lam = 10.0 ** np.linspace(-8, 0, n)
+    A = prescribed(lam, 7)
+    w, V, info = O.syev(A, "V", uplo)
+    assert info == 0
+    assert np.linalg.norm(w - lam) <= 1e-13 * n * max(np.linalg.norm(w), np.linalg.norm(lam))
+    assert residual(A, V, w) < 1e-13
+    assert orth(V) < 1e-13
+    wn = O.syev(A, "N", uplo)[0]
+    assert np.linalg.norm(wn - w) <= np.sqrt(2.2e-16) * np.linalg.norm(w)
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_symtri_and_eigenq(uplo):
+    # test/eigenselfadjoint.jl:61-68: Q == lmul!(Q, I), Q ≈ rmul!(I, Q), Q'Q ≈ I, Q'AQ ≈ T
+    n = 12
+    A = goe(n, 21)
+    F, tau, d, e = O.symtri(A, uplo)
+    Q, F1 = O.eigenq_lmul(uplo, F, tau, np.eye(n))
+    Q2, _ = O.eigenq_lmul(uplo, F, tau, np.eye(n))
+    assert np.array_equal(Q, Q2)
+    Q3, _ = O.eigenq_rmul(uplo, F, tau, np.eye(n))
+    assert np.allclose(Q, Q3, atol=1e-14)
+    assert np.allclose(Q.T @ Q, np.eye(n), atol=1e-14)
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    assert np.allclose(Q.T @ sym_from(A, uplo) @ Q, T, atol=1e-13)
+
+
+@pytest.mark.parametrize("n,seed", [(3, 11), (5, 12), (8, 13), (16, 14), (24, 15)])
+def test_goe_against_256bit(n, seed):
+    g = [c for c in golden()["goe"] if c["n"] == n][0]
+    A = from_hex(g["A"])
+    w256 = np.array([float(mpmath.mpf(v)) for v in g["w"]])
+    V256 = np.array(g["V"])
+    nA = np.linalg.norm(A, 2)
+    for uplo in "LU":
+        w, V, info = O.syev(A, "V", uplo)
+        assert info == 0
+        assert np.abs(w - w256).max() <= 4 * n * 2.2e-16 * nA
+        assert vec_parity(A, V, V256, w256) <= 1.0
+    # the binary128 run of the same algorithm agrees with the 256-bit one
+    whi, wlo, Vhi, Vlo, info = O.syev_quad(A)
+    for i in range(n):
+        assert abs(mpmath.mpf(whi[i]) + mpmath.mpf(wlo[i]) - mpmath.mpf(g["w"][i])) <= 1e-30 * nA
+
+
+def test_against_lapack():
+    rng = np.random.default_rng(9)
+    for n in [2, 3, 7, 31, 64, 100, 128]:
+        A = goe(n, int(rng.integers(1 << 30)))
+        ws = sl.eigh(A, eigvals_only=True)
+        for use_qr in (False, True):
+            w, V, info = O.syev(A, "V", use_qr=use_qr)
+            assert info == 0
+            assert np.abs(w - ws).max() <= 4 * n * 2.2e-16 * np.linalg.norm(A, 2)
+            assert residual(A, V, w) < 1e-13 and orth(V) < 1e-13
+
+
+def test_symtridiagonal_against_256bit():
+    # test/eigenselfadjoint.jl:5-32 (SymTridiagonal, QL default and QR version)
+    g = golden()["symtridiagonal"]
+    dv = np.array([float.fromhex(v) for v in g["dv"]])
+    ev = np.array([float.fromhex(v) for v in g["ev"]])
+    T = np.diag(dv) + np.diag(ev, 1) + np.diag(ev, -1)
+    w256 = np.array([float(mpmath.mpf(v)) for v in g["w"]])
+    nT = np.linalg.norm(T, 2)
+    for use_qr in (False, True):
+        w, V, info = O.stev(dv, ev, "V", use_qr=use_qr)
+        assert info == 0 and np.all(np.diff(w) >= 0)
+        assert np.abs(w - w256).max() <= 200 * 2.2e-16 * nT
+        assert residual(T, V, w) < 1e-13 and orth(V) < 1e-13
+        assert vec_parity(T, V, np.array(g["V"]), w256) <= 1.0
+    wp = O.stev(dv, ev, "N")[0]
+    wp256 = np.array([float(mpmath.mpf(v)) for v in g["w_pwk"]])
+    assert np.abs(wp - wp256).max() <= 200 * 2.2e-16 * nT
+    assert np.abs(wp - w).max() <= np.sqrt(2.2e-16) * nT
+
+
+def test_eigen2_rows_equal_full_vectors():
+    # test/eigenselfadjoint.jl:18-24: eigen2 rows == vecs[[1, n], :] exactly
+    g = golden()["symtridiagonal"]
+    dv = np.array([float.fromhex(v) for v in g["dv"]])
+    ev = np.array([float.fromhex(v) for v in g["ev"]])
+    n = len(dv)
+    d1, _, Vf, _ = O.eigql(dv, ev, np.eye(n))
+    V2 = np.zeros((2, n))
+    V2[0, 0] = 1
+    V2[1, n - 1] = 1
+    d2, _, Vp, _ = O.eigql(dv, ev, V2)
+    assert np.array_equal(d1, d2)
+    assert np.array_equal(Vf[[0, n - 1], :], Vp)
+
+
+def test_nonfinite_and_cap():
+    A = goe(6, 1)
+    A[3, 1] = np.nan
+    assert O.syev(A)[2] == -1
+    A[3, 1] = np.inf
+    assert O.syev(A, "N")[2] == -1
+    # the reference has no sweep cap; the oracle's cap reports the unconverged count
+    B = goe(20, 2)
+    w, V, info = O.syev(B, max_sweeps=0)
+    assert info > 0
+
+
+def test_batched_matches_single():
+    mats = [goe(n, 100 + n) for n in [1, 2, 5, 17, 64]]
+    ws, Vs, info = O.syev_batched(mats)
+    for A, w, V in zip(mats, ws, Vs):
+        w1, V1, _ = O.syev(A)
+        assert np.array_equal(w, w1) and np.array_equal(V, V1)
+    assert (info == 0).all()
