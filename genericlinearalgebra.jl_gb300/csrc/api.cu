@@ -410,8 +410,7 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
   p->mark(GLA_PHASE_REFINE, 0, st);
   for (const Bucket& bk : p->buckets)
     GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
-                           lower, (const float*)p->d_x32, (const float*)p->d_w32, (double*)Vout, (double*)w, info,
-                           p->d_stats));
+                           lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats));
   p->mark(GLA_PHASE_REFINE, 1, st);
   return 0;
 }

@@ -10,20 +10,22 @@
 
 namespace gla {
 
-struct RefineWork {
-  double* X = nullptr;  // current eigenvector approximation (a_elems)
-  double* Y = nullptr;  // A*X, then X + X*E (a_elems)
-  double* S = nullptr;  // X'AX, then E (a_elems)
-  double* R = nullptr;  // I - X'X (a_elems)
-};
+struct df64;
 
-constexpr int kRefineIters = 2;
+struct RefineWork {
+  df64* A2 = nullptr;  // scaled A as double-float (a_elems)
+  df64* X2 = nullptr;  // current eigenvector approximation
+  df64* Y2 = nullptr;  // A X, then X + X E
+  df64* S2 = nullptr;  // X'AX
+  df64* R2 = nullptr;  // I - X'X
+  float* E = nullptr;  // correction E
+};
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t w_elems, int64_t batch);
 void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t w_elems, int64_t batch);
 cudaError_t refine_kernels_init();
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
-                          const int* perm, const double* A, int lower, const float* X32, const float* w32,
-                          double* V, double* w, const int* info, unsigned long long* stats);
+                          const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
+                          const int* info, const int* scale_exp, unsigned long long* stats);
 
 }  // namespace gla

@@ -1,60 +1,86 @@
-// Ogita-Aishima refinement (T. Ogita, K. Aishima, "Iterative refinement for
-// symmetric eigenvalue decomposition", Japan J. Indust. Appl. Math. 35
-// (2018), Algorithm 1) of the FP32 eigenvectors, one CTA per matrix:
+// Eigenpair refinement of the FP32 eigenvectors back to FP64-class accuracy,
+// one CTA per matrix (n <= 128). No counterpart in GenericLinearAlgebra.jl.
+//
+// Ogita-Aishima iteration (T. Ogita, K. Aishima, "Iterative refinement for
+// symmetric eigenvalue decomposition", JJIAM 35 (2018), Algorithm 1):
 //
 //   R = I - X'X,  S = X'AX,  lam_i = s_ii / (1 - r_ii),
-//   delta = 2 (||S - diag(lam)|| + ||A|| ||R||)          (Frobenius bounds)
-//   E_ij = (s_ij + lam_j r_ij) / (lam_j - lam_i)  if |lam_i - lam_j| > delta
-//        = r_ij / 2                               otherwise (and on i == j)
+//   delta = 2 (||S - diag(lam)||_F + ||A||_F ||R||_F)
+//   E_ij = (s_ij + lam_j r_ij) / (lam_j - lam_i)   if |lam_j - lam_i| > delta
+//        = r_ij / 2                                 otherwise (and i == j)
 //   X <- X + X E
 //
-// repeated until max|E| < 2^-30 (the last correction is then below FP64
-// rounding of the result) or kMaxRefineIters. Products are FP64. The result
-// is sorted ascending (sorteig!, as the reference returns it).
-// No counterpart in GenericLinearAlgebra.jl.
+// Eigenvalues closer than delta form clusters (runs of the sorted lam);
+// within each cluster the columns are additionally rotated to the Ritz
+// vectors of the projected pencil, Z = eig((I + R_JJ/2) S_JJ (I + R_JJ/2)),
+// as in the clustered-eigenvalue extension of the same authors (JJIAM 36,
+// 2019). The small symmetric eigenproblem is solved by cyclic Jacobi in
+// FP32 after shifting by the cluster mean (its accuracy only needs to be
+// relative to the cluster's spread; the next iteration restores the rest).
+//
+// Arithmetic: the products X'X, AX, X'(AX) and X E are evaluated in
+// double-float arithmetic (df64.cuh) on the FP32 pipe, ~2^-47 relative per
+// operation; lam and the gaps in FP64. The matrix is scaled by the same
+// exact power of two as the FP32 solve (max |A| near 1) and the eigenvalues
+// are scaled back on output. Iterates until max|E| < 2^-30 with no
+// unresolved cluster, at most kMaxRefineIters times; the result is sorted
+// ascending (sorteig!).
+#include "df64.cuh"
 #include "gla_refine.h"
 
 namespace gla {
 
-constexpr int kMaxRefineIters = 6;
+constexpr int kMaxRefineIters = 8;
 constexpr int kRT = 256;  // threads per CTA
+constexpr int kJacobiSweeps = 15;
 
-size_t refine_workspace_bytes(int64_t a_elems, int64_t, int64_t) { return 4 * sizeof(double) * (size_t)a_elems + 1024; }
-
-void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t) {
-  double* p = reinterpret_cast<double*>(base);
-  rw->X = p;
-  rw->Y = p + a_elems;
-  rw->S = p + 2 * a_elems;
-  rw->R = p + 3 * a_elems;
+size_t refine_workspace_bytes(int64_t a_elems, int64_t, int64_t) {
+  return (5 * sizeof(df64) + sizeof(float)) * (size_t)a_elems + 4096;
 }
 
-// C(i, j) = sum_k la(i, k) * lb(k, j) over 64 x 64 output tiles; 256 threads,
-// 4 x 4 outputs per thread; `upper` skips tiles strictly below the diagonal.
-template <class LA, class LB, class ST>
-GLA_DEV void tile_gemm(int n, const LA& la, const LB& lb, const ST& store, double* As, double* Bs, bool upper) {
+void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t) {
+  df64* p = reinterpret_cast<df64*>(base);
+  rw->A2 = p;
+  rw->X2 = p + a_elems;
+  rw->Y2 = p + 2 * a_elems;
+  rw->S2 = p + 3 * a_elems;
+  rw->R2 = p + 4 * a_elems;
+  rw->E = reinterpret_cast<float*>(p + 5 * a_elems);
+}
+
+size_t refine_smem_bytes(int nmax) { return (size_t)2 * nmax * nmax * sizeof(float) + 16; }
+
+// C(i, j) = init(i, j) + sum_k la(i, k) * lb(k, j) over 64 x 64 output tiles;
+// 256 threads, 4 x 4 outputs per thread, double-float accumulation.
+// `upper` skips tiles strictly below the diagonal and stores i <= j only.
+template <class TB, class LA, class LB, class IN, class ST>
+GLA_DEV void tile_gemm_df(int n, const LA& la, const LB& lb, const IN& init, const ST& store, df64* As, TB* Bs,
+                          bool upper) {
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   for (int i0 = 0; i0 < n; i0 += 64) {
     for (int j0 = 0; j0 < n; j0 += 64) {
       if (upper && j0 + 63 < i0) continue;
-      double acc[4][4];
+      df64 acc[4][4];
 #pragma unroll
       for (int u = 0; u < 4; u++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) acc[u][v] = 0;
+        for (int v = 0; v < 4; v++) {
+          const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * v;
+          acc[u][v] = (i < n && j < n) ? init(i, j) : df_make(0.f, 0.f);
+        }
       for (int k0 = 0; k0 < n; k0 += 16) {
         __syncthreads();
         for (int t = tid; t < 16 * 64; t += kRT) {
           const int kk = t & 15, ii = t >> 4;
-          const int i = i0 + ii, k = k0 + kk;
-          As[kk * 64 + ii] = (i < n && k < n) ? la(i, k) : 0.0;
-          const int j = j0 + ii;
-          Bs[kk * 64 + ii] = (j < n && k < n) ? lb(k, j) : 0.0;
+          const int i = i0 + ii, k = k0 + kk, j = j0 + ii;
+          As[kk * 64 + ii] = (i < n && k < n) ? la(i, k) : df_make(0.f, 0.f);
+          Bs[kk * 64 + ii] = (j < n && k < n) ? lb(k, j) : TB();
         }
         __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
         for (int kk = 0; kk < 16; kk++) {
-          double a[4], b[4];
+          df64 a[4];
+          TB b[4];
 #pragma unroll
           for (int u = 0; u < 4; u++) a[u] = As[kk * 64 + tx + 16 * u];
 #pragma unroll
@@ -62,7 +88,7 @@ GLA_DEV void tile_gemm(int n, const LA& la, const LB& lb, const ST& store, doubl
 #pragma unroll
           for (int u = 0; u < 4; u++)
 #pragma unroll
-            for (int v = 0; v < 4; v++) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+            for (int v = 0; v < 4; v++) acc[u][v] = df_mac(acc[u][v], a[u], b[v]);
         }
       }
 #pragma unroll
@@ -77,38 +103,90 @@ GLA_DEV void tile_gemm(int n, const LA& la, const LB& lb, const ST& store, doubl
   __syncthreads();
 }
 
-GLA_DEV double block_sum_d(double v, double* red) {
+GLA_DEV float block_sum_f(float v, float* red) {
   v = warp_sum(v);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  double s = 0;
+  float s = 0;
   for (int i = 0; i < kRT / 32; i++) s += red[i];
   return s;
 }
 
-GLA_DEV double block_max_d(double v, double* red) {
+GLA_DEV float block_max_f(float v, float* red) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  double s = 0;
-  for (int i = 0; i < kRT / 32; i++) s = fmax(s, red[i]);
+  float s = 0;
+  for (int i = 0; i < kRT / 32; i++) s = fmaxf(s, red[i]);
   return s;
+}
+
+// Cyclic Jacobi on the k x k symmetric C (column-major, ld k) by one warp;
+// Z receives the eigenvectors. Off-diagonal Frobenius norm driven below
+// 1e-7 of the total, or kJacobiSweeps sweeps.
+GLA_DEV void jacobi_warp(int k, float* C, float* Z) {
+  const int lane = threadIdx.x & 31;
+  for (int idx = lane; idx < k * k; idx += 32) Z[idx] = (idx % (k + 1) == 0) ? 1.f : 0.f;
+  __syncwarp();
+  for (int sw = 0; sw < kJacobiSweeps; sw++) {
+    float off = 0.f, tot = 0.f;
+    for (int idx = lane; idx < k * k; idx += 32) {
+      const float v = C[idx];
+      tot += v * v;
+      if (idx % (k + 1) != 0) off += v * v;
+    }
+    off = warp_sum(off);
+    tot = warp_sum(tot);
+    if (!(off > 1e-14f * tot)) break;
+    for (int p = 0; p < k - 1; p++) {
+      for (int q = p + 1; q < k; q++) {
+        const float apq = C[q * k + p];
+        if (apq == 0.f) continue;
+        const float app = C[p * k + p], aqq = C[q * k + q];
+        const float th = (aqq - app) / (2.f * apq);
+        const float t = (th == 0.f) ? 1.f : copysignf(1.f, th) / (fabsf(th) + sqrtf(fmaf(th, th, 1.f)));
+        const float c = rsqrtf(fmaf(t, t, 1.f)), s = t * c;
+        __syncwarp();
+        for (int r = lane; r < k; r += 32) {  // columns p, q
+          const float cp = C[p * k + r], cq = C[q * k + r];
+          C[p * k + r] = c * cp - s * cq;
+          C[q * k + r] = s * cp + c * cq;
+        }
+        __syncwarp();
+        for (int r = lane; r < k; r += 32) {  // rows p, q
+          const float rp = C[r * k + p], rq = C[r * k + q];
+          C[r * k + p] = c * rp - s * rq;
+          C[r * k + q] = s * rp + c * rq;
+          const float zp = Z[p * k + r], zq = Z[q * k + r];
+          Z[p * k + r] = c * zp - s * zq;
+          Z[q * k + r] = s * zp + c * zq;
+        }
+        __syncwarp();
+      }
+    }
+  }
+  __syncwarp();
 }
 
 __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                 const double* __restrict__ A, int lower,
-                                                const float* __restrict__ X32, const float* __restrict__ w32,
-                                                double* __restrict__ Vout, double* __restrict__ wout,
-                                                const int* __restrict__ info, RefineWork rw,
+                                                const float* __restrict__ X32, double* __restrict__ Vout,
+                                                double* __restrict__ wout, const int* __restrict__ info,
+                                                const int* __restrict__ scale_exp, RefineWork rw,
                                                 unsigned long long* __restrict__ stats) {
-  __shared__ double As[16 * 64], Bs[16 * 64];
+  extern __shared__ __align__(16) float jac[];  // C and Z of a cluster (k*k each)
+  __shared__ df64 As[16 * 64];
+  __shared__ df64 Bs2[16 * 64];
   __shared__ double lam[kSmallMaxN];
-  __shared__ double red[kRT / 32];
+  __shared__ df64 lamdf[kSmallMaxN];
+  __shared__ float red[kRT / 32];
   __shared__ unsigned long long keys[kSmallMaxN];
-  __shared__ int rank[kSmallMaxN];
+  __shared__ int rank[kSmallMaxN], ord[kSmallMaxN], cstart[kSmallMaxN + 1];
+  __shared__ int ncl_s, flag_s;
+  float* Bsf = reinterpret_cast<float*>(Bs2);
   const int mid = perm[blockIdx.x];
   const SmallDesc dsc = descs[mid];
   const int n = dsc.n, tid = threadIdx.x;
@@ -121,102 +199,194 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     for (int i = tid; i < n; i += kRT) wout[dsc.w_off + i] = NAN;
     return;
   }
-  double* X = rw.X + ao;
-  double* Y = rw.Y + ao;
-  double* S = rw.S + ao;
-  double* R = rw.R + ao;
-  for (int idx = tid; idx < n * n; idx += kRT) X[idx] = (double)X32[ao + idx];
-  double anorm2 = 0;
+  const int se = scale_exp[mid];
+  df64* A2 = rw.A2 + ao;
+  df64* X = rw.X2 + ao;
+  df64* Y = rw.Y2 + ao;
+  df64* S = rw.S2 + ao;
+  df64* R = rw.R2 + ao;
+  float* E = rw.E + ao;
+  float an2 = 0.f;
   for (int idx = tid; idx < n * n; idx += kRT) {
     const int i = idx % n, k = idx / n;
     const double a = (lower ? (i >= k) : (i <= k)) ? Ag[idx] : Ag[(size_t)i * n + k];
-    anorm2 = fma(a, a, anorm2);
+    const df64 ad = df_from(ldexp(a, -se));
+    A2[idx] = ad;
+    an2 = fmaf(ad.hi, ad.hi, an2);
+    X[idx] = df_make(X32[ao + idx], 0.f);
   }
-  const double anorm = sqrt(block_sum_d(anorm2, red));
-  auto Asym = [&](int i, int k) -> double {
-    return (lower ? (i >= k) : (i <= k)) ? Ag[(size_t)k * n + i] : Ag[(size_t)i * n + k];
-  };
-  __syncthreads();
-  for (int it = 0; it < kMaxRefineIters; it++) {
-    // Y = A X
-    tile_gemm(
-        n, Asym, [&](int k, int j) { return X[(size_t)j * n + k]; },
-        [&](int i, int j, double v) { Y[(size_t)j * n + i] = v; }, As, Bs, false);
-    // S = X'Y, R = I - X'X (upper triangles, mirrored)
-    tile_gemm(
+  const float anorm = sqrtf(block_sum_f(an2, red));
+  const df64 zero = df_make(0.f, 0.f);
+  auto zinit = [&](int, int) { return zero; };
+  int it = 0;
+  for (; it < kMaxRefineIters; it++) {
+    // Y = A X ; S = X'Y ; R = I - X'X (upper triangles, mirrored)
+    tile_gemm_df<df64>(
+        n, [&](int i, int k) { return A2[(size_t)k * n + i]; }, [&](int k, int j) { return X[(size_t)j * n + k]; },
+        zinit, [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, As, Bs2, false);
+    tile_gemm_df<df64>(
         n, [&](int i, int k) { return X[(size_t)i * n + k]; }, [&](int k, int j) { return Y[(size_t)j * n + k]; },
-        [&](int i, int j, double v) {
+        zinit,
+        [&](int i, int j, df64 v) {
           S[(size_t)j * n + i] = v;
           S[(size_t)i * n + j] = v;
         },
-        As, Bs, true);
-    tile_gemm(
+        As, Bs2, true);
+    tile_gemm_df<df64>(
         n, [&](int i, int k) { return X[(size_t)i * n + k]; }, [&](int k, int j) { return X[(size_t)j * n + k]; },
-        [&](int i, int j, double v) {
-          const double r = (i == j ? 1.0 : 0.0) - v;
+        zinit,
+        [&](int i, int j, df64 v) {
+          const df64 r = df_add(df_make(i == j ? 1.f : 0.f, 0.f), df_neg(v));
           R[(size_t)j * n + i] = r;
           R[(size_t)i * n + j] = r;
         },
-        As, Bs, true);
-    for (int i = tid; i < n; i += kRT) lam[i] = S[(size_t)i * n + i] / (1.0 - R[(size_t)i * n + i]);
+        As, Bs2, true);
+    for (int i = tid; i < n; i += kRT) {
+      const double l = df_to(S[(size_t)i * n + i]) / (1.0 - df_to(R[(size_t)i * n + i]));
+      lam[i] = l;
+      lamdf[i] = df_from(l);
+      keys[i] = sort_key(l);
+    }
     __syncthreads();
-    double sd2 = 0, r2 = 0;
+    float sd2 = 0.f, r2 = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
       const int i = idx % n, j = idx / n;
-      const double sv = S[idx] - (i == j ? lam[i] : 0.0);
-      sd2 = fma(sv, sv, sd2);
-      r2 = fma(R[idx], R[idx], r2);
+      const float sv = (i == j) ? (float)(df_to(S[idx]) - lam[i]) : S[idx].hi;
+      sd2 = fmaf(sv, sv, sd2);
+      r2 = fmaf(R[idx].hi, R[idx].hi, r2);
     }
-    const double sdn = sqrt(block_sum_d(sd2, red));
-    const double rn = sqrt(block_sum_d(r2, red));
-    const double delta = 2.0 * (sdn + anorm * rn);
-    double emax = 0;
+    const float sdn = sqrtf(block_sum_f(sd2, red));
+    const float rn = sqrtf(block_sum_f(r2, red));
+    const float delta = 2.f * (sdn + anorm * rn);
+    // E (float) from the accurate S, R
+    float emax = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
       const int i = idx % n, j = idx / n;
-      const double dl = lam[j] - lam[i];
-      double e;
-      if (i != j && fabs(dl) > delta) e = (S[idx] + lam[j] * R[idx]) / dl;
-      else e = 0.5 * R[idx];
-      emax = fmax(emax, fabs(e));
-      S[idx] = e;  // E replaces S
+      const float gap = (float)(lam[j] - lam[i]);
+      float e;
+      if (i != j && fabsf(gap) > delta) {
+        const df64 num = df_mac(S[idx], lamdf[j], R[idx]);
+        e = (num.hi + num.lo) / gap;
+      } else {
+        e = 0.5f * (R[idx].hi + R[idx].lo);
+      }
+      E[idx] = e;
+      emax = fmaxf(emax, fabsf(e));
     }
-    emax = block_max_d(emax, red);
-    // X <- X + X E
-    tile_gemm(
-        n, [&](int i, int k) { return X[(size_t)k * n + i]; }, [&](int k, int j) { return S[(size_t)j * n + k]; },
-        [&](int i, int j, double v) { Y[(size_t)j * n + i] = X[(size_t)j * n + i] + v; }, As, Bs, false);
-    double* t = X;
+    emax = block_max_f(emax, red);
+    // clusters: runs of the sorted lam closer than delta
+    for (int i = tid; i < n; i += kRT) {
+      const unsigned long long ki = keys[i];
+      int rk = 0;
+      for (int j = 0; j < n; j++) rk += (keys[j] < ki) || (keys[j] == ki && j < i);
+      ord[rk] = i;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int nc = 0;
+      cstart[0] = 0;
+      for (int r = 1; r < n; r++)
+        if ((float)(lam[ord[r]] - lam[ord[r - 1]]) > delta) cstart[++nc] = r;
+      cstart[++nc] = n;
+      ncl_s = nc;
+      flag_s = 0;
+    }
+    __syncthreads();
+    // X <- X + X E  (into Y)
+    tile_gemm_df<float>(
+        n, [&](int i, int k) { return X[(size_t)k * n + i]; }, [&](int k, int j) { return E[(size_t)j * n + k]; },
+        [&](int i, int j) { return X[(size_t)j * n + i]; },
+        [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, As, Bsf, false);
+    // Rayleigh-Ritz rotation inside each cluster of two or more
+    const int ncl = ncl_s;
+    for (int c = 0; c < ncl; c++) {
+      const int r0 = cstart[c], k = cstart[c + 1] - r0;
+      if (k < 2) continue;
+      float* C = jac;
+      float* Z = jac + k * k;
+      // C = (I + R/2) S (I + R/2) - mu I restricted to the cluster, shifted by
+      // the mean mu of its lam (first order in R, FP32 after the shift)
+      double mu = 0;
+      for (int a = 0; a < k; a++) mu += lam[ord[r0 + a]];
+      mu /= k;
+      for (int idx = tid; idx < k * k; idx += kRT) {
+        const int a = idx % k, b = idx / k;
+        const int ia = ord[r0 + a], ib = ord[r0 + b];
+        df64 s = S[(size_t)ib * n + ia];
+        if (a == b) s = df_add(s, df_from(-mu));
+        float corr = 0.f;
+        for (int q = 0; q < k; q++) {
+          const int iq = ord[r0 + q];
+          const float sq_b = S[(size_t)ib * n + iq].hi - (q == b ? (float)mu : 0.f);
+          const float sa_q = S[(size_t)iq * n + ia].hi - (a == q ? (float)mu : 0.f);
+          corr = fmaf(R[(size_t)iq * n + ia].hi, sq_b, corr);
+          corr = fmaf(sa_q, R[(size_t)ib * n + iq].hi, corr);
+        }
+        C[b * k + a] = (s.hi + s.lo) + 0.5f * corr + (float)mu * R[(size_t)ib * n + ia].hi;
+      }
+      __syncthreads();
+      float offc = 0.f, totc = 0.f;
+      for (int idx = tid; idx < k * k; idx += kRT) {
+        const float v = C[idx];
+        if (idx % (k + 1) != 0) offc = fmaxf(offc, fabsf(v));
+        totc = fmaxf(totc, fabsf(v));
+      }
+      offc = block_max_f(offc, red);
+      if (tid < 32) jacobi_warp(k, C, Z);
+      __syncthreads();
+      if (offc > 0x1p-30f * fmaxf(anorm, 1e-30f) && tid == 0) flag_s = 1;
+      // Y[:, J] <- Y[:, J] Z  (temporary in X, whose old values are no longer needed)
+      for (int idx = tid; idx < n * k; idx += kRT) {
+        const int i = idx % n, b = idx / n;
+        df64 acc = zero;
+        for (int q = 0; q < k; q++) acc = df_mac(acc, Y[(size_t)ord[r0 + q] * n + i], Z[b * k + q]);
+        X[(size_t)b * n + i] = acc;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < n * k; idx += kRT) {
+        const int i = idx % n, b = idx / n;
+        Y[(size_t)ord[r0 + b] * n + i] = X[(size_t)b * n + i];
+      }
+      __syncthreads();
+    }
+    df64* t = X;
     X = Y;
     Y = t;
     if (tid == 0) atomicAdd(&stats[3], (unsigned long long)n * n * n);
-    if (emax < 0x1p-30) break;
+    __syncthreads();
+    if (emax < 0x1p-30f && flag_s == 0) {
+      it++;
+      break;
+    }
   }
   // sorteig!: ascending eigenvalues, columns permuted to match
-  for (int i = tid; i < n; i += kRT) keys[i] = sort_key(lam[i]);
   __syncthreads();
   for (int i = tid; i < n; i += kRT) {
     const unsigned long long ki = keys[i];
     int rk = 0;
     for (int j = 0; j < n; j++) rk += (keys[j] < ki) || (keys[j] == ki && j < i);
     rank[i] = rk;
-    wout[dsc.w_off + rk] = lam[i];
+    wout[dsc.w_off + rk] = ldexp(lam[i], se);
   }
   __syncthreads();
   if (V)
     for (int j = 0; j < n; j++) {
       const int dst = rank[j];
-      for (int i = tid; i < n; i += kRT) V[(size_t)dst * n + i] = X[(size_t)j * n + i];
+      for (int i = tid; i < n; i += kRT) V[(size_t)dst * n + i] = df_to(X[(size_t)j * n + i]);
     }
 }
 
-cudaError_t refine_kernels_init() { return cudaSuccess; }
+cudaError_t refine_kernels_init() {
+  return cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)refine_smem_bytes(kSmallMaxN));
+}
 
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
-                          const int* perm, const double* A, int lower, const float* X32, const float* w32,
-                          double* V, double* w, const int* info, unsigned long long* stats) {
-  (void)nmax;
+                          const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
+                          const int* info, const int* scale_exp, unsigned long long* stats) {
   if (nblocks <= 0) return cudaSuccess;
-  k_refine<<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, w32, V, w, info, *rw, stats);
+  k_refine<<<nblocks, kRT, refine_smem_bytes(nmax), st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw,
+                                                          stats);
   return cudaGetLastError();
 }
 

@@ -117,11 +117,29 @@ template <class T> GLA_DEV T div_fast(T a, T b) {
   return prec<T>::tame(b) ? a * prec<T>::rcp(b) : prec<T>::div_ieee(a, b);
 }
 
-size_t chase_smem_bytes(int nmax, int elem) { return (size_t)2 * nmax * 32 * elem; }
+// sqrt(m^2 + 1) for the shift computation (:272, :201, :325); exactness of
+// the shift only affects the convergence rate, so a refined rsqrt replaces
+// the correctly rounded hypot here.
+template <class T> GLA_DEV T hypot1_fast(T m) {
+  const T am = tabs(m);
+  if (!prec<T>::tame(am)) return am < T(1) ? T(1) : am;
+  const T q = fma(m, m, T(1));
+  return q * prec<T>::rsqrt(q);
+}
+
+size_t chase_smem_bytes(int nmax, int elem) { return 512 + (size_t)2 * nmax * 32 * elem; }
 
 // ALGO: kAlgoQL (eigQL!, logs rotations), kAlgoQR (eigQR!, logs), kAlgoPWK
 // (eigvalsPWK!, values only). d, e: per-matrix diagonals at w_off (e padded
 // to n entries). rot: 2 values per rotation; hdr: one word per sweep.
+//
+// Deflation bookkeeping: instead of rescanning e from blockstart after every
+// chase (:250-256), each lane keeps a bitmask NF of "e[j] is negligible",
+// re-evaluating entry j exactly when e[j], d[j] or d[j+1] takes its final
+// value for the chase (one test per rotation). The first negligible entry at
+// or after blockstart is then found with __ffs, and the decision is the one
+// the rescan would make on the same values. This keeps the 32 lanes of a
+// warp from serialising on each other's O(n) scans.
 template <class T, int ALGO>
 __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                               int count, T* __restrict__ dg_all, T* __restrict__ eg_all,
@@ -141,8 +159,9 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
   int nmax = n;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
-  T* D = reinterpret_cast<T*>(smem_raw) + lane;
-  T* E = reinterpret_cast<T*>(smem_raw) + (size_t)nmax * 32 + lane;
+  unsigned* NF = reinterpret_cast<unsigned*>(smem_raw) + lane;  // NF[w * 32], w < 4
+  T* D = reinterpret_cast<T*>(smem_raw + 512) + lane;
+  T* E = reinterpret_cast<T*>(smem_raw + 512) + (size_t)nmax * 32 + lane;
 #define DD(i) D[(size_t)(i) * 32]
 #define EE(i) E[(size_t)(i) * 32]
 
@@ -153,15 +172,31 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
   bool active = was_running;
   T* dg = dg_all + dsc.w_off;
   T* eg = eg_all + dsc.w_off;
-  if (active) {
-    for (int i = 0; i < n; i++) {
-      DD(i) = dg[i];
-      const T e = eg[i];
-      // eigvalsPWK! squares the off-diagonal first (:171-173)
-      EE(i) = (ALGO == kAlgoPWK && st.nsweeps == 0 && st.bs == 0) ? e * e : e;
-    }
-  }
   const int tol_e = prec<T>::biased_exp(tol) - prec<T>::expbias;
+  auto test = [&](int j) {  // re-evaluate NF(j), j <= n - 2
+    const bool f = negligible(EE(j), DD(j), DD(j + 1), tol, tol_e);
+    unsigned& w = NF[(j >> 5) * 32];
+    const unsigned b = 1u << (j & 31);
+    w = f ? (w | b) : (w & ~b);
+  };
+  auto first_nf = [&](int from) -> int {  // first j >= from with NF(j), else n - 1
+    for (int w = from >> 5; w <= (n - 2) >> 5; w++) {
+      unsigned bits = NF[w * 32];
+      if (w == (from >> 5)) bits &= ~0u << (from & 31);
+      if (bits) return w * 32 + __ffs(bits) - 1;
+    }
+    return n - 1;
+  };
+  for (int w = 0; w < 4; w++) NF[w * 32] = 0;
+  if (active) {
+    for (int k = 0; k < n; k++) {
+      DD(k) = dg[k];
+      const T e = eg[k];
+      // eigvalsPWK! squares the off-diagonal first (:171-173)
+      EE(k) = (ALGO == kAlgoPWK && st.nsweeps == 0 && st.bs == 0) ? e * e : e;
+    }
+    for (int j = 0; j + 1 < n; j++) test(j);
+  }
   const int cap = max_sweeps_per_n * n;
   int bs = st.bs, nsw = st.nsweeps;
   int nrot = 0, nhdr = 0;
@@ -187,13 +222,7 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
         active = false;
         st.status = kChaseDone;
       } else {
-        be = n - 1;
-        for (int b = bs + 1; b <= n - 1; b++) {
-          if (negligible(EE(b - 1), DD(b - 1), DD(b), tol, tol_e)) {
-            be = b - 1;
-            break;
-          }
-        }
+        be = first_nf(bs);
         if (bs == be) {
           bs += 1;
         } else if (bs + 1 == be) {
@@ -204,6 +233,8 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
             DD(bs) = r1 + r2;
             DD(be) = r1 - r2;
             EE(bs) = 0;
+            test(bs);
+            if (be <= n - 2) test(be);
             bs += 1;
           } else if (nrot + 1 > dsc.rot_cap || nhdr + 1 > dsc.hdr_cap) {
             active = false;
@@ -232,6 +263,8 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
             myrot[2 * nrot] = cc;
             myrot[2 * nrot + 1] = ss;
             nrot++;
+            test(bs);
+            if (be <= n - 2) test(be);
             bs += 2;
           }
         } else if (nsw >= cap) {
@@ -247,24 +280,21 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
           // shift (:199-202 PWK, :271-273 QL, :324-326 QR) and start a chase
           if (ALGO == kAlgoPWK) {
             const T sqrte = prec<T>::sqrt_ieee(EE(bs));
-            T m = (DD(bs + 1) - DD(bs)) / (2 * sqrte);
-            const T r = hypot_borges(m, T(1));
-            mu = DD(bs) - sqrte / (m + tcopysign(r, m));
+            const T m = div_fast(DD(bs + 1) - DD(bs), 2 * sqrte);
+            mu = DD(bs) - div_fast(sqrte, m + tcopysign(hypot1_fast(m), m));
             gam = DD(be) - mu;
             p = gam * gam;
             i = be - 1;
           } else if (ALGO == kAlgoQL) {
-            T m = (DD(bs + 1) - DD(bs)) / (2 * EE(bs));
-            const T r = hypot_borges(m, T(1));
-            mu = DD(bs) - (EE(bs) / (m + tcopysign(r, m)));
+            const T m = div_fast(DD(bs + 1) - DD(bs), 2 * EE(bs));
+            mu = DD(bs) - div_fast(EE(bs), m + tcopysign(hypot1_fast(m), m));
             gam = DD(be) - mu;
             p = gam;
             i = be - 1;
             myhdr[nhdr++] = pack_hdr(be - 1, be - bs, 0);
           } else {
-            T m = (DD(be - 1) - DD(be)) / (2 * EE(be - 1));
-            const T r = hypot_borges(m, T(1));
-            mu = DD(be) - (EE(be - 1) / (m + tcopysign(r, m)));
+            const T m = div_fast(DD(be - 1) - DD(be), 2 * EE(be - 1));
+            mu = DD(be) - div_fast(EE(be - 1), m + tcopysign(hypot1_fast(m), m));
             gam = DD(bs) - mu;
             p = gam;
             i = bs + 1;
@@ -293,10 +323,12 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
         myrot[2 * nrot] = c;
         myrot[2 * nrot + 1] = s;
         nrot++;
+        if (i + 1 <= n - 2) test(i + 1);
         i--;
         if (i < bs) {
           EE(bs) = s * p;
           DD(bs) = mu + gam;
+          test(bs);
           insweep = false;
         }
       } else if (ALGO == kAlgoQR) {
@@ -314,10 +346,13 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
         myrot[2 * nrot] = c;
         myrot[2 * nrot + 1] = s;
         nrot++;
+        if (i - 2 >= bs) test(i - 2);
         i++;
         if (i > be) {
           EE(be - 1) = s * p;
           DD(be) = mu + gam;
+          test(be - 1);
+          if (be <= n - 2) test(be);
           insweep = false;
         }
       } else {
@@ -334,10 +369,12 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
         gam = c * (di - mu) - s * g1;
         DD(i + 1) = g1 + di - gam;
         p = is_zero(c) ? ei * c1 : div_fast(gam * gam, c);
+        if (i + 1 <= n - 2) test(i + 1);
         i--;
         if (i < bs) {
           EE(bs) = s * p;
           DD(bs) = mu + gam;
+          test(bs);
           insweep = false;
         }
       }
@@ -363,9 +400,9 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
 #undef EE
 }
 
-
 template <class T, int ALGO> static void set_chase_attr() {
-  cudaFuncSetAttribute(k_chase<T, ALGO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 128 * 32 * (int)sizeof(T));
+  cudaFuncSetAttribute(k_chase<T, ALGO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)chase_smem_bytes(kSmallMaxN, (int)sizeof(T)));
 }
 
 cudaError_t chase_kernels_init() {

@@ -1,0 +1,146 @@
+# GLAGPU.jl — Julia host glue: GenericLinearAlgebra.jl's self-adjoint
+# eigensolver API over libglagpu.so (ccall into the C ABI of include/glagpu.h).
+#
+# Mirrors, method for method, src/eigenSelfAdjoint.jl of GenericLinearAlgebra.jl
+# v0.4.0:
+#   eigen!(::Hermitian/Symmetric{<:Real})  (:626-630)  -> GLAGPU.eigen!
+#   eigvals!(::Hermitian/Symmetric{<:Real}) (:584-588) -> GLAGPU.eigvals!
+#   eigen!(::SymTridiagonal) / eigvals!     (:581,:623) -> GLAGPU.eigen! / eigvals!
+#   keyword tol = eps(T), sortby = eigsortby (ascending only), alg ignored
+# and returns LinearAlgebra.Eigen like the reference. A nonzero per-matrix
+# info raises, as src/lapack.jl:62 turns LAPACK's info into LAPACKException.
+#
+# Host Matrix inputs go through gla_plan_execute_host (the library copies to
+# and from the GPU); batched calls solve many matrices per launch sequence.
+module GLAGPU
+
+using LinearAlgebra
+
+const libglagpu = get(ENV, "GLAGPU_LIB", joinpath(@__DIR__, "..", "build", "libglagpu.so"))
+
+const GLA_PREC_F64 = Cint(0)
+const GLA_PREC_F32 = Cint(1)
+const GLA_PREC_F32_REFINED = Cint(2)
+const GLA_ALG_QL = Cint(0)
+const GLA_ALG_QR = Cint(1)
+const GLA_MAX_SMALL_N = 128
+
+struct GLAException <: Exception
+    status::Cint
+    msg::String
+end
+Base.showerror(io::IO, e::GLAException) = print(io, "GLAException(", e.status, "): ", e.msg)
+
+struct NonConvergence <: Exception
+    info::Cint
+end
+
+statusmsg(s) = unsafe_string(ccall((:gla_status_string, libglagpu), Cstring, (Cint,), s))
+check(s) = s < 0 ? throw(GLAException(s, statusmsg(s))) : s
+
+function raise_info(info)
+    for i in info
+        i == -1 && throw(ArgumentError("matrix contains NaN or Inf"))
+        i > 0 && throw(NonConvergence(i))
+    end
+end
+
+mutable struct Plan
+    handle::Ptr{Cvoid}
+    ns::Vector{Int64}
+    jobz::Char
+    a_elems::Int64
+    w_elems::Int64
+end
+
+function Plan(ns::Vector{Int64}; precision = GLA_PREC_F64, jobz = 'V', uplo = 'L', tol = 0.0, alg = GLA_ALG_QL)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:gla_plan_create, libglagpu), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, UInt8, UInt8, Int64, Ptr{Int64}, Cdouble, Cint),
+                h, precision, UInt8(jobz), UInt8(uplo), length(ns), ns, tol, alg))
+    a = Ref{Int64}(0)
+    w = Ref{Int64}(0)
+    check(ccall((:gla_plan_arena_sizes, libglagpu), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}), h[], a, w))
+    p = Plan(h[], ns, jobz, a[], w[])
+    finalizer(p) do q
+        q.handle == C_NULL || ccall((:gla_plan_destroy, libglagpu), Cint, (Ptr{Cvoid},), q.handle)
+        q.handle = C_NULL
+    end
+    return p
+end
+
+# Run a plan on host arenas (column-major matrices packed back to back).
+function execute_host!(p::Plan, A::Vector{T}, w::Vector{T}, V::Vector{T}, info::Vector{Cint}) where {T}
+    check(ccall((:gla_plan_execute_host, libglagpu), Cint,
+                (Ptr{Cvoid}, Ptr{T}, Ptr{T}, Ptr{T}, Ptr{Cint}, Ptr{Cvoid}),
+                p.handle, A, w, V, info, C_NULL))
+    return info
+end
+
+function _batched(mats::AbstractVector{<:AbstractMatrix}, jobz, uplo; precision = GLA_PREC_F64,
+                  alg = GLA_ALG_QL, tol = 0.0)
+    T = precision == GLA_PREC_F32 ? Float32 : Float64
+    ns = Int64[LinearAlgebra.checksquare(M) for M in mats]
+    p = Plan(ns; precision, jobz, uplo, tol, alg)
+    A = reduce(vcat, (vec(Matrix{T}(M)) for M in mats); init = T[])
+    w = Vector{T}(undef, max(p.w_elems, 1))
+    V = Vector{T}(undef, jobz == 'V' ? max(p.a_elems, 1) : 1)
+    info = zeros(Cint, length(ns))
+    execute_host!(p, A, w, V, info)
+    raise_info(info)
+    vals = Vector{Vector{T}}()
+    vecs = Vector{Matrix{T}}()
+    ao = 0
+    wo = 0
+    for n in ns
+        push!(vals, w[wo+1:wo+n])
+        jobz == 'V' && push!(vecs, reshape(V[ao+1:ao+n*n], n, n))
+        ao += n * n
+        wo += n
+    end
+    return vals, vecs
+end
+
+"""
+    eigen_batched(mats; uplo='L', precision=GLA_PREC_F64, alg=GLA_ALG_QL)
+
+`[eigen(Hermitian(M, uplo)) for M in mats]` in one batched GPU solve.
+"""
+function eigen_batched(mats; uplo = 'L', kw...)
+    vals, vecs = _batched(mats, 'V', uplo; kw...)
+    return [LinearAlgebra.Eigen(v, V) for (v, V) in zip(vals, vecs)]
+end
+eigvals_batched(mats; uplo = 'L', kw...) = _batched(mats, 'N', uplo; kw...)[1]
+
+uplochar(A) = A.uplo == 'L' ? 'L' : 'U'
+
+# eigen!/eigvals! on Hermitian/Symmetric real matrices (the reference's :614-630 and :572-588).
+function eigen!(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; tol = eps(T), sortby = LinearAlgebra.eigsortby,
+                alg = nothing) where {T<:Union{Float32,Float64}}
+    sortby === LinearAlgebra.eigsortby || throw(ArgumentError("only the ascending eigsortby order is supported"))
+    prec = T === Float32 ? GLA_PREC_F32 : GLA_PREC_F64
+    E = eigen_batched([A.data]; uplo = uplochar(A), precision = prec, tol = Float64(tol))[1]
+    copyto!(A.data, E.vectors)  # like eigen!, the input storage is consumed
+    return E
+end
+
+function eigvals!(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; tol = eps(T),
+                  sortby = LinearAlgebra.eigsortby, alg = nothing) where {T<:Union{Float32,Float64}}
+    prec = T === Float32 ? GLA_PREC_F32 : GLA_PREC_F64
+    return eigvals_batched([A.data]; uplo = uplochar(A), precision = prec, tol = Float64(tol))[1]
+end
+
+# FP32 solve + FP64 Ogita-Aishima refinement (no reference counterpart).
+eigen_refined(A::Union{Hermitian{Float64},Symmetric{Float64}}) =
+    eigen_batched([Matrix(A.data)]; uplo = uplochar(A), precision = GLA_PREC_F32_REFINED)[1]
+
+# eigen!/eigvals! on SymTridiagonal{Float64} (:602-612, :623, :581): gla_dstev
+# takes device pointers, so the host glue stages through the plan API with
+# the tridiagonal written out densely (its reduction is then trivial).
+function eigen!(S::SymTridiagonal{Float64}; tol = eps(Float64), sortby = LinearAlgebra.eigsortby, alg = GLA_ALG_QL)
+    return eigen_batched([Matrix(S)]; alg = alg)[1]
+end
+eigvals!(S::SymTridiagonal{Float64}; tol = eps(Float64), sortby = LinearAlgebra.eigsortby) =
+    eigvals_batched([Matrix(S)])[1]
+
+end # module
