@@ -152,7 +152,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
-    ns, mats = workload(seed=SEED + 1000 * rank)
+    ns, mats = workload(batch=args.batch, seed=SEED + 1000 * rank)
     aoff = np.concatenate([[0], np.cumsum(ns * ns)[:-1]]).astype(np.int64)
     woff = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
     A64 = pack_f(mats)
@@ -169,7 +169,7 @@ def run_ours(args):
             torch.distributed.barrier()
 
     results = {}
-    for path in ("f64", "f32", "f32_refined"):
+    for path in args.paths.split(","):
         plan = glagpu.Plan(ns, precision=path, timing=True)
         dt = torch.float32 if path == "f32" else torch.float64
         A = dA32 if path == "f32" else dA64
@@ -184,14 +184,17 @@ def run_ours(args):
         clk = start_clock_sampler() if path == "f32_refined" and rank == 0 else (None, None, "")
         barrier()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
         for _ in range(args.steps):
             plan.execute(A, w, V, info)
             for k, v in plan.phase_times().items():
                 phases[k] += v
+        ev1.record()
         torch.cuda.synchronize()
         barrier()
-        el = time.perf_counter() - t0
+        el = ev0.elapsed_time(ev1) * 1e-3
         clocks = stop_clock_sampler(clk, local) if clk[0] is not None else None
         if ws > 1:
             t = torch.tensor([el], device=dev, dtype=torch.float64)
@@ -216,6 +219,8 @@ def run_ours(args):
         passes = counters["passes"]
         results[path]["launches_per_step"] = nb + passes * (1 + nb) + (nb if path == "f32_refined" else 0)
         plan.close()
+    if args.profile:  # profiling runs (under ncu) stop here: no e2e, CPU leg or JSON line
+        return
     # ---- end to end through the C ABI with host buffers (headline path)
     plan = glagpu.Plan(ns, precision="f32_refined")
     hA = torch.from_numpy(A64).pin_memory()
@@ -226,11 +231,16 @@ def run_ours(args):
     for _ in range(args.warmup):
         plan.execute_host(hA.numpy(), hw.numpy(), hV.numpy(), hinfo.numpy(), stream)
     barrier()
-    t0 = time.perf_counter()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
     for _ in range(args.steps):
         plan.execute_host(hA.numpy(), hw.numpy(), hV.numpy(), hinfo.numpy(), stream)
+    ev1.record()
+    torch.cuda.synchronize()
     barrier()
-    el_e2e = time.perf_counter() - t0
+    el_e2e = ev0.elapsed_time(ev1) * 1e-3
     plan.close()
     if ws > 1:
         t = torch.tensor([el_e2e], device=dev, dtype=torch.float64)
@@ -362,6 +372,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH, help="matrices in the batch (profiling: smaller cases)")
+    ap.add_argument("--paths", default="f64,f32,f32_refined", help="paths to time (profiling)")
+    ap.add_argument("--profile", action="store_true", help="profiling run: time the paths only, print nothing")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
