@@ -217,7 +217,8 @@ def run_ours(args):
         }
         nb = len(plan_buckets(ns))
         passes = counters["passes"]
-        results[path]["launches_per_step"] = nb + passes * (1 + nb) + (nb if path == "f32_refined" else 0)
+        # per bucket: tridiag, (chase + apply) per pass, refine
+        results[path]["launches_per_step"] = nb * (1 + 2 * passes + (1 if path == "f32_refined" else 0))
         plan.close()
     if args.profile:  # profiling runs (under ncu) stop here: no e2e, CPU leg or JSON line
         return
@@ -299,8 +300,8 @@ def run_ours(args):
 
 
 def plan_buckets(ns):
-    edges = [0, 32, 64, 96, 128]
-    return [i for i in range(4) if ((ns > edges[i]) & (ns <= edges[i + 1])).any()]
+    """Size buckets of width 16 that the plan creates (one stream each)."""
+    return [i for i in range(8) if ((ns > 16 * i) & (ns <= 16 * (i + 1))).any()]
 
 
 def cpu_baseline(ns, mats, budget_s=15.0):

@@ -41,6 +41,8 @@ constexpr int kRotPerN2 = 2;    // rotation-log capacity per pass, in units of n
 constexpr int kHdrPerN = 3;     // header-log capacity per pass, in units of n
 constexpr int kMaxSweepsPerN = 30;  // chase cap per matrix (src/eigenGeneral.jl:52 uses 30n)
 constexpr int kMaxPasses = 64;
+constexpr int kAsyncPasses = 2;     // chase passes enqueued without a host check
+constexpr int kMaxBuckets = 8;      // size buckets of width 16 over (0, 128]
 
 #define GLA_CUDA(x)                                  \
   do {                                               \
@@ -51,8 +53,10 @@ constexpr int kMaxPasses = 64;
 struct Bucket {
   int nmax;   // largest order in the bucket
   int nt;     // threads per CTA
-  int start;  // first index into perm_bucket
+  int start;  // first index into perm_bucket (orders descending inside the bucket)
   int count;
+  cudaStream_t stream = nullptr;  // the bucket's pipeline runs on its own stream
+  cudaEvent_t join = nullptr;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -83,15 +87,12 @@ struct gla_plan_s {
   int64_t a_elems = 0, w_elems = 0;
   int nwork = 0;  // matrices with n >= 1
   std::vector<Bucket> buckets;
-  int chase_count = 0;
-  int chase_nmax = 0;
   int nmax = 0;
   // device workspace
   char* ws = nullptr;
   size_t ws_bytes = 0;
   SmallDesc* d_desc = nullptr;
   int* d_perm_bucket = nullptr;
-  int* d_perm_chase = nullptr;
   void* d_d = nullptr;
   void* d_e = nullptr;
   void* d_rot = nullptr;
@@ -112,17 +113,16 @@ struct gla_plan_s {
   int* pin_pending = nullptr;
   cudaStream_t last_stream = nullptr;
   int last_passes = 0;
-  // phase timing (GLA_FLAG_TIMING): events[phase][0/1] per chase pass
+  cudaEvent_t fork = nullptr;
+  // phase timing (GLA_FLAG_TIMING): begin/end events per bucket and phase;
+  // a phase's time is the sum over buckets of its kernels' stream time
   bool timing = false;
-  static constexpr int kEv = 2 * GLA_NUM_PHASES * (kMaxPasses + 1);
-  cudaEvent_t ev[kEv] = {};
-  int nev[GLA_NUM_PHASES] = {};
-  void mark(int phase, int end, cudaStream_t st) {
-    if (!timing) return;
-    const int slot = nev[phase] / 2;
-    if (slot > kMaxPasses) return;
-    cudaEventRecord(ev[(phase * (kMaxPasses + 1) + slot) * 2 + end], st);
-    nev[phase]++;
+  cudaEvent_t tev[kMaxBuckets][GLA_NUM_PHASES][2] = {};
+  bool tused[kMaxBuckets][GLA_NUM_PHASES] = {};
+  void mark(int b, int phase, int end, cudaStream_t st) {
+    if (!timing || b >= kMaxBuckets) return;
+    cudaEventRecord(tev[b][phase][end], st);
+    if (end) tused[b][phase] = true;
   }
   int tcode() const { return prec == GLA_PREC_F64 ? kF64 : (prec == GLA_PREC_F32 ? kF32 : kF32FromF64); }
   size_t elem() const { return prec == GLA_PREC_F64 ? 8 : 4; }          // working element size
@@ -176,14 +176,6 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->batch = batch;
   p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? 0x1p-52 : (double)0x1p-23f);
   p->timing = (flags & GLA_FLAG_TIMING) != 0;
-  if (p->timing)
-    for (int i = 0; i < gla_plan_s::kEv; i++) {
-      cudaError_t e = cudaEventCreate(&p->ev[i]);
-      if (e != cudaSuccess) {
-        delete p;
-        return -1000 - (int)e;
-      }
-    }
   p->n.assign(n, n + batch);
 
   // ---- descriptors and offsets
@@ -216,15 +208,14 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->nwork = (int)idx.size();
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return n[a] > n[b]; });
   std::vector<int> perm_bucket;
-  const int edges[4] = {32, 64, 96, 128};
-  int lo = 0;
-  for (int ei = 0; ei < 4; ei++) {
+  for (int ei = kMaxBuckets - 1; ei >= 0; ei--) {  // largest orders first: longest pipelines start first
+    const int lo = 16 * ei, hi = 16 * (ei + 1);
     Bucket bk;
     bk.nmax = 0;
     bk.start = (int)perm_bucket.size();
     bk.count = 0;
     for (int b : idx) {
-      if (n[b] > lo && n[b] <= edges[ei]) {
+      if (n[b] > lo && n[b] <= hi) {
         perm_bucket.push_back(b);
         bk.count++;
         bk.nmax = std::max(bk.nmax, (int)n[b]);
@@ -232,11 +223,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     }
     bk.nt = std::max(32, (bk.nmax + 31) / 32 * 32);
     if (bk.count) p->buckets.push_back(bk);
-    lo = edges[ei];
   }
-  std::vector<int> perm_chase = idx;  // n >= 2 only need a chase, n == 1 too (trivially done)
-  p->chase_count = (int)perm_chase.size();
-  p->chase_nmax = p->nmax;
 
   // ---- workspace carve-up
   const size_t el = p->elem();
@@ -248,14 +235,13 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   };
   const size_t o_desc = carve(sizeof(SmallDesc) * batch);
   const size_t o_pb = carve(sizeof(int) * perm_bucket.size());
-  const size_t o_pc = carve(sizeof(int) * perm_chase.size());
   const size_t o_d = carve(el * woff);
   const size_t o_e = carve(el * woff);
   const bool wantvec = jobz == 'V' || precision == GLA_PREC_F32_REFINED;
   const size_t o_rot = carve(wantvec ? 2 * el * roff : 0);
   const size_t o_hdr = carve(wantvec ? sizeof(unsigned) * hoff : 0);
   const size_t o_cst = carve(sizeof(ChaseState) * batch);
-  const size_t o_pend = carve(sizeof(int) * 4);
+  const size_t o_pend = carve(sizeof(int) * kMaxBuckets);
   const size_t o_stats = carve(sizeof(unsigned long long) * 4);
   const size_t o_scale = carve(sizeof(int) * batch);
   const bool refined = precision == GLA_PREC_F32_REFINED;
@@ -273,7 +259,6 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   char* w = p->ws;
   p->d_desc = (SmallDesc*)(w + o_desc);
   p->d_perm_bucket = (int*)(w + o_pb);
-  p->d_perm_chase = (int*)(w + o_pc);
   p->d_d = w + o_d;
   p->d_e = w + o_e;
   p->d_rot = w + o_rot;
@@ -289,13 +274,19 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   if (batch) err = cudaMemcpy(p->d_desc, desc.data(), sizeof(SmallDesc) * batch, cudaMemcpyHostToDevice);
   if (err == cudaSuccess && !perm_bucket.empty())
     err = cudaMemcpy(p->d_perm_bucket, perm_bucket.data(), sizeof(int) * perm_bucket.size(), cudaMemcpyHostToDevice);
-  if (err == cudaSuccess && !perm_chase.empty())
-    err = cudaMemcpy(p->d_perm_chase, perm_chase.data(), sizeof(int) * perm_chase.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMemset(p->d_scale, 0, sizeof(int) * std::max<int64_t>(batch, 1));
-  if (err == cudaSuccess) err = cudaMallocHost((void**)&p->pin_pending, sizeof(int) * 4);
+  if (err == cudaSuccess) err = cudaMallocHost((void**)&p->pin_pending, sizeof(int) * kMaxBuckets);
+  if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+  for (Bucket& bk : p->buckets) {
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&bk.stream, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&bk.join, cudaEventDisableTiming);
+  }
+  if (p->timing)
+    for (int b = 0; b < kMaxBuckets && err == cudaSuccess; b++)
+      for (int ph = 0; ph < GLA_NUM_PHASES && err == cudaSuccess; ph++)
+        for (int k = 0; k < 2 && err == cudaSuccess; k++) err = cudaEventCreate(&p->tev[b][ph][k]);
   if (err != cudaSuccess) {
-    cudaFree(p->ws);
-    delete p;
+    gla_plan_destroy(p);
     return -1000 - (int)err;
   }
   *plan_out = p;
@@ -304,8 +295,15 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
 
 int gla_plan_destroy(gla_plan_t p) {
   if (!p) return -1;
-  if (p->timing)
-    for (int i = 0; i < gla_plan_s::kEv; i++) cudaEventDestroy(p->ev[i]);
+  for (Bucket& bk : p->buckets) {
+    if (bk.stream) cudaStreamDestroy(bk.stream);
+    if (bk.join) cudaEventDestroy(bk.join);
+  }
+  if (p->fork) cudaEventDestroy(p->fork);
+  for (int b = 0; b < kMaxBuckets; b++)
+    for (int ph = 0; ph < GLA_NUM_PHASES; ph++)
+      for (int k = 0; k < 2; k++)
+        if (p->tev[b][ph][k]) cudaEventDestroy(p->tev[b][ph][k]);
   cudaFree(p->ws);
   cudaFree(p->h_A);
   cudaFree(p->h_w);
@@ -334,84 +332,126 @@ int gla_plan_arena_sizes(gla_plan_t p, int64_t* a_elems, int64_t* w_elems) {
 
 namespace {
 
-// Chase passes + apply (vectors) for the working type; V holds Q on entry.
-int run_chase_apply(gla_plan_t p, int tcode, void* V, void* wout, int* info, const int* scale, cudaStream_t st) {
-  const size_t el = tcode == kF64 ? 8 : 4;
+// One chase pass (+ rotation replay, and the sort once a matrix is done) of
+// bucket b on stream st. V holds Q (or the previous pass's rotated Q).
+int enqueue_pass(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info, const int* scale,
+                 cudaStream_t st, bool timed = false) {
+  const Bucket& bk = p->buckets[b];
   const int work_t = tcode == kF64 ? kF64 : kF32;
-  const size_t chase_smem = chase_smem_bytes(p->chase_nmax, (int)el);
-  int passes = 0;
-  for (;;) {
-    GLA_CUDA(cudaMemsetAsync(p->d_pending, 0, sizeof(int), st));
-    p->mark(GLA_PHASE_CHASE, 0, st);
-    GLA_CUDA(launch_chase(work_t, p->algo, p->chase_count, chase_smem, st, p->d_desc, p->d_perm_chase, p->d_d,
-                          p->d_e, p->d_cst, p->d_rot, p->d_hdr, info, p->tol, kMaxSweepsPerN, p->d_pending,
-                          p->d_stats));
-    p->mark(GLA_PHASE_CHASE, 1, st);
-    p->mark(GLA_PHASE_APPLY, 0, st);
-    for (const Bucket& bk : p->buckets)
-      GLA_CUDA(launch_apply(work_t, bk.count, bk.nt, apply_smem_bytes(bk.nmax, (int)el), st, p->d_desc,
-                            p->d_perm_bucket + bk.start, V, p->d_d, wout, p->d_cst, p->d_rot, p->d_hdr, info,
-                            scale));
-    p->mark(GLA_PHASE_APPLY, 1, st);
-    passes++;
-    GLA_CUDA(cudaMemcpyAsync(p->pin_pending, p->d_pending, sizeof(int), cudaMemcpyDeviceToHost, st));
-    GLA_CUDA(cudaStreamSynchronize(st));
-    if (*p->pin_pending == 0 || passes >= kMaxPasses) break;
+  const int el = tcode == kF64 ? 8 : 4;
+  GLA_CUDA(cudaMemsetAsync(p->d_pending + b, 0, sizeof(int), st));
+  if (timed) p->mark(b, GLA_PHASE_CHASE, 0, st);
+  GLA_CUDA(launch_chase(work_t, p->algo, bk.count, chase_smem_bytes(bk.nmax, el), st, p->d_desc,
+                        p->d_perm_bucket + bk.start, p->d_d, p->d_e, p->d_cst, p->d_rot, p->d_hdr, info, p->tol,
+                        kMaxSweepsPerN, p->d_pending + b, p->d_stats));
+  if (timed) {
+    p->mark(b, GLA_PHASE_CHASE, 1, st);
+    p->mark(b, GLA_PHASE_APPLY, 0, st);
   }
-  p->last_passes = passes;
+  GLA_CUDA(launch_apply(work_t, bk.count, bk.nt, apply_smem_bytes(bk.nmax, el), st, p->d_desc,
+                        p->d_perm_bucket + bk.start, V, p->d_d, wout, p->d_cst, p->d_rot, p->d_hdr, info, scale));
+  if (timed) p->mark(b, GLA_PHASE_APPLY, 1, st);
   return 0;
 }
 
+// Chase passes until bucket b has no matrix left with a full rotation log
+// (host-checked; used by the single-matrix drivers and as the fallback).
+int run_passes_sync(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info, const int* scale,
+                    cudaStream_t st, int done_passes) {
+  int passes = done_passes;
+  for (;;) {
+    if (passes > 0) {
+      GLA_CUDA(cudaMemcpyAsync(p->pin_pending + b, p->d_pending + b, sizeof(int), cudaMemcpyDeviceToHost, st));
+      GLA_CUDA(cudaStreamSynchronize(st));
+      if (p->pin_pending[b] == 0 || passes >= kMaxPasses) break;
+    }
+    int rc = enqueue_pass(p, b, tcode, V, wout, info, scale, st);
+    if (rc) return rc;
+    passes++;
+  }
+  p->last_passes = std::max(p->last_passes, passes);
+  return 0;
+}
+
+int enqueue_refine(gla_plan_t p, int b, const void* A, int lower, void* Vout, void* w, int* info, cudaStream_t st) {
+  const Bucket& bk = p->buckets[b];
+  GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
+                         lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats));
+  return 0;
+}
+
+// Every size bucket runs its whole pipeline on its own stream (buckets are
+// independent), forked from and joined back into the caller's stream, so
+// the long chases of the largest matrices overlap with the other buckets.
 int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaStream_t st) {
   p->last_stream = st;
-  for (int i = 0; i < GLA_NUM_PHASES; i++) p->nev[i] = 0;
+  p->last_passes = 0;
+  for (int b = 0; b < kMaxBuckets; b++)
+    for (int ph = 0; ph < GLA_NUM_PHASES; ph++) p->tused[b][ph] = false;
   GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
   if (p->batch) GLA_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * p->batch, st));
   if (p->nwork == 0) return 0;
   const int lower = p->uplo == 'L';
+  const bool refined = p->prec == GLA_PREC_F32_REFINED;
+  const bool wantq = p->jobz == 'V' || refined;
   const int tc = p->tcode();
-  const size_t el = p->elem();
-  if (p->prec != GLA_PREC_F32_REFINED) {
-    const bool wantq = p->jobz == 'V';
-    p->mark(GLA_PHASE_TRIDIAG, 0, st);
-    for (const Bucket& bk : p->buckets)
-      GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt, tridiag_smem_bytes(bk.nmax, bk.nt, (int)el), st,
-                              p->d_desc, p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, V, info, p->d_cst,
-                              nullptr));
-    p->mark(GLA_PHASE_TRIDIAG, 1, st);
+  const int work_t = tc == kF64 ? kF64 : kF32;
+  const int el = (int)p->elem();
+  void* Q = refined ? p->d_x32 : V;
+  void* wq = refined ? p->d_w32 : w;
+  const int* scale = refined ? p->d_scale : nullptr;
+  void* Vout = p->jobz == 'V' ? V : p->d_vtmp;
+  const int nb = (int)p->buckets.size();
+  GLA_CUDA(cudaEventRecord(p->fork, st));
+  for (int b = 0; b < nb; b++) {
+    const Bucket& bk = p->buckets[b];
+    cudaStream_t s = bk.stream;
+    GLA_CUDA(cudaStreamWaitEvent(s, p->fork, 0));
+    p->mark(b, GLA_PHASE_TRIDIAG, 0, s);
+    GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt, tridiag_smem_bytes(bk.nmax, bk.nt, el), s, p->d_desc,
+                            p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, Q, info, p->d_cst, p->d_scale));
+    p->mark(b, GLA_PHASE_TRIDIAG, 1, s);
     if (wantq) {
-      int rc = run_chase_apply(p, tc, V, w, info, nullptr, st);
-      if (rc) return rc;
+      for (int k = 0; k < kAsyncPasses; k++) {  // the second pass only finishes overflowed logs
+        int rc = enqueue_pass(p, b, tc, Q, wq, info, scale, s, k == 0);
+        if (rc) return rc;
+      }
+      if (refined) {
+        p->mark(b, GLA_PHASE_REFINE, 0, s);
+        int rc = enqueue_refine(p, b, A, lower, Vout, w, info, s);
+        if (rc) return rc;
+        p->mark(b, GLA_PHASE_REFINE, 1, s);
+      }
+      GLA_CUDA(cudaMemcpyAsync(p->pin_pending + b, p->d_pending + b, sizeof(int), cudaMemcpyDeviceToHost, s));
     } else {
-      p->mark(GLA_PHASE_CHASE, 0, st);
-      GLA_CUDA(launch_chase(tc, kAlgoPWK, p->chase_count, chase_smem_bytes(p->chase_nmax, (int)el), st, p->d_desc,
-                            p->d_perm_chase, p->d_d, p->d_e, p->d_cst, nullptr, nullptr, info, p->tol,
-                            kMaxSweepsPerN, p->d_pending, p->d_stats));
-      p->mark(GLA_PHASE_CHASE, 1, st);
-      p->mark(GLA_PHASE_APPLY, 0, st);
-      for (const Bucket& bk : p->buckets)
-        GLA_CUDA(launch_sort_values(tc, bk.count, st, p->d_desc, p->d_perm_bucket + bk.start, p->d_d, w, info,
-                                    nullptr));
-      p->mark(GLA_PHASE_APPLY, 1, st);
-      p->last_passes = 1;
+      p->mark(b, GLA_PHASE_CHASE, 0, s);
+      GLA_CUDA(launch_chase(work_t, kAlgoPWK, bk.count, chase_smem_bytes(bk.nmax, el), s, p->d_desc,
+                            p->d_perm_bucket + bk.start, p->d_d, p->d_e, p->d_cst, nullptr, nullptr, info, p->tol,
+                            kMaxSweepsPerN, p->d_pending + b, p->d_stats));
+      GLA_CUDA(launch_sort_values(work_t, bk.count, s, p->d_desc, p->d_perm_bucket + bk.start, p->d_d, w, info,
+                                  nullptr));
+      p->mark(b, GLA_PHASE_CHASE, 1, s);
     }
+    GLA_CUDA(cudaEventRecord(bk.join, s));
+    GLA_CUDA(cudaStreamWaitEvent(st, bk.join, 0));
+  }
+  if (!wantq) {
+    p->last_passes = 1;
     return 0;
   }
-  // ---- FP32 solve on the 2^-s scaled matrix, then FP64 refinement
-  p->mark(GLA_PHASE_TRIDIAG, 0, st);
-  for (const Bucket& bk : p->buckets)
-    GLA_CUDA(launch_tridiag(kF32FromF64, true, bk.count, bk.nt, tridiag_smem_bytes(bk.nmax, bk.nt, 4), st,
-                            p->d_desc, p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, p->d_x32, info,
-                            p->d_cst, p->d_scale));
-  p->mark(GLA_PHASE_TRIDIAG, 1, st);
-  int rc = run_chase_apply(p, kF32FromF64, p->d_x32, p->d_w32, info, p->d_scale, st);
-  if (rc) return rc;
-  void* Vout = p->jobz == 'V' ? V : p->d_vtmp;
-  p->mark(GLA_PHASE_REFINE, 0, st);
-  for (const Bucket& bk : p->buckets)
-    GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
-                           lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats));
-  p->mark(GLA_PHASE_REFINE, 1, st);
+  // A matrix whose rotation log filled up in both asynchronous passes (never
+  // seen on random spectra with the 2 n^2 capacity) is finished here.
+  GLA_CUDA(cudaStreamSynchronize(st));
+  p->last_passes = kAsyncPasses;
+  for (int b = 0; b < nb; b++) {
+    if (p->pin_pending[b] == 0) continue;
+    int rc = run_passes_sync(p, b, tc, Q, wq, info, scale, st, kAsyncPasses);
+    if (rc) return rc;
+    if (refined) {
+      rc = enqueue_refine(p, b, A, lower, Vout, w, info, st);
+      if (rc) return rc;
+    }
+  }
   return 0;
 }
 
@@ -462,14 +502,13 @@ int gla_plan_phase_times(gla_plan_t p, float* ms) {
   for (int ph = 0; ph < GLA_NUM_PHASES; ph++) ms[ph] = 0.f;
   if (!p->timing) return 0;
   GLA_CUDA(cudaStreamSynchronize(p->last_stream));
-  for (int ph = 0; ph < GLA_NUM_PHASES; ph++) {
-    for (int slot = 0; slot < p->nev[ph] / 2; slot++) {
+  for (int b = 0; b < kMaxBuckets; b++)
+    for (int ph = 0; ph < GLA_NUM_PHASES; ph++) {
+      if (!p->tused[b][ph]) continue;
       float t = 0.f;
-      const int base = (ph * (kMaxPasses + 1) + slot) * 2;
-      GLA_CUDA(cudaEventElapsedTime(&t, p->ev[base], p->ev[base + 1]));
+      GLA_CUDA(cudaEventElapsedTime(&t, p->tev[b][ph][0], p->tev[b][ph][1]));
       ms[ph] += t;
     }
-  }
   return 0;
 }
 
@@ -603,12 +642,13 @@ int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz
   GLA_CUDA(launch_init_tridiagonal(kF64, 1, st, p->d_desc, p->d_perm_bucket, d, epad, p->d_d, p->d_e, buf,
                                    ent->dinfo, p->d_cst, jobz == 'V'));
   if (jobz == 'V') {
-    rc = run_chase_apply(p, kF64, buf, d, ent->dinfo, nullptr, st);
+    p->last_passes = 0;
+    rc = run_passes_sync(p, 0, kF64, buf, d, ent->dinfo, nullptr, st, 0);
     if (rc) return rc;
     GLA_CUDA(cudaMemcpy2DAsync(Z, sizeof(double) * ldz, buf, sizeof(double) * n, sizeof(double) * n, n,
                                cudaMemcpyDeviceToDevice, st));
   } else {
-    GLA_CUDA(launch_chase(kF64, kAlgoPWK, 1, chase_smem_bytes((int)n, 8), st, p->d_desc, p->d_perm_chase, p->d_d,
+    GLA_CUDA(launch_chase(kF64, kAlgoPWK, 1, chase_smem_bytes((int)n, 8), st, p->d_desc, p->d_perm_bucket, p->d_d,
                           p->d_e, p->d_cst, nullptr, nullptr, ent->dinfo, p->tol, kMaxSweepsPerN, p->d_pending,
                           p->d_stats));
     GLA_CUDA(launch_sort_values(kF64, 1, st, p->d_desc, p->d_perm_bucket, p->d_d, d, ent->dinfo, nullptr));

@@ -19,6 +19,7 @@ struct RefineWork {
   df64* S2 = nullptr;  // X'AX
   df64* R2 = nullptr;  // I - X'X
   float* E = nullptr;  // correction E
+  float* J = nullptr;  // Jacobi scratch of cluster rotations (2 * a_elems)
 };
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t w_elems, int64_t batch);

@@ -22,9 +22,10 @@
 // double-float arithmetic (df64.cuh) on the FP32 pipe, ~2^-47 relative per
 // operation; lam and the gaps in FP64. The matrix is scaled by the same
 // exact power of two as the FP32 solve (max |A| near 1) and the eigenvalues
-// are scaled back on output. Iterates until max|E| < 2^-30 with no
-// unresolved cluster, at most kMaxRefineIters times; the result is sorted
-// ascending (sorteig!).
+// are scaled back on output. Iterates until the predicted next correction
+// max|E|^2 ||A||_2 / gap_min (||A||_2 = max|lam|) falls below 1e-14 with no
+// unresolved cluster, at
+// most kMaxRefineIters times; the result is sorted ascending (sorteig!).
 #include "df64.cuh"
 #include "gla_refine.h"
 
@@ -35,7 +36,7 @@ constexpr int kRT = 256;  // threads per CTA
 constexpr int kJacobiSweeps = 15;
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t, int64_t) {
-  return (5 * sizeof(df64) + sizeof(float)) * (size_t)a_elems + 4096;
+  return (5 * sizeof(df64) + 3 * sizeof(float)) * (size_t)a_elems + 4096;
 }
 
 void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t) {
@@ -46,9 +47,8 @@ void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t)
   rw->S2 = p + 3 * a_elems;
   rw->R2 = p + 4 * a_elems;
   rw->E = reinterpret_cast<float*>(p + 5 * a_elems);
+  rw->J = rw->E + a_elems;
 }
-
-size_t refine_smem_bytes(int nmax) { return (size_t)2 * nmax * nmax * sizeof(float) + 16; }
 
 // C(i, j) = init(i, j) + sum_k la(i, k) * lb(k, j) over 64 x 64 output tiles;
 // 256 threads, 4 x 4 outputs per thread, double-float accumulation.
@@ -177,7 +177,6 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
                                                 double* __restrict__ wout, const int* __restrict__ info,
                                                 const int* __restrict__ scale_exp, RefineWork rw,
                                                 unsigned long long* __restrict__ stats) {
-  extern __shared__ __align__(16) float jac[];  // C and Z of a cluster (k*k each)
   __shared__ df64 As[16 * 64];
   __shared__ df64 Bs2[16 * 64];
   __shared__ double lam[kSmallMaxN];
@@ -186,6 +185,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   __shared__ unsigned long long keys[kSmallMaxN];
   __shared__ int rank[kSmallMaxN], ord[kSmallMaxN], cstart[kSmallMaxN + 1];
   __shared__ int ncl_s, flag_s;
+  __shared__ double gmin_s, lmax_s;
   float* Bsf = reinterpret_cast<float*>(Bs2);
   const int mid = perm[blockIdx.x];
   const SmallDesc dsc = descs[mid];
@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   df64* S = rw.S2 + ao;
   df64* R = rw.R2 + ao;
   float* E = rw.E + ao;
+  float* jac = rw.J + 2 * ao;  // C and Z of a cluster (k*k each), k <= n
   float an2 = 0.f;
   for (int idx = tid; idx < n * n; idx += kRT) {
     const int i = idx % n, k = idx / n;
@@ -284,12 +285,20 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     __syncthreads();
     if (tid == 0) {
       int nc = 0;
+      double gmin = 1e300;
+      lmax_s = fmax(fabs(lam[ord[0]]), fabs(lam[ord[n - 1]]));  // ||A||_2 of the scaled matrix
       cstart[0] = 0;
-      for (int r = 1; r < n; r++)
-        if ((float)(lam[ord[r]] - lam[ord[r - 1]]) > delta) cstart[++nc] = r;
+      for (int r = 1; r < n; r++) {
+        const double g = lam[ord[r]] - lam[ord[r - 1]];
+        if ((float)g > delta) {
+          cstart[++nc] = r;
+          gmin = fmin(gmin, g);
+        }
+      }
       cstart[++nc] = n;
       ncl_s = nc;
       flag_s = 0;
+      gmin_s = gmin;
     }
     __syncthreads();
     // X <- X + X E  (into Y)
@@ -354,7 +363,9 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     Y = t;
     if (tid == 0) atomicAdd(&stats[3], (unsigned long long)n * n * n);
     __syncthreads();
-    if (emax < 0x1p-30f && flag_s == 0) {
+    // the next correction would be about emax^2 ||A|| / gap (quadratic
+    // convergence): stop when that is below 1e-14 and no cluster is unresolved
+    if (flag_s == 0 && (double)emax * emax * lmax_s < 1e-14 * gmin_s) {
       it++;
       break;
     }
@@ -376,16 +387,14 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     }
 }
 
-cudaError_t refine_kernels_init() {
-  return cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)refine_smem_bytes(kSmallMaxN));
-}
+cudaError_t refine_kernels_init() { return cudaSuccess; }
 
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
                           const int* info, const int* scale_exp, unsigned long long* stats) {
   if (nblocks <= 0) return cudaSuccess;
-  k_refine<<<nblocks, kRT, refine_smem_bytes(nmax), st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw,
+  (void)nmax;
+  k_refine<<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw,
                                                           stats);
   return cudaGetLastError();
 }

@@ -20,8 +20,9 @@ namespace gla {
 constexpr int kRotChunk = 512;
 
 size_t apply_smem_bytes(int n, int elem) {
-  // S[n*(n+1)] | rotation chunk (2*kRotChunk) | keys (u64, n) | rank (int, n)
-  return (size_t)elem * ((size_t)n * (n + 1) + 2 * kRotChunk) + 8 * (size_t)n + 4 * (size_t)n + 16;
+  // S[n*(n+1)] | rotation chunk (2*kRotChunk) | keys (u64, n) | rank (int, n) | headers (3n+4)
+  return (size_t)elem * ((size_t)n * (n + 1) + 2 * kRotChunk) + 8 * (size_t)n + 4 * (size_t)n +
+         4 * (3 * (size_t)n + 4) + 16;
 }
 
 // V: Q in (from k_tridiag or a previous pass) and the rotated, sorted
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ des
   ChaseState st = cst[mid];
   if (st.applied) return;
   const bool done = st.status == kChaseDone;
-  if (!done && st.nhdr == 0) return;
+  if (!done && st.nhdr == 0) return;  // nothing logged for this matrix in this pass
   const int n = dsc.n, ld = n + 1;
   const int tid = threadIdx.x, NT = blockDim.x;
   T* S = reinterpret_cast<T*>(smem_raw);
@@ -62,42 +63,45 @@ __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ des
     for (int i = tid; i < n; i += NT) S[(size_t)j * ld + i] = Vg[(size_t)j * n + i];
   __syncthreads();
 
-  // ---- replay this pass's rotations
+  // ---- replay this pass's rotations: whole sweeps per staged chunk
   const T* myrot = rot + 2 * dsc.rot_off;
-  const unsigned* myhdr = hdr + dsc.hdr_off;
-  const int nrot = st.nrot;
+  unsigned* hs = reinterpret_cast<unsigned*>(rank + n);
+  const int nhdr = st.nhdr;
+  for (int h = tid; h < nhdr; h += NT) hs[h] = hdr[dsc.hdr_off + h];
   const int r = tid;
   const bool row = r < n;
   T* Sr = S + r;
-  int h = 0, k = 0, start = 0, cnt = 0, dir = 1;
-  T carry = 0;
-  for (int q0 = 0; q0 < nrot; q0 += kRotChunk) {
-    const int q1 = min(nrot, q0 + kRotChunk);
+  int h = 0, q0 = 0;
+  while (h < nhdr) {
+    // sweeps [h, h2) whose rotations fit in the chunk (a sweep has < n <= kRotChunk)
     __syncthreads();
-    for (int q = q0 * 2 + tid; q < q1 * 2; q += NT) buf[q - q0 * 2] = myrot[q];
+    int h2 = h, tot = 0;
+    while (h2 < nhdr && tot + hdr_count(hs[h2]) <= kRotChunk) tot += hdr_count(hs[h2++]);
+    for (int q = tid; q < 2 * tot; q += NT) buf[q] = myrot[2 * q0 + q];
     __syncthreads();
-    for (int q = q0; q < q1; q++) {
-      if (k == 0) {
-        const unsigned hw = myhdr[h];
-        start = hdr_start(hw);
-        cnt = hdr_count(hw);
-        dir = hdr_up(hw) ? -1 : 1;
-        if (row) carry = Sr[(size_t)(start + dir) * ld];
-      }
-      const int i = start - dir * k;
-      const T c = buf[2 * (q - q0)], s = buf[2 * (q - q0) + 1];
-      if (row) {
-        const T v = Sr[(size_t)i * ld];
-        Sr[(size_t)(i + dir) * ld] = fma(c, carry, s * v);
-        carry = fma(c, v, -(s * carry));
-      }
-      k++;
-      if (k == cnt) {
-        if (row) Sr[(size_t)i * ld] = carry;
-        h++;
-        k = 0;
+    if (row) {
+      const T* cs = buf;
+      for (int hh = h; hh < h2; hh++) {
+        const unsigned hw = hs[hh];
+        const int start = hdr_start(hw), cnt = hdr_count(hw);
+        const int dir = hdr_up(hw) ? -1 : 1;
+        T carry = Sr[(size_t)(start + dir) * ld];
+        int i = start;
+        T v = Sr[(size_t)i * ld];
+        for (int k = 0; k < cnt; k++) {
+          const T c = cs[2 * k], sn = cs[2 * k + 1];
+          const T vnext = (k + 1 < cnt) ? Sr[(size_t)(i - dir) * ld] : T(0);
+          Sr[(size_t)(i + dir) * ld] = fma(c, carry, sn * v);
+          carry = fma(c, v, -(sn * carry));
+          v = vnext;
+          i -= dir;
+        }
+        Sr[(size_t)(i + dir) * ld] = carry;
+        cs += 2 * cnt;
       }
     }
+    q0 += tot;
+    h = h2;
   }
   __syncthreads();
 

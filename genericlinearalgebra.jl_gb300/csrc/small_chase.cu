@@ -117,6 +117,25 @@ template <class T> GLA_DEV T div_fast(T a, T b) {
   return prec<T>::tame(b) ? a * prec<T>::rcp(b) : prec<T>::div_ieee(a, b);
 }
 
+// gamma / c of the QL/QR recurrence. FP32: the hardware reciprocal
+// (rcp.approx, ~1 ulp) without refinement, an error of the size of one
+// rounding in the recurrence; FP64: the Newton-refined reciprocal.
+GLA_DEV float div_chase(float a, float b) {
+  if (!prec<float>::tame(b)) return __fdiv_rn(a, b);
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(b));
+  return a * y;
+}
+GLA_DEV double div_chase(double a, double b) { return div_fast(a, b); }
+
+// Append (c, s) to the rotation log as one 8- or 16-byte store.
+GLA_DEV void store_rot(float* log, int k, float c, float s) {
+  reinterpret_cast<float2*>(log)[k] = make_float2(c, s);
+}
+GLA_DEV void store_rot(double* log, int k, double c, double s) {
+  reinterpret_cast<double2*>(log)[k] = make_double2(c, s);
+}
+
 // sqrt(m^2 + 1) for the shift computation (:272, :201, :325); exactness of
 // the shift only affects the convergence rate, so a refined rsqrt replaces
 // the correctly rounded hypot here.
@@ -146,11 +165,13 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
                                               ChaseState* __restrict__ cst, T* __restrict__ rot,
                                               unsigned* __restrict__ hdr, int* __restrict__ info, T tol,
                                               int max_sweeps_per_n, int* __restrict__ pending,
-                                              unsigned long long* __restrict__ stats) {
+                                              unsigned long long* __restrict__ stats, int lanes_per_warp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x;
-  const int slot = blockIdx.x * 32 + lane;
-  const bool have = slot < count;
+  // lanes_per_warp matrices per warp (the other lanes idle): fewer lanes cut
+  // the divergence between lanes that are between sweeps and lanes inside one
+  const int slot = blockIdx.x * lanes_per_warp + lane;
+  const bool have = lane < lanes_per_warp && slot < count;
   const int mid = have ? perm[slot] : 0;
   SmallDesc dsc;
   dsc.n = 0;
@@ -205,6 +226,15 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
   bool insweep = false, stopped_full = false;
   int i = 0, be = 0;
   T mu = 0, gam = 0, p = 0, c = 1, s = 0;
+  // register cache of the sweep: next (e, d) to consume, the d two positions
+  // behind (for the deflation test) and e beyond the block end
+  T e_nx = 0, d_nx = 0, d_up = 0, e_end = 0;
+  auto test_v = [&](int j, T ev, T d1, T d2) {  // NF(j) from register values
+    const bool f = negligible(ev, d1, d2, tol, tol_e);
+    unsigned& w = NF[(j >> 5) * 32];
+    const unsigned b = 1u << (j & 31);
+    w = f ? (w | b) : (w & ~b);
+  };
   int iters = 0;
   const int iter_cap = (max_sweeps_per_n + 4) * 4 * nmax * nmax + 64;  // hard bound on loop trips
 
@@ -300,6 +330,16 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
             i = bs + 1;
             myhdr[nhdr++] = pack_hdr(bs + 1, be - bs, 1);
           }
+          if (ALGO == kAlgoQR) {
+            e_nx = EE(bs);
+            d_nx = DD(bs + 1);
+            d_up = DD(bs);  // d[i-2] of the first test (unused: j < bs)
+          } else {
+            e_nx = EE(be - 1);
+            d_nx = DD(be - 1);
+            d_up = (be + 1 <= n - 1) ? DD(be + 1) : T(0);
+            e_end = (be <= n - 2) ? EE(be) : T(0);
+          }
           c = 1;
           s = 0;
           insweep = true;
@@ -309,72 +349,94 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
     }
     if (active && insweep) {
       if (ALGO == kAlgoQL) {
-        // singleShiftQL! step at i (:389-405)
-        const T ei = EE(i);
+        // singleShiftQL! step at i (:389-405), operands from registers
+        const T ei = e_nx, di = d_nx;
+        if (i > bs) {
+          e_nx = EE(i - 1);
+          d_nx = DD(i - 1);
+        }
         const T c1 = c, s1 = s;
         T zeta;
         givens(p, ei, c, s, zeta);
-        if (i < be - 1) EE(i + 1) = s1 * zeta;
-        const T di = DD(i);
+        const T enew = (i < be - 1) ? s1 * zeta : e_end;
+        if (i < be - 1) EE(i + 1) = enew;
         const T g1 = gam;
         gam = c * c * (di - mu) - s * s * g1;
-        DD(i + 1) = g1 + di - gam;
-        p = is_zero(c) ? -ei * c1 : div_fast(gam, c);
-        myrot[2 * nrot] = c;
-        myrot[2 * nrot + 1] = s;
+        const T dnew = g1 + di - gam;
+        DD(i + 1) = dnew;
+        p = is_zero(c) ? -ei * c1 : div_chase(gam, c);
+        store_rot(myrot, nrot, c, s);
         nrot++;
-        if (i + 1 <= n - 2) test(i + 1);
+        if (i + 1 <= n - 2) test_v(i + 1, enew, dnew, d_up);
+        d_up = dnew;
         i--;
         if (i < bs) {
-          EE(bs) = s * p;
-          DD(bs) = mu + gam;
-          test(bs);
+          const T eb = s * p, db = mu + gam;
+          EE(bs) = eb;
+          DD(bs) = db;
+          test_v(bs, eb, db, d_up);
           insweep = false;
         }
       } else if (ALGO == kAlgoQR) {
-        // singleShiftQR! step at i (:424-440)
-        const T ei = EE(i - 1);
+        // singleShiftQR! step at i (:424-440), operands from registers;
+        // d_up holds d[i-2] (the previous step's new d)
+        const T ei = e_nx, di = d_nx;
+        if (i < be) {
+          e_nx = EE(i);
+          d_nx = DD(i + 1);
+        }
         const T c1 = c, s1 = s;
         T zeta;
         givens(p, ei, c, s, zeta);
-        if (i > bs + 1) EE(i - 2) = s1 * zeta;
-        const T di = DD(i);
         const T g1 = gam;
         gam = c * c * (di - mu) - s * s * g1;
-        DD(i - 1) = g1 + di - gam;
-        p = is_zero(c) ? -ei * c1 : div_fast(gam, c);
-        myrot[2 * nrot] = c;
-        myrot[2 * nrot + 1] = s;
+        const T dnew = g1 + di - gam;
+        DD(i - 1) = dnew;
+        if (i > bs + 1) {
+          const T enew = s1 * zeta;
+          EE(i - 2) = enew;
+          test_v(i - 2, enew, d_up, dnew);
+        }
+        p = is_zero(c) ? -ei * c1 : div_chase(gam, c);
+        store_rot(myrot, nrot, c, s);
         nrot++;
-        if (i - 2 >= bs) test(i - 2);
+        d_up = dnew;
         i++;
         if (i > be) {
-          EE(be - 1) = s * p;
-          DD(be) = mu + gam;
-          test(be - 1);
+          const T eb = s * p, db = mu + gam;
+          EE(be - 1) = eb;
+          DD(be) = db;
+          test_v(be - 1, eb, d_up, db);
           if (be <= n - 2) test(be);
           insweep = false;
         }
       } else {
         // singleShiftQLPWK! step at i (:356-370); e holds squares
-        const T ei = EE(i);
+        const T ei = e_nx, di = d_nx;
+        if (i > bs) {
+          e_nx = EE(i - 1);
+          d_nx = DD(i - 1);
+        }
         const T zeta = p + ei;
-        if (i < be - 1) EE(i + 1) = s * zeta;
+        const T enew = (i < be - 1) ? s * zeta : e_end;
+        if (i < be - 1) EE(i + 1) = enew;
         const T c1 = c;
         const T rz = prec<T>::tame(zeta) ? prec<T>::rcp(zeta) : prec<T>::div_ieee(T(1), zeta);
         c = p * rz;
         s = ei * rz;
-        const T di = DD(i);
         const T g1 = gam;
         gam = c * (di - mu) - s * g1;
-        DD(i + 1) = g1 + di - gam;
+        const T dnew = g1 + di - gam;
+        DD(i + 1) = dnew;
         p = is_zero(c) ? ei * c1 : div_fast(gam * gam, c);
-        if (i + 1 <= n - 2) test(i + 1);
+        if (i + 1 <= n - 2) test_v(i + 1, enew, dnew, d_up);
+        d_up = dnew;
         i--;
         if (i < bs) {
-          EE(bs) = s * p;
-          DD(bs) = mu + gam;
-          test(bs);
+          const T eb = s * p, db = mu + gam;
+          EE(bs) = eb;
+          DD(bs) = db;
+          test_v(bs, eb, db, d_up);
           insweep = false;
         }
       }
@@ -419,10 +481,14 @@ cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream
                          const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,
                          double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats) {
   if (count <= 0) return cudaSuccess;
-  const int nb = (count + 31) / 32;
+  // FP32 chases are instruction-latency bound: 8 matrices per warp keeps the
+  // lanes of a warp in step; FP64 pays ~64 cycles per warp instruction, so
+  // the cost of divergence and of idle lanes balance at 16.
+  const int lpw = tcode == kF64 ? 16 : 8;
+  const int nb = (count + lpw - 1) / lpw;
 #define GLA_CH(T, A)                                                                                             \
   k_chase<T, A><<<nb, 32, smem, st>>>(descs, perm, count, (T*)d, (T*)e, cst, (T*)rot, hdr, info, (T)tol,        \
-                                      max_sweeps_per_n, pending, stats)
+                                      max_sweeps_per_n, pending, stats, lpw)
   if (tcode == kF64) {
     if (algo == kAlgoQL) GLA_CH(double, kAlgoQL);
     else if (algo == kAlgoQR) GLA_CH(double, kAlgoQR);

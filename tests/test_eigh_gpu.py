@@ -246,7 +246,7 @@ def test_plan_stats_rotation_count(G):
     st = plan.stats()
     nrot = sum(O.syev(m, return_stats=True)[3]["nrot"] for m in mats)
     assert abs(st["rotations"] - nrot) <= 0.05 * nrot
-    assert st["passes"] == 1
+    assert st["passes"] <= 2  # the second, asynchronous pass only finishes overflowed logs
 
 
 def test_multi_pass_chase_identical(G):
@@ -263,5 +263,5 @@ def test_multi_pass_chase_identical(G):
         plan.execute(A, w, V, info)
         outs.append((w.cpu().numpy(), V.cpu().numpy(), plan.stats()["passes"]))
         plan.close()
-    assert outs[0][2] == 1 and outs[1][2] > 3
+    assert outs[0][2] <= 2 and outs[1][2] > 3
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
