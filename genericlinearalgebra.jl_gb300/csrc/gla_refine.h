@@ -18,8 +18,11 @@ struct RefineWork {
   df64* Y2 = nullptr;  // A X, then X + X E
   df64* S2 = nullptr;  // X'AX
   df64* R2 = nullptr;  // I - X'X
+  df64* S0 = nullptr;  // first-iteration X0'AX0 (kept for the implicit iterations)
+  df64* R0 = nullptr;  // first-iteration I - X0'X0
   float* E = nullptr;  // correction E
   float* J = nullptr;  // Jacobi scratch of cluster rotations (2 * a_elems)
+  float* T = nullptr;  // FP32 product X E (a_elems)
 };
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t w_elems, int64_t batch);

@@ -20,12 +20,13 @@
 //
 // Arithmetic: the products X'X, AX, X'(AX) and X E are evaluated in
 // double-float arithmetic (df64.cuh) on the FP32 pipe, ~2^-47 relative per
-// operation; lam and the gaps in FP64. The matrix is scaled by the same
-// exact power of two as the FP32 solve (max |A| near 1) and the eigenvalues
-// are scaled back on output. Iterates until the predicted next correction
-// max|E|^2 ||A||_2 / gap_min (||A||_2 = max|lam|) falls below 1e-14 with no
-// unresolved cluster, at
-// most kMaxRefineIters times; the result is sorted ascending (sorteig!).
+// operation; lam and the gaps in FP64.
+//
+// The first iteration exploits that X0 (the FP32 eigenvectors) holds exact
+// floats. The update X <- X + X E is evaluated in FP32: its rounding error
+// (<= 2^-24 |X E| per entry, |E| <= 1e-3) is a perturbation of the next
+// iterate that the next iteration removes quadratically; from the second
+// iteration on |E| <= 1e-8 and the error is below 1e-15.
 #include "df64.cuh"
 #include "gla_refine.h"
 
@@ -36,7 +37,7 @@ constexpr int kRT = 256;  // threads per CTA
 constexpr int kJacobiSweeps = 15;
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t, int64_t) {
-  return (5 * sizeof(df64) + 3 * sizeof(float)) * (size_t)a_elems + 4096;
+  return (7 * sizeof(df64) + 4 * sizeof(float)) * (size_t)a_elems + 4096;
 }
 
 void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t) {
@@ -46,8 +47,11 @@ void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t)
   rw->Y2 = p + 2 * a_elems;
   rw->S2 = p + 3 * a_elems;
   rw->R2 = p + 4 * a_elems;
-  rw->E = reinterpret_cast<float*>(p + 5 * a_elems);
+  rw->S0 = p + 5 * a_elems;
+  rw->R0 = p + 6 * a_elems;
+  rw->E = reinterpret_cast<float*>(p + 7 * a_elems);
   rw->J = rw->E + a_elems;
+  rw->T = rw->J + 2 * a_elems;
 }
 
 // C(i, j) = init(i, j) + sum_k la(i, k) * lb(k, j) over 64 x 64 output tiles;
@@ -89,6 +93,52 @@ GLA_DEV void tile_gemm_df(int n, const LA& la, const LB& lb, const IN& init, con
           for (int u = 0; u < 4; u++)
 #pragma unroll
             for (int v = 0; v < 4; v++) acc[u][v] = df_mac(acc[u][v], a[u], b[v]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+          const int i = i0 + tx + 16 * u, j = j0 + ty + 16 * v;
+          if (i < n && j < n && (!upper || i <= j)) store(i, j, acc[u][v]);
+        }
+    }
+  }
+  __syncthreads();
+}
+
+// FP32 variant of tile_gemm_df (the X E update).
+template <class LA, class LB, class ST>
+GLA_DEV void tile_gemm_f32(int n, const LA& la, const LB& lb, const ST& store, float* As, float* Bs, bool upper) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  for (int i0 = 0; i0 < n; i0 += 64) {
+    for (int j0 = 0; j0 < n; j0 += 64) {
+      if (upper && j0 + 63 < i0) continue;
+      float acc[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[u][v] = 0.f;
+      for (int k0 = 0; k0 < n; k0 += 16) {
+        __syncthreads();
+        for (int t = tid; t < 16 * 64; t += kRT) {
+          const int kk = t & 15, ii = t >> 4;
+          const int i = i0 + ii, k = k0 + kk, j = j0 + ii;
+          As[kk * 64 + ii] = (i < n && k < n) ? la(i, k) : 0.f;
+          Bs[kk * 64 + ii] = (j < n && k < n) ? lb(k, j) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < 16; kk++) {
+          float a[4], b[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) a[u] = As[kk * 64 + tx + 16 * u];
+#pragma unroll
+          for (int v = 0; v < 4; v++) b[v] = Bs[kk * 64 + ty + 16 * v];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
         }
       }
 #pragma unroll
@@ -184,7 +234,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   __shared__ float red[kRT / 32];
   __shared__ unsigned long long keys[kSmallMaxN];
   __shared__ int rank[kSmallMaxN], ord[kSmallMaxN], cstart[kSmallMaxN + 1];
-  __shared__ int ncl_s, flag_s;
+  __shared__ int ncl_s, flag_s, big_s;
   __shared__ double gmin_s, lmax_s;
   float* Bsf = reinterpret_cast<float*>(Bs2);
   const int mid = perm[blockIdx.x];
@@ -205,8 +255,13 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   df64* Y = rw.Y2 + ao;
   df64* S = rw.S2 + ao;
   df64* R = rw.R2 + ao;
+  df64* S0 = rw.S0 + ao;
+  df64* R0 = rw.R0 + ao;
   float* E = rw.E + ao;
   float* jac = rw.J + 2 * ao;  // C and Z of a cluster (k*k each), k <= n
+  float* T1 = rw.T + ao;       // X E
+  const float* X0 = X32 + ao;
+  float* Asf = reinterpret_cast<float*>(As);
   float an2 = 0.f;
   for (int idx = tid; idx < n * n; idx += kRT) {
     const int i = idx % n, k = idx / n;
@@ -214,36 +269,66 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     const df64 ad = df_from(ldexp(a, -se));
     A2[idx] = ad;
     an2 = fmaf(ad.hi, ad.hi, an2);
-    X[idx] = df_make(X32[ao + idx], 0.f);
   }
   const float anorm = sqrtf(block_sum_f(an2, red));
   const df64 zero = df_make(0.f, 0.f);
   auto zinit = [&](int, int) { return zero; };
-  int it = 0;
-  for (; it < kMaxRefineIters; it++) {
-    // Y = A X ; S = X'Y ; R = I - X'X (upper triangles, mirrored)
-    tile_gemm_df<df64>(
-        n, [&](int i, int k) { return A2[(size_t)k * n + i]; }, [&](int k, int j) { return X[(size_t)j * n + k]; },
-        zinit, [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, As, Bs2, false);
-    tile_gemm_df<df64>(
-        n, [&](int i, int k) { return X[(size_t)i * n + k]; }, [&](int k, int j) { return Y[(size_t)j * n + k]; },
-        zinit,
-        [&](int i, int j, df64 v) {
-          S[(size_t)j * n + i] = v;
-          S[(size_t)i * n + j] = v;
-        },
-        As, Bs2, true);
-    tile_gemm_df<df64>(
-        n, [&](int i, int k) { return X[(size_t)i * n + k]; }, [&](int k, int j) { return X[(size_t)j * n + k]; },
-        zinit,
-        [&](int i, int j, df64 v) {
-          const df64 r = df_add(df_make(i == j ? 1.f : 0.f, 0.f), df_neg(v));
-          R[(size_t)j * n + i] = r;
-          R[(size_t)i * n + j] = r;
-        },
-        As, Bs2, true);
+  df64* cS = S0;
+  df64* cR = R0;
+  for (int it = 0; it < kMaxRefineIters; it++) {
+    if (it == 0) {
+      // ---- first iteration on the FP32 eigenvectors X0 (exact floats)
+      tile_gemm_df<float>(
+          n, [&](int i, int k) { return A2[(size_t)k * n + i]; }, [&](int k, int j) { return X0[(size_t)j * n + k]; },
+          zinit, [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, As, Bsf, false);
+      // S0 = X0'Y computed as (Y'X0) (symmetric): upper triangle, mirrored
+      tile_gemm_df<float>(
+          n, [&](int i, int k) { return Y[(size_t)i * n + k]; }, [&](int k, int j) { return X0[(size_t)j * n + k]; },
+          zinit,
+          [&](int i, int j, df64 v) {
+            S0[(size_t)j * n + i] = v;
+            S0[(size_t)i * n + j] = v;
+          },
+          As, Bsf, true);
+      tile_gemm_df<float>(
+          n, [&](int i, int k) { return df_make(X0[(size_t)i * n + k], 0.f); },
+          [&](int k, int j) { return X0[(size_t)j * n + k]; }, zinit,
+          [&](int i, int j, df64 v) {
+            const df64 r = df_add(df_make(i == j ? 1.f : 0.f, 0.f), df_neg(v));
+            R0[(size_t)j * n + i] = r;
+            R0[(size_t)i * n + j] = r;
+          },
+          As, Bsf, true);
+      cS = S0;
+      cR = R0;
+    } else {
+      // ---- explicit: Y = A X ; S = X'Y ; R = I - X'X (upper triangles, mirrored)
+      tile_gemm_df<df64>(
+          n, [&](int i, int k) { return A2[(size_t)k * n + i]; }, [&](int k, int j) { return X[(size_t)j * n + k]; },
+          zinit, [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, As, Bs2, false);
+      tile_gemm_df<df64>(
+          n, [&](int i, int k) { return X[(size_t)i * n + k]; }, [&](int k, int j) { return Y[(size_t)j * n + k]; },
+          zinit,
+          [&](int i, int j, df64 v) {
+            S[(size_t)j * n + i] = v;
+            S[(size_t)i * n + j] = v;
+          },
+          As, Bs2, true);
+      tile_gemm_df<df64>(
+          n, [&](int i, int k) { return X[(size_t)i * n + k]; }, [&](int k, int j) { return X[(size_t)j * n + k]; },
+          zinit,
+          [&](int i, int j, df64 v) {
+            const df64 r = df_add(df_make(i == j ? 1.f : 0.f, 0.f), df_neg(v));
+            R[(size_t)j * n + i] = r;
+            R[(size_t)i * n + j] = r;
+          },
+          As, Bs2, true);
+      cS = S;
+      cR = R;
+    }
+    // ---- Rayleigh quotients, delta, E, clusters
     for (int i = tid; i < n; i += kRT) {
-      const double l = df_to(S[(size_t)i * n + i]) / (1.0 - df_to(R[(size_t)i * n + i]));
+      const double l = df_to(cS[(size_t)i * n + i]) / (1.0 - df_to(cR[(size_t)i * n + i]));
       lam[i] = l;
       lamdf[i] = df_from(l);
       keys[i] = sort_key(l);
@@ -252,30 +337,28 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     float sd2 = 0.f, r2 = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
       const int i = idx % n, j = idx / n;
-      const float sv = (i == j) ? (float)(df_to(S[idx]) - lam[i]) : S[idx].hi;
+      const float sv = (i == j) ? (float)(df_to(cS[idx]) - lam[i]) : cS[idx].hi;
       sd2 = fmaf(sv, sv, sd2);
-      r2 = fmaf(R[idx].hi, R[idx].hi, r2);
+      r2 = fmaf(cR[idx].hi, cR[idx].hi, r2);
     }
     const float sdn = sqrtf(block_sum_f(sd2, red));
     const float rn = sqrtf(block_sum_f(r2, red));
     const float delta = 2.f * (sdn + anorm * rn);
-    // E (float) from the accurate S, R
     float emax = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
       const int i = idx % n, j = idx / n;
       const float gap = (float)(lam[j] - lam[i]);
       float e;
       if (i != j && fabsf(gap) > delta) {
-        const df64 num = df_mac(S[idx], lamdf[j], R[idx]);
+        const df64 num = df_mac(cS[idx], lamdf[j], cR[idx]);
         e = (num.hi + num.lo) / gap;
       } else {
-        e = 0.5f * (R[idx].hi + R[idx].lo);
+        e = 0.5f * (cR[idx].hi + cR[idx].lo);
       }
       E[idx] = e;
       emax = fmaxf(emax, fabsf(e));
     }
     emax = block_max_f(emax, red);
-    // clusters: runs of the sorted lam closer than delta
     for (int i = tid; i < n; i += kRT) {
       const unsigned long long ki = keys[i];
       int rk = 0;
@@ -284,7 +367,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     }
     __syncthreads();
     if (tid == 0) {
-      int nc = 0;
+      int nc = 0, big = 0;
       double gmin = 1e300;
       lmax_s = fmax(fabs(lam[ord[0]]), fabs(lam[ord[n - 1]]));  // ||A||_2 of the scaled matrix
       cstart[0] = 0;
@@ -296,79 +379,81 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
         }
       }
       cstart[++nc] = n;
+      for (int c = 0; c < nc; c++) big |= (cstart[c + 1] - cstart[c]) >= 2;
       ncl_s = nc;
       flag_s = 0;
       gmin_s = gmin;
+      big_s = big;
     }
     __syncthreads();
-    // X <- X + X E  (into Y)
-    tile_gemm_df<float>(
-        n, [&](int i, int k) { return X[(size_t)k * n + i]; }, [&](int k, int j) { return E[(size_t)j * n + k]; },
-        [&](int i, int j) { return X[(size_t)j * n + i]; },
-        [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, As, Bsf, false);
-    // Rayleigh-Ritz rotation inside each cluster of two or more
-    const int ncl = ncl_s;
-    for (int c = 0; c < ncl; c++) {
-      const int r0 = cstart[c], k = cstart[c + 1] - r0;
-      if (k < 2) continue;
-      float* C = jac;
-      float* Z = jac + k * k;
-      // C = (I + R/2) S (I + R/2) - mu I restricted to the cluster, shifted by
-      // the mean mu of its lam (first order in R, FP32 after the shift)
-      double mu = 0;
-      for (int a = 0; a < k; a++) mu += lam[ord[r0 + a]];
-      mu /= k;
-      for (int idx = tid; idx < k * k; idx += kRT) {
-        const int a = idx % k, b = idx / k;
-        const int ia = ord[r0 + a], ib = ord[r0 + b];
-        df64 s = S[(size_t)ib * n + ia];
-        if (a == b) s = df_add(s, df_from(-mu));
-        float corr = 0.f;
-        for (int q = 0; q < k; q++) {
-          const int iq = ord[r0 + q];
-          const float sq_b = S[(size_t)ib * n + iq].hi - (q == b ? (float)mu : 0.f);
-          const float sa_q = S[(size_t)iq * n + ia].hi - (a == q ? (float)mu : 0.f);
-          corr = fmaf(R[(size_t)iq * n + ia].hi, sq_b, corr);
-          corr = fmaf(sa_q, R[(size_t)ib * n + iq].hi, corr);
+    // ---- X <- X + X E (FP32 product, see above), then Rayleigh-Ritz inside clusters
+    tile_gemm_f32(
+        n, [&](int i, int k) { return it == 0 ? X0[(size_t)k * n + i] : X[(size_t)k * n + i].hi; },
+        [&](int k, int j) { return E[(size_t)j * n + k]; }, [&](int i, int j, float v) { T1[(size_t)j * n + i] = v; },
+        Asf, Bsf, false);
+    for (int idx = tid; idx < n * n; idx += kRT) {
+      const df64 x = it == 0 ? df_make(X0[idx], 0.f) : X[idx];
+      Y[idx] = df_add(x, df_make(T1[idx], 0.f));
+    }
+    __syncthreads();
+    if (big_s) {
+      const int ncl = ncl_s;
+      for (int c = 0; c < ncl; c++) {
+        const int r0 = cstart[c], k = cstart[c + 1] - r0;
+        if (k < 2) continue;
+        float* C = jac;
+        float* Z = jac + k * k;
+        // C = (I + R/2) S (I + R/2) - mu I restricted to the cluster, shifted by
+        // the mean mu of its lam (first order in R, FP32 after the shift)
+        double mu = 0;
+        for (int a = 0; a < k; a++) mu += lam[ord[r0 + a]];
+        mu /= k;
+        for (int idx = tid; idx < k * k; idx += kRT) {
+          const int a = idx % k, b = idx / k;
+          const int ia = ord[r0 + a], ib = ord[r0 + b];
+          df64 sv = cS[(size_t)ib * n + ia];
+          if (a == b) sv = df_add(sv, df_from(-mu));
+          float corr = 0.f;
+          for (int q = 0; q < k; q++) {
+            const int iq = ord[r0 + q];
+            const float sq_b = cS[(size_t)ib * n + iq].hi - (q == b ? (float)mu : 0.f);
+            const float sa_q = cS[(size_t)iq * n + ia].hi - (a == q ? (float)mu : 0.f);
+            corr = fmaf(cR[(size_t)iq * n + ia].hi, sq_b, corr);
+            corr = fmaf(sa_q, cR[(size_t)ib * n + iq].hi, corr);
+          }
+          C[b * k + a] = (sv.hi + sv.lo) + 0.5f * corr + (float)mu * cR[(size_t)ib * n + ia].hi;
         }
-        C[b * k + a] = (s.hi + s.lo) + 0.5f * corr + (float)mu * R[(size_t)ib * n + ia].hi;
+        __syncthreads();
+        float offc = 0.f;
+        for (int idx = tid; idx < k * k; idx += kRT)
+          if (idx % (k + 1) != 0) offc = fmaxf(offc, fabsf(C[idx]));
+        offc = block_max_f(offc, red);
+        if (tid < 32) jacobi_warp(k, C, Z);
+        __syncthreads();
+        if (offc > 0x1p-30f * fmaxf(anorm, 1e-30f) && tid == 0) flag_s = 1;
+        // Y[:, J] <- Y[:, J] Z  (temporary in X, whose old values are no longer needed)
+        for (int idx = tid; idx < n * k; idx += kRT) {
+          const int i = idx % n, b = idx / n;
+          df64 acc = zero;
+          for (int q = 0; q < k; q++) acc = df_mac(acc, Y[(size_t)ord[r0 + q] * n + i], Z[b * k + q]);
+          X[(size_t)b * n + i] = acc;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < n * k; idx += kRT) {
+          const int i = idx % n, b = idx / n;
+          Y[(size_t)ord[r0 + b] * n + i] = X[(size_t)b * n + i];
+        }
+        __syncthreads();
       }
-      __syncthreads();
-      float offc = 0.f, totc = 0.f;
-      for (int idx = tid; idx < k * k; idx += kRT) {
-        const float v = C[idx];
-        if (idx % (k + 1) != 0) offc = fmaxf(offc, fabsf(v));
-        totc = fmaxf(totc, fabsf(v));
-      }
-      offc = block_max_f(offc, red);
-      if (tid < 32) jacobi_warp(k, C, Z);
-      __syncthreads();
-      if (offc > 0x1p-30f * fmaxf(anorm, 1e-30f) && tid == 0) flag_s = 1;
-      // Y[:, J] <- Y[:, J] Z  (temporary in X, whose old values are no longer needed)
-      for (int idx = tid; idx < n * k; idx += kRT) {
-        const int i = idx % n, b = idx / n;
-        df64 acc = zero;
-        for (int q = 0; q < k; q++) acc = df_mac(acc, Y[(size_t)ord[r0 + q] * n + i], Z[b * k + q]);
-        X[(size_t)b * n + i] = acc;
-      }
-      __syncthreads();
-      for (int idx = tid; idx < n * k; idx += kRT) {
-        const int i = idx % n, b = idx / n;
-        Y[(size_t)ord[r0 + b] * n + i] = X[(size_t)b * n + i];
-      }
-      __syncthreads();
     }
     df64* t = X;
     X = Y;
     Y = t;
     if (tid == 0) atomicAdd(&stats[3], (unsigned long long)n * n * n);
     __syncthreads();
-    // the next correction would be about emax^2 ||A|| / gap (quadratic
+    // the next correction would be about emax^2 ||A||_2 / gap (quadratic
     // convergence): stop when that is below 1e-14 and no cluster is unresolved
-    if (flag_s == 0 && (double)emax * emax * lmax_s < 1e-14 * gmin_s) {
-      it++;
-      break;
-    }
+    if (flag_s == 0 && (double)emax * emax * lmax_s < 1e-14 * gmin_s) break;
   }
   // sorteig!: ascending eigenvalues, columns permuted to match
   __syncthreads();
