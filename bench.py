@@ -153,6 +153,10 @@ def run_ours(args):
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
     ns, mats = workload(batch=args.batch, seed=SEED + 1000 * rank)
+    if args.nrange:  # profiling: keep one size range of the workload
+        lo, hi = (int(x) for x in args.nrange.split(","))
+        keep = [i for i in range(len(ns)) if lo <= ns[i] <= hi]
+        ns, mats = ns[keep], [mats[i] for i in keep]
     aoff = np.concatenate([[0], np.cumsum(ns * ns)[:-1]]).astype(np.int64)
     woff = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
     A64 = pack_f(mats)
@@ -376,6 +380,7 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="matrices in the batch (profiling: smaller cases)")
     ap.add_argument("--paths", default="f64,f32,f32_refined", help="paths to time (profiling)")
     ap.add_argument("--profile", action="store_true", help="profiling run: time the paths only, print nothing")
+    ap.add_argument("--nrange", default="", help="profiling: keep matrices with lo <= n <= hi, as 'lo,hi'")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

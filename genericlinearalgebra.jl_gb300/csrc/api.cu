@@ -52,7 +52,8 @@ constexpr int kMaxBuckets = 8;      // size buckets of width 16 over (0, 128]
 
 struct Bucket {
   int nmax;   // largest order in the bucket
-  int nt;     // threads per CTA
+  int nt;     // threads per CTA (apply)
+  int nt_tri; // threads per CTA (tridiagonalisation)
   int start;  // first index into perm_bucket (orders descending inside the bucket)
   int count;
   cudaStream_t stream = nullptr;  // the bucket's pipeline runs on its own stream
@@ -222,6 +223,10 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
       }
     }
     bk.nt = std::max(32, (bk.nmax + 31) / 32 * 32);
+    // FP32 reductions are latency bound: two threads per row halve the
+    // per-thread loops of the tridiagonalisation (FP64 keeps one: its cost
+    // is the FP64 pipe, not latency)
+    bk.nt_tri = precision == GLA_PREC_F64 ? bk.nt : std::min(256, 2 * bk.nt);
     if (bk.count) p->buckets.push_back(bk);
   }
 
@@ -408,7 +413,7 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
     cudaStream_t s = bk.stream;
     GLA_CUDA(cudaStreamWaitEvent(s, p->fork, 0));
     p->mark(b, GLA_PHASE_TRIDIAG, 0, s);
-    GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt, tridiag_smem_bytes(bk.nmax, bk.nt, el), s, p->d_desc,
+    GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt_tri, tridiag_smem_bytes(bk.nmax, bk.nt_tri, el), s, p->d_desc,
                             p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, Q, info, p->d_cst, p->d_scale));
     p->mark(b, GLA_PHASE_TRIDIAG, 1, s);
     if (wantq) {

@@ -113,6 +113,78 @@ template <class T> GLA_DEV void givens(T f, T g, T& c, T& s, T& r) {
   }
 }
 
+// Givens rotation for the sweep step: the refined-rsqrt radius when
+// f^2 + g^2 is comfortably inside the normal range, the exact dlartg port
+// otherwise. Same convention as givens() (c >= 0 when |f| > |g|; f == 0 gives
+// c = 0, s = 1, r = g). FP32 tests use float compares; FP64 tests use the
+// exponent bits (an FP64 compare costs a full FP64 warp-instruction slot).
+GLA_DEV void givens_step(float f, float g, float& c, float& s, float& r) {
+  const float r2 = fmaf(f, f, g * g);
+  if (r2 >= 0x1p-120f && r2 <= 0x1p+120f) {
+    const float y = prec<float>::rsqrt(r2);
+    r = r2 * y;
+    c = f * y;
+    s = g * y;
+    if (f == 0.f) {
+      c = 0.f;
+      s = 1.f;
+      r = g;
+    } else if (f < 0.f && fabsf(f) > fabsf(g)) {
+      c = -c;
+      s = -s;
+      r = -r;
+    }
+  } else {
+    givens(f, g, c, s, r);
+  }
+}
+GLA_DEV void givens_step(double f, double g, double& c, double& s, double& r) {
+  const double r2 = fma(f, f, g * g);
+  const int be = prec<double>::biased_exp(r2);
+  if (be >= 1023 - 1000 && be <= 1023 + 1000) {
+    const double y = prec<double>::rsqrt(r2);
+    r = r2 * y;
+    c = f * y;
+    s = g * y;
+    if (is_zero(f)) {
+      c = 0.0;
+      s = 1.0;
+      r = g;
+    } else if (!abs_le(f, g) && (prec<double>::bits(f) >> 63)) {
+      c = -c;
+      s = -s;
+      r = -r;
+    }
+  } else {
+    givens(f, g, c, s, r);
+  }
+}
+
+// Deflation test on register values: FP32 decides on the squared sides
+// (margin 4x each way) and falls back to the exact form near the threshold
+// or when a square leaves the normal range; FP64 uses the exponent filter.
+GLA_DEV bool negligible_step(float ev, float d1, float d2, float tol, int tol_e) {
+  const float e2 = ev * ev;
+  const float rhs = (tol * tol) * fabsf(d1 * d2);
+  if (rhs >= 0x1p-120f && rhs <= 0x1p+120f && e2 <= 0x1p+120f) {
+    if (e2 < 0.25f * rhs) return true;
+    if (e2 > 4.f * rhs) return false;
+  }
+  return negligible(ev, d1, d2, tol, tol_e);
+}
+GLA_DEV bool negligible_step(double ev, double d1, double d2, double tol, int tol_e) {
+  return negligible(ev, d1, d2, tol, tol_e);
+}
+
+// gamma / c: FP32 uses rcp.approx (~1 ulp, one rounding in the recurrence)
+// guarded by a float compare; FP64 the Newton-refined reciprocal.
+GLA_DEV float div_step(float a, float b) {
+  if (fabsf(b) < 0x1p-100f) return __fdiv_rn(a, b);
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(b));
+  return a * y;
+}
+
 template <class T> GLA_DEV T div_fast(T a, T b) {
   return prec<T>::tame(b) ? a * prec<T>::rcp(b) : prec<T>::div_ieee(a, b);
 }
@@ -127,6 +199,7 @@ GLA_DEV float div_chase(float a, float b) {
   return a * y;
 }
 GLA_DEV double div_chase(double a, double b) { return div_fast(a, b); }
+GLA_DEV double div_step(double a, double b) { return div_fast(a, b); }
 
 // Append (c, s) to the rotation log as one 8- or 16-byte store.
 GLA_DEV void store_rot(float* log, int k, float c, float s) {
@@ -229,11 +302,23 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
   // register cache of the sweep: next (e, d) to consume, the d two positions
   // behind (for the deflation test) and e beyond the block end
   T e_nx = 0, d_nx = 0, d_up = 0, e_end = 0;
+  // NF word of the current sweep position cached in a register
+  unsigned nfw = 0;
+  int nfw_idx = -1;
+  auto nf_flush = [&]() {
+    if (nfw_idx >= 0) NF[nfw_idx * 32] = nfw;
+    nfw_idx = -1;
+  };
   auto test_v = [&](int j, T ev, T d1, T d2) {  // NF(j) from register values
-    const bool f = negligible(ev, d1, d2, tol, tol_e);
-    unsigned& w = NF[(j >> 5) * 32];
+    const bool f = negligible_step(ev, d1, d2, tol, tol_e);
+    const int wi = j >> 5;
+    if (wi != nfw_idx) {
+      nf_flush();
+      nfw_idx = wi;
+      nfw = NF[wi * 32];
+    }
     const unsigned b = 1u << (j & 31);
-    w = f ? (w | b) : (w & ~b);
+    nfw = f ? (nfw | b) : (nfw & ~b);
   };
   int iters = 0;
   const int iter_cap = (max_sweeps_per_n + 4) * 4 * nmax * nmax + 64;  // hard bound on loop trips
@@ -248,6 +333,7 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
       continue;
     }
     if (active && !insweep) {
+      nf_flush();
       if (bs >= n - 1) {
         active = false;
         st.status = kChaseDone;
@@ -347,98 +433,103 @@ __global__ void __launch_bounds__(32) k_chase(const SmallDesc* __restrict__ desc
         }
       }
     }
-    if (active && insweep) {
-      if (ALGO == kAlgoQL) {
-        // singleShiftQL! step at i (:389-405), operands from registers
-        const T ei = e_nx, di = d_nx;
-        if (i > bs) {
-          e_nx = EE(i - 1);
-          d_nx = DD(i - 1);
+    // tight sweep loop: runs while every active lane is inside a chase
+    while (__all_sync(0xffffffffu, !active || insweep) && __any_sync(0xffffffffu, active)) {
+      if (++iters > iter_cap) break;
+      if (active) {
+        if (ALGO == kAlgoQL) {
+          // singleShiftQL! step at i (:389-405), operands from registers
+          const T ei = e_nx, di = d_nx;
+          if (i > bs) {
+            e_nx = EE(i - 1);
+            d_nx = DD(i - 1);
+          }
+          const T c1 = c, s1 = s;
+          T zeta;
+          givens_step(p, ei, c, s, zeta);
+          const T enew = (i < be - 1) ? s1 * zeta : e_end;
+          if (i < be - 1) EE(i + 1) = enew;
+          const T g1 = gam;
+          gam = c * c * (di - mu) - s * s * g1;
+          const T dnew = g1 + di - gam;
+          DD(i + 1) = dnew;
+          p = is_zero(c) ? -ei * c1 : div_step(gam, c);
+          store_rot(myrot, nrot, c, s);
+          nrot++;
+          if (i + 1 <= n - 2) test_v(i + 1, enew, dnew, d_up);
+          d_up = dnew;
+          i--;
+          if (i < bs) {
+            const T eb = s * p, db = mu + gam;
+            EE(bs) = eb;
+            DD(bs) = db;
+            test_v(bs, eb, db, d_up);
+            insweep = false;
+          }
+        } else if (ALGO == kAlgoQR) {
+          // singleShiftQR! step at i (:424-440), operands from registers;
+          // d_up holds d[i-2] (the previous step's new d)
+          const T ei = e_nx, di = d_nx;
+          if (i < be) {
+            e_nx = EE(i);
+            d_nx = DD(i + 1);
+          }
+          const T c1 = c, s1 = s;
+          T zeta;
+          givens_step(p, ei, c, s, zeta);
+          const T g1 = gam;
+          gam = c * c * (di - mu) - s * s * g1;
+          const T dnew = g1 + di - gam;
+          DD(i - 1) = dnew;
+          if (i > bs + 1) {
+            const T enew = s1 * zeta;
+            EE(i - 2) = enew;
+            test_v(i - 2, enew, d_up, dnew);
+          }
+          p = is_zero(c) ? -ei * c1 : div_step(gam, c);
+          store_rot(myrot, nrot, c, s);
+          nrot++;
+          d_up = dnew;
+          i++;
+          if (i > be) {
+            const T eb = s * p, db = mu + gam;
+            EE(be - 1) = eb;
+            DD(be) = db;
+            test_v(be - 1, eb, d_up, db);
+            if (be <= n - 2) test_v(be, EE(be), db, DD(be + 1));
+            insweep = false;
+          }
+        } else {
+          // singleShiftQLPWK! step at i (:356-370); e holds squares
+          const T ei = e_nx, di = d_nx;
+          if (i > bs) {
+            e_nx = EE(i - 1);
+            d_nx = DD(i - 1);
+          }
+          const T zeta = p + ei;
+          const T enew = (i < be - 1) ? s * zeta : e_end;
+          if (i < be - 1) EE(i + 1) = enew;
+          const T c1 = c;
+          const T rz = prec<T>::tame(zeta) ? prec<T>::rcp(zeta) : prec<T>::div_ieee(T(1), zeta);
+          c = p * rz;
+          s = ei * rz;
+          const T g1 = gam;
+          gam = c * (di - mu) - s * g1;
+          const T dnew = g1 + di - gam;
+          DD(i + 1) = dnew;
+          p = is_zero(c) ? ei * c1 : div_fast(gam * gam, c);
+          if (i + 1 <= n - 2) test_v(i + 1, enew, dnew, d_up);
+          d_up = dnew;
+          i--;
+          if (i < bs) {
+            const T eb = s * p, db = mu + gam;
+            EE(bs) = eb;
+            DD(bs) = db;
+            test_v(bs, eb, db, d_up);
+            insweep = false;
+          }
         }
-        const T c1 = c, s1 = s;
-        T zeta;
-        givens(p, ei, c, s, zeta);
-        const T enew = (i < be - 1) ? s1 * zeta : e_end;
-        if (i < be - 1) EE(i + 1) = enew;
-        const T g1 = gam;
-        gam = c * c * (di - mu) - s * s * g1;
-        const T dnew = g1 + di - gam;
-        DD(i + 1) = dnew;
-        p = is_zero(c) ? -ei * c1 : div_chase(gam, c);
-        store_rot(myrot, nrot, c, s);
-        nrot++;
-        if (i + 1 <= n - 2) test_v(i + 1, enew, dnew, d_up);
-        d_up = dnew;
-        i--;
-        if (i < bs) {
-          const T eb = s * p, db = mu + gam;
-          EE(bs) = eb;
-          DD(bs) = db;
-          test_v(bs, eb, db, d_up);
-          insweep = false;
-        }
-      } else if (ALGO == kAlgoQR) {
-        // singleShiftQR! step at i (:424-440), operands from registers;
-        // d_up holds d[i-2] (the previous step's new d)
-        const T ei = e_nx, di = d_nx;
-        if (i < be) {
-          e_nx = EE(i);
-          d_nx = DD(i + 1);
-        }
-        const T c1 = c, s1 = s;
-        T zeta;
-        givens(p, ei, c, s, zeta);
-        const T g1 = gam;
-        gam = c * c * (di - mu) - s * s * g1;
-        const T dnew = g1 + di - gam;
-        DD(i - 1) = dnew;
-        if (i > bs + 1) {
-          const T enew = s1 * zeta;
-          EE(i - 2) = enew;
-          test_v(i - 2, enew, d_up, dnew);
-        }
-        p = is_zero(c) ? -ei * c1 : div_chase(gam, c);
-        store_rot(myrot, nrot, c, s);
-        nrot++;
-        d_up = dnew;
-        i++;
-        if (i > be) {
-          const T eb = s * p, db = mu + gam;
-          EE(be - 1) = eb;
-          DD(be) = db;
-          test_v(be - 1, eb, d_up, db);
-          if (be <= n - 2) test(be);
-          insweep = false;
-        }
-      } else {
-        // singleShiftQLPWK! step at i (:356-370); e holds squares
-        const T ei = e_nx, di = d_nx;
-        if (i > bs) {
-          e_nx = EE(i - 1);
-          d_nx = DD(i - 1);
-        }
-        const T zeta = p + ei;
-        const T enew = (i < be - 1) ? s * zeta : e_end;
-        if (i < be - 1) EE(i + 1) = enew;
-        const T c1 = c;
-        const T rz = prec<T>::tame(zeta) ? prec<T>::rcp(zeta) : prec<T>::div_ieee(T(1), zeta);
-        c = p * rz;
-        s = ei * rz;
-        const T g1 = gam;
-        gam = c * (di - mu) - s * g1;
-        const T dnew = g1 + di - gam;
-        DD(i + 1) = dnew;
-        p = is_zero(c) ? ei * c1 : div_fast(gam * gam, c);
-        if (i + 1 <= n - 2) test_v(i + 1, enew, dnew, d_up);
-        d_up = dnew;
-        i--;
-        if (i < bs) {
-          const T eb = s * p, db = mu + gam;
-          EE(bs) = eb;
-          DD(bs) = db;
-          test_v(bs, eb, db, d_up);
-          insweep = false;
-        }
+    
       }
     }
   }

@@ -57,13 +57,18 @@ GLA_DEV void block_sum_max(T v, unsigned long long m, T* red, unsigned long long
   mx = x;
 }
 
+// Leading dimension of the staged matrix: odd, so that transposed accesses
+// (stride ld across the lanes of a warp) spread over all shared-memory banks.
+GLA_DEV int stage_ld(int n) { return (n + 1) | 1; }
+
 size_t tridiag_smem_bytes(int n, int nt, int elem) {
-  // redm[32] u64 | red[32] (8-byte slots) | S[n*(n+1)] | vv,uu,ww,taus [n] | part[4*nt]
-  return 512 + (size_t)elem * ((size_t)n * (n + 1) + 4 * (size_t)n + 4 * (size_t)nt);
+  // redm[32] u64 | red[32] (8-byte slots) | S[n*ld] | vv,uu,ww,taus [n] | part[8*nt]
+  const size_t ld = (size_t)((n + 1) | 1);
+  return 512 + (size_t)elem * ((size_t)n * ld + 4 * (size_t)n + 8 * (size_t)nt);
 }
 
 template <class T, class Tin, bool WANTQ>
-__global__ void __launch_bounds__(128) k_tridiag(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
+__global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                  const Tin* __restrict__ A, int lower, T* __restrict__ dout,
                                                  T* __restrict__ eout, T* __restrict__ Qout, int* __restrict__ info,
                                                  ChaseState* __restrict__ cst, int* __restrict__ scale_exp) {
@@ -71,7 +76,7 @@ __global__ void __launch_bounds__(128) k_tridiag(const SmallDesc* __restrict__ d
   const int mid = perm[blockIdx.x];
   const SmallDesc dsc = descs[mid];
   const int n = dsc.n;
-  const int ld = n + 1;
+  const int ld = stage_ld(n);
   const int tid = threadIdx.x, NT = blockDim.x;
   unsigned long long* redm = reinterpret_cast<unsigned long long*>(smem_raw);
   T* red = reinterpret_cast<T*>(smem_raw + 256);
@@ -188,16 +193,20 @@ __global__ void __launch_bounds__(128) k_tridiag(const SmallDesc* __restrict__ d
     {
       const int R = (m + 31) & ~31;
       int P = NT / R;
-      P = P > 4 ? 4 : P;
+      P = P > 8 ? 8 : P;
       const int p = tid / R, i = tid - p * R;
       if (p < P && i < m) {
         const int j0 = (p * m) / P, j1 = ((p + 1) * m) / P;
-        T acc = 0;
-        for (int j = j0; j < j1; j++) {
-          const int addr = (j <= i) ? (j * ld + i) : (i * ld + j);
-          acc = fma(At[addr], vv[j], acc);
+        T acc0 = 0, acc1 = 0;
+        int j = j0;
+        for (; j + 1 < j1; j += 2) {
+          const int a0 = (j <= i) ? (j * ld + i) : (i * ld + j);
+          const int a1 = (j + 1 <= i) ? ((j + 1) * ld + i) : (i * ld + j + 1);
+          acc0 = fma(At[a0], vv[j], acc0);
+          acc1 = fma(At[a1], vv[j + 1], acc1);
         }
-        part[p * NT + i] = acc;
+        if (j < j1) acc0 = fma(At[(j <= i) ? (j * ld + i) : (i * ld + j)], vv[j], acc0);
+        part[p * NT + i] = acc0 + acc1;
       }
       __syncthreads();
       T ui = 0;
@@ -257,12 +266,27 @@ __global__ void __launch_bounds__(128) k_tridiag(const SmallDesc* __restrict__ d
     __syncthreads();
     const int C = n - kk - 2;
     if (tau != T(0)) {
-      for (int t = tid; t < C; t += NT) {
-        T* col = S + (size_t)(kk + 2 + t) * ld + (kk + 1);
-        T dot = 0;
-        for (int r = 0; r < M; r++) dot = fma(vv[r], col[r], dot);
+      // two lanes per column (row halves), partial dots combined by shuffle
+      const int half = (M + 1) >> 1;
+      for (int t2 = tid; t2 < 2 * ((C + 15) / 16) * 16; t2 += NT) {
+        const int t = t2 >> 1, h = t2 & 1;
+        const bool live = t < C;
+        T* col = S + (size_t)(kk + 2 + (live ? t : 0)) * ld + (kk + 1);
+        const int r0 = h * half, r1 = h ? M : half;
+        T d0 = 0, d1 = 0;
+        if (live) {
+          int r = r0;
+          for (; r + 1 < r1; r += 2) {
+            d0 = fma(vv[r], col[r], d0);
+            d1 = fma(vv[r + 1], col[r + 1], d1);
+          }
+          if (r < r1) d0 = fma(vv[r], col[r], d0);
+        }
+        T dot = d0 + d1;
+        dot += __shfl_xor_sync(0xffffffffu, dot, 1);
         const T tmp = tau * dot;
-        for (int r = 0; r < M; r++) col[r] = fma(-vv[r], tmp, col[r]);
+        if (live)
+          for (int r = r0; r < r1; r++) col[r] = fma(-vv[r], tmp, col[r]);
       }
     }
     __syncthreads();
@@ -283,7 +307,7 @@ __global__ void __launch_bounds__(128) k_tridiag(const SmallDesc* __restrict__ d
 
 template <class T, class Tin, bool Q> static void set_tri_attr() {
   cudaFuncSetAttribute(k_tridiag<T, Tin, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)tridiag_smem_bytes(kSmallMaxN, 128, sizeof(T)));
+                       (int)tridiag_smem_bytes(kSmallMaxN, 256, sizeof(T)));
 }
 
 cudaError_t tridiag_kernels_init() {
