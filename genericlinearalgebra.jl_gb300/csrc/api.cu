@@ -137,6 +137,7 @@ int gla_version(void) { return GLA_VERSION; }
 const char* gla_status_string(int status) {
   if (status == 0) return "success";
   if (status > 0) return "some matrices did not converge or held non-finite values (see info)";
+  if (status == GLA_ERR_STATIC_TOO_LARGE) return "order exceeds GLA_STATIC_MAX_N (128) for gla_dsyev_static";
   if (status <= -1000) return cudaGetErrorString((cudaError_t)(-1000 - status));
   switch (status) {
     case -1: return "invalid argument 1";

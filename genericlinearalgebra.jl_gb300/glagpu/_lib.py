@@ -16,6 +16,8 @@ GLA_PREC_F32_REFINED = 2
 GLA_ALG_QL = 0
 GLA_ALG_QR = 1
 GLA_MAX_SMALL_N = 128
+GLA_STATIC_MAX_N = 128
+GLA_ERR_STATIC_TOO_LARGE = -2001
 GLA_FLAG_SMALL_LOG = 4
 GLA_FLAG_TIMING = 8
 PHASES = ("tridiag", "chase", "apply", "refine")
@@ -42,6 +44,7 @@ SIGNATURES = {
     "gla_dsyev": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
     "gla_ssyev": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
     "gla_dstev": ([_ch, _i64, _vp, _vp, _vp, _i64, _int, C.POINTER(_int), _vp], _int),
+    "gla_dsyev_static": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
 }
 
 _lib = None

@@ -11,6 +11,7 @@
  *   status   0  success
  *           <0  argument -status is invalid (LAPACK xerbla convention)
  *         -1000 - e  CUDA runtime error e (see gla_status_string)
+ *         -2001 order above GLA_STATIC_MAX_N (gla_dsyev_static only)
  *           >0  number of matrices whose per-matrix info is nonzero
  *   info[b]  0  converged
  *           >0  number of off-diagonal entries still above the deflation
@@ -59,6 +60,8 @@ extern "C" {
 #define GLA_NUM_PHASES 4
 
 #define GLA_MAX_SMALL_N 128
+#define GLA_STATIC_MAX_N 128
+#define GLA_ERR_STATIC_TOO_LARGE (-2001)
 
 typedef struct gla_plan_s* gla_plan_t;
 
@@ -140,6 +143,24 @@ int gla_plan_phase_times(gla_plan_t plan, float* ms);
  */
 int gla_dsyev(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, int* info, void* stream);
 int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, int* info, void* stream);
+
+/*
+ * gla_dsyev without any device allocation: same arguments, results and
+ * synchronisation as gla_dsyev, for callers that cannot call cudaMalloc when
+ * they need the decomposition (e.g. an application whose memory pool already
+ * owns the whole device, a latency-critical loop where an allocation would
+ * synchronise the device, a fixed memory budget). No counterpart in the
+ * reference.
+ *
+ * Limit: n <= GLA_STATIC_MAX_N (128); larger orders return
+ * GLA_ERR_STATIC_TOO_LARGE. Scratch comes from one file-scope device array of
+ * about 660 KB that every GPU loading the library holds until exit. The
+ * first call on a device looks up that array's device address (and sets the
+ * kernels' shared-memory limits), so make it before any stream capture.
+ * All calls share the array: calls whose GPU work overlaps (other streams,
+ * other host threads on the same device) race and must be serialised.
+ */
+int gla_dsyev_static(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, int* info, void* stream);
 
 /*
  * eigen!/eigvals! of SymTridiagonal(d, e) (src/eigenSelfAdjoint.jl:581,
