@@ -226,6 +226,37 @@ def run_ours(args):
         plan.close()
     if args.profile:  # profiling runs (under ncu) stop here: no e2e, CPU leg or JSON line
         return
+    # ---- headline path captured in a CUDA graph and replayed
+    graph_res = {}
+    for path in ("f32_refined", "f64"):
+        gplan = glagpu.Plan(ns, precision=path, graph=True)
+        w = torch.empty(nW, dtype=torch.float64, device=dev)
+        V = torch.empty(nA, dtype=torch.float64, device=dev)
+        info = torch.zeros(len(ns), dtype=torch.int32, device=dev)
+        Ag = dA64.clone()
+        g = gplan.capture(Ag, w, V, info)
+        for _ in range(args.warmup):
+            g.replay()
+        torch.cuda.synchronize()
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(args.steps):
+            g.replay()
+        ev1.record()
+        torch.cuda.synchronize()
+        barrier()
+        el = ev0.elapsed_time(ev1) * 1e-3
+        if ws > 1:
+            t = torch.tensor([el], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        acc = check_sample(ns, mats, w.cpu().numpy(), V.cpu().numpy(), woff, aoff, sample, np.float64)
+        graph_res[path] = {"eigh_per_s": ws * len(ns) * args.steps / el, "ms_per_step": 1e3 * el / args.steps,
+                           "accuracy": acc, "info_nonzero": int((info.cpu().numpy() != 0).sum())}
+        del g
+        gplan.close()
     # ---- end to end through the C ABI with host buffers (headline path)
     plan = glagpu.Plan(ns, precision="f32_refined")
     hA = torch.from_numpy(A64).pin_memory()
@@ -254,10 +285,12 @@ def run_ours(args):
     peak = measured_dgemm_tflops(torch) if rank == 0 else None
 
     if rank == 0:
-        head = results["f32_refined"]
-        ok = head["accuracy"]["max_residual"] <= 1e-13 and head["accuracy"]["max_eig_err_vs_oracle"] <= 1e-13
-        hp = "f32_refined" if ok else "f64"
+        def meets(r):
+            a = r["accuracy"]
+            return r["info_nonzero"] == 0 and a["max_residual"] <= 1e-13 and a["max_eig_err_vs_oracle"] <= 1e-13
+        hp = "f32_refined" if meets(results["f32_refined"]) and meets(graph_res["f32_refined"]) else "f64"
         H = results[hp]
+        G = graph_res[hp]
         ph = H["phase_ms_per_step"]
         dom = max(ph, key=lambda k: ph[k])
         c = H["counters"]
@@ -271,12 +304,12 @@ def run_ours(args):
         cpu = cpu_baseline(ns, mats)
         line = {
             "metric": METRIC,
-            "value": H["eigh_per_s"],
+            "value": G["eigh_per_s"],
             "unit": "eigh/s",
             "n_gpus": ws,
             "steps": args.steps,
             "warmup": args.warmup,
-            "ms_per_step": H["ms_per_step"],
+            "ms_per_step": G["ms_per_step"],
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
@@ -284,7 +317,8 @@ def run_ours(args):
             "data": "synthetic (seeded GOE)",
             "config": {"workload": f"batched eigen!(Hermitian): {len(ns)} GOE matrices, n~U[{NLO},{NHI}], seed {SEED}",
                        "path": hp, "batch": len(ns), "sum_n": int(ns.sum()), "sum_n3": ns3,
-                       "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}"},
+                       "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}",
+                       "timing": "CUDA-graph replay of the whole batched solve (plan with GLA_FLAG_GRAPH)"},
             "roofline": {"kernel": dom, "bound": "fp64" if dom != "chase" else "latency",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if peak else None, "traffic": None,
@@ -296,7 +330,8 @@ def run_ours(args):
             "clocks": results["f32_refined"]["clocks"],
             "gpu_launches": int(H["launches_per_step"] * args.steps),
             "paths": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} for k, v in results.items()},
-            "speedup_f32refined_vs_f64": results["f32_refined"]["eigh_per_s"] / results["f64"]["eigh_per_s"],
+            "graph": graph_res,
+            "speedup_f32refined_vs_f64": graph_res["f32_refined"]["eigh_per_s"] / graph_res["f64"]["eigh_per_s"],
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -42,6 +42,7 @@ constexpr int kHdrPerN = 3;     // header-log capacity per pass, in units of n
 constexpr int kMaxSweepsPerN = 30;  // chase cap per matrix (src/eigenGeneral.jl:52 uses 30n)
 constexpr int kMaxPasses = 64;
 constexpr int kAsyncPasses = 2;     // chase passes enqueued without a host check
+constexpr int kGraphPasses = 4;     // chase passes of a capture-safe (GLA_FLAG_GRAPH) execute
 constexpr int kMaxBuckets = 8;      // size buckets of width 16 over (0, 128]
 
 #define GLA_CUDA(x)                                  \
@@ -118,6 +119,7 @@ struct gla_plan_s {
   // phase timing (GLA_FLAG_TIMING): begin/end events per bucket and phase;
   // a phase's time is the sum over buckets of its kernels' stream time
   bool timing = false;
+  bool graph = false;  // capture-safe execute (no host synchronisation)
   cudaEvent_t tev[kMaxBuckets][GLA_NUM_PHASES][2] = {};
   bool tused[kMaxBuckets][GLA_NUM_PHASES] = {};
   void mark(int b, int phase, int end, cudaStream_t st) {
@@ -166,7 +168,8 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   for (int64_t b = 0; b < batch; b++)
     if (n[b] < 0 || n[b] > GLA_MAX_SMALL_N) return -6;
   if (!(tol == tol)) return -7;
-  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING)) != 0 || (flags & 3) > GLA_ALG_QR) return -8;
+  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH)) != 0 || (flags & 3) > GLA_ALG_QR)
+    return -8;
   GLA_CUDA(ensure_init());
 
   gla_plan_s* p = new (std::nothrow) gla_plan_s();
@@ -178,6 +181,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->batch = batch;
   p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? 0x1p-52 : (double)0x1p-23f);
   p->timing = (flags & GLA_FLAG_TIMING) != 0;
+  p->graph = (flags & GLA_FLAG_GRAPH) != 0;
   p->n.assign(n, n + batch);
 
   // ---- descriptors and offsets
@@ -418,17 +422,21 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
                             p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, Q, info, p->d_cst, p->d_scale));
     p->mark(b, GLA_PHASE_TRIDIAG, 1, s);
     if (wantq) {
-      for (int k = 0; k < kAsyncPasses; k++) {  // the second pass only finishes overflowed logs
+      const int npass = p->graph ? kGraphPasses : kAsyncPasses;
+      for (int k = 0; k < npass; k++) {  // passes after the first only finish overflowed logs
         int rc = enqueue_pass(p, b, tc, Q, wq, info, scale, s, k == 0);
         if (rc) return rc;
       }
+      if (p->graph)
+        GLA_CUDA(launch_mark_unfinished(bk.count, s, p->d_desc, p->d_perm_bucket + bk.start, p->d_cst, info));
       if (refined) {
         p->mark(b, GLA_PHASE_REFINE, 0, s);
         int rc = enqueue_refine(p, b, A, lower, Vout, w, info, s);
         if (rc) return rc;
         p->mark(b, GLA_PHASE_REFINE, 1, s);
       }
-      GLA_CUDA(cudaMemcpyAsync(p->pin_pending + b, p->d_pending + b, sizeof(int), cudaMemcpyDeviceToHost, s));
+      if (!p->graph)
+        GLA_CUDA(cudaMemcpyAsync(p->pin_pending + b, p->d_pending + b, sizeof(int), cudaMemcpyDeviceToHost, s));
     } else {
       p->mark(b, GLA_PHASE_CHASE, 0, s);
       GLA_CUDA(launch_chase(work_t, kAlgoPWK, bk.count, chase_smem_bytes(bk.nmax, el), s, p->d_desc,
@@ -443,6 +451,10 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
   }
   if (!wantq) {
     p->last_passes = 1;
+    return 0;
+  }
+  if (p->graph) {
+    p->last_passes = kGraphPasses;
     return 0;
   }
   // A matrix whose rotation log filled up in both asynchronous passes (never

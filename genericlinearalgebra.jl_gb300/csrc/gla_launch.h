@@ -33,6 +33,10 @@ cudaError_t launch_apply(int tcode, int nblocks, int nt, size_t smem, cudaStream
 cudaError_t launch_sort_values(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
                                const void* d, void* w, const int* info, const int* scale_exp);
 
+// Capture-safe executes: info = -2 for matrices whose chase is still running.
+cudaError_t launch_mark_unfinished(int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
+                                   const ChaseState* cst, int* info);
+
 // SymTridiagonal input: copy (d, e) into the working arrays, Q := I, reset state.
 cudaError_t launch_init_tridiagonal(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs,
                                     const int* perm, const void* din, const void* ein, void* d, void* e, void* Q,

@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   const size_t ao = dsc.a_off;
   const double* Ag = A + ao;
   double* V = Vout ? Vout + ao : nullptr;
-  if (info[mid] == -1) {
+  if (info[mid] < 0) {  // non-finite input, or (capture-safe plans) an unfinished chase
     for (int idx = tid; idx < n * n; idx += kRT)
       if (V) V[idx] = NAN;
     for (int i = tid; i < n; i += kRT) wout[dsc.w_off + i] = NAN;

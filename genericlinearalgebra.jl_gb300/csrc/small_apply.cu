@@ -229,6 +229,21 @@ cudaError_t launch_sort_values(int tcode, int nblocks, cudaStream_t st, const Sm
   return cudaGetLastError();
 }
 
+__global__ void k_mark_unfinished(const SmallDesc* __restrict__ descs, const int* __restrict__ perm, int count,
+                                  const ChaseState* __restrict__ cst, int* __restrict__ info) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int mid = perm[t];
+  if (cst[mid].status != kChaseDone && info[mid] == 0) info[mid] = -2;
+}
+
+cudaError_t launch_mark_unfinished(int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
+                                   const ChaseState* cst, int* info) {
+  if (nblocks <= 0) return cudaSuccess;
+  k_mark_unfinished<<<(nblocks + 127) / 128, 128, 0, st>>>(descs, perm, nblocks, cst, info);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_init_tridiagonal(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs,
                                     const int* perm, const void* din, const void* ein, void* d, void* e, void* Q,
                                     int* info, ChaseState* cst, bool wantq) {

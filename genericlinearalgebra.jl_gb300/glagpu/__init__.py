@@ -99,7 +99,7 @@ class Plan:
     """
 
     def __init__(self, ns, precision="f64", jobz="V", uplo="L", tol=None, alg="QL", small_log=False,
-                 timing=False):
+                 timing=False, graph=False):
         L = _lib.load()
         ns = np.ascontiguousarray(np.asarray(ns, dtype=np.int64))
         if (ns < 0).any() or (ns > GLA_MAX_SMALL_N).any():
@@ -110,7 +110,8 @@ class Plan:
         self.uplo = uplo
         self.dtype = np.float32 if precision == "f32" else np.float64
         flags = (GLA_ALG_QR if alg == "QR" else GLA_ALG_QL) | (_lib.GLA_FLAG_SMALL_LOG if small_log else 0) | \
-            (_lib.GLA_FLAG_TIMING if timing else 0)
+            (_lib.GLA_FLAG_TIMING if timing else 0) | (_lib.GLA_FLAG_GRAPH if graph else 0)
+        self.graph = graph
         h = C.c_void_p()
         _lib.check(L.gla_plan_create(C.byref(h), PRECISIONS[precision], jobz.encode(), uplo.encode(), len(ns),
                                      ns.ctypes.data_as(C.POINTER(C.c_int64)), float(tol or 0.0), flags),
@@ -150,6 +151,19 @@ class Plan:
                                           C.c_void_p(V.data_ptr()) if V is not None else None,
                                           C.c_void_p(info.data_ptr()), _stream_ptr(stream))
         return _lib.check(rc, "gla_plan_execute")
+
+    def capture(self, A, w, V, info):
+        """Capture execute(A, w, V, info) into a torch.cuda.CUDAGraph (plan made
+        with graph=True). Replaying it re-solves whatever A holds at replay."""
+        if not self.graph:
+            raise ValueError("plan was not created with graph=True")
+        torch = _torch()
+        self.execute(A, w, V, info)  # warm-up outside the capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.execute(A, w, V, info)
+        return g
 
     def execute_host(self, A, w, V, info, stream=None):
         """Host-buffer run (numpy arenas); copies in/out and synchronizes.

@@ -20,6 +20,7 @@ GLA_STATIC_MAX_N = 128
 GLA_ERR_STATIC_TOO_LARGE = -2001
 GLA_FLAG_SMALL_LOG = 4
 GLA_FLAG_TIMING = 8
+GLA_FLAG_GRAPH = 16
 PHASES = ("tridiag", "chase", "apply", "refine")
 COUNTERS = ("rotations", "sweeps", "row_rotations", "refine_n3", "passes")
 

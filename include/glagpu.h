@@ -18,6 +18,8 @@
  *               threshold after the sweep cap (30*n chases per matrix;
  *               the reference has no cap and never returns on such input)
  *           -1  the referenced triangle held NaN or Inf (outputs are NaN)
+ *           -2  (GLA_FLAG_GRAPH plans only) the chase needed more passes than
+ *               the captured sequence holds (outputs are not valid)
  *
  * Buffers are caller-owned; the library owns only plans and their
  * workspace. All pointers passed to *_execute are device pointers unless
@@ -51,6 +53,11 @@ extern "C" {
 /* Flag bit: record CUDA events around each phase of every execute (see
  * gla_plan_phase_times). */
 #define GLA_FLAG_TIMING 8
+/* Flag bit: capture-safe execute for CUDA graphs. gla_plan_execute then never
+ * synchronizes the host: it enqueues a fixed four chase passes (8 n^2
+ * rotations, twice what random spectra need) and a matrix that would need more
+ * is reported with info = -2 instead of being finished by extra passes. */
+#define GLA_FLAG_GRAPH 16
 
 /* Phases reported by gla_plan_phase_times. */
 #define GLA_PHASE_TRIDIAG 0 /* symtri! + Array(Q)          */

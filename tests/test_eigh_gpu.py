@@ -265,3 +265,33 @@ def test_multi_pass_chase_identical(G):
         plan.close()
     assert outs[0][2] <= 2 and outs[1][2] > 3
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32_refined"])
+def test_cuda_graph_capture_and_replay(G, precision):
+    # the batched solve captured once, replayed on two different inputs:
+    # bit-identical to the uncaptured execute of each input
+    import torch
+    rng = np.random.default_rng(12)
+    sizes = list(rng.integers(1, 129, size=50))
+    mats1 = batch_mats(12, sizes)
+    mats2 = batch_mats(13, sizes)
+    ref = G.Plan(sizes, precision=precision)
+    gp = G.Plan(sizes, precision=precision, graph=True)
+    A = gp.pack(mats1, device="cuda")
+    w = torch.empty(gp.w_elems, dtype=torch.float64, device="cuda")
+    V = torch.empty(gp.a_elems, dtype=torch.float64, device="cuda")
+    info = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    g = gp.capture(A, w, V, info)
+    for mats in (mats2, mats1):
+        A.copy_(gp.pack(mats, device="cuda"))
+        g.replay()
+        torch.cuda.synchronize()
+        A2 = ref.pack(mats, device="cuda")
+        w2 = torch.empty_like(w)
+        V2 = torch.empty_like(V)
+        info2 = torch.zeros_like(info)
+        ref.execute(A2, w2, V2, info2)
+        torch.cuda.synchronize()
+        assert (info.cpu().numpy() == 0).all()
+        assert torch.equal(w, w2) and torch.equal(V, V2)
