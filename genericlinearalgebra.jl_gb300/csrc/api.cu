@@ -25,6 +25,7 @@
 
 #include "../../include/glagpu.h"
 #include "gla_launch.h"
+#include "gla_adjoint.h"
 #include "gla_refine.h"
 
 using namespace gla;
@@ -113,6 +114,7 @@ struct gla_plan_s {
   void* h_V = nullptr;
   int* h_info = nullptr;
   int* pin_pending = nullptr;
+  df64* d_adj = nullptr;  // adjoint workspace (allocated by the first gla_plan_adjoint)
   cudaStream_t last_stream = nullptr;
   int last_passes = 0;
   cudaEvent_t fork = nullptr;
@@ -320,6 +322,7 @@ int gla_plan_destroy(gla_plan_t p) {
   cudaFree(p->h_V);
   cudaFree(p->h_info);
   cudaFreeHost(p->pin_pending);
+  cudaFree(p->d_adj);
   delete p;
   return 0;
 }
@@ -512,6 +515,24 @@ int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* 
   int bad = 0;
   for (int64_t b = 0; b < p->batch; b++) bad += info_host[b] != 0;
   return bad;
+}
+
+int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const double* wbar, const double* Vbar,
+                     double* Abar, double gap_rel, void* stream) {
+  if (!p) return -1;
+  if (p->prec == GLA_PREC_F32) return -1;  // the adjoint works on FP64 eigenpairs
+  if (!w && p->w_elems) return -2;
+  if (!V && p->a_elems) return -3;
+  if (!wbar && p->w_elems) return -4;
+  if (!Vbar && p->a_elems) return -5;
+  if (!Abar && p->a_elems) return -6;
+  if (!(gap_rel == gap_rel)) return -7;
+  if (p->nwork == 0) return 0;
+  if (!p->d_adj) GLA_CUDA(cudaMalloc((void**)&p->d_adj, adjoint_workspace_bytes(p->a_elems)));
+  cudaStream_t st = (cudaStream_t)stream;
+  GLA_CUDA(launch_adjoint(p->nwork, st, p->d_desc, p->d_perm_bucket, w, V, wbar, Vbar, Abar, p->d_adj, p->a_elems,
+                          gap_rel > 0 ? gap_rel : 1e-10));
+  return 0;
 }
 
 int gla_plan_phase_times(gla_plan_t p, float* ms) {

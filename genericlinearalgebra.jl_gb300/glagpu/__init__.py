@@ -174,6 +174,14 @@ class Plan:
                                                _stream_ptr(stream) if stream is not None else None)
         return _lib.check(rc, "gla_plan_execute_host")
 
+    def adjoint(self, w, V, wbar, Vbar, Abar, gap_rel=0.0, stream=None):
+        """Abar = V (diag(wbar) + sym(F o V'Vbar)) V' for every matrix (torch CUDA
+        arenas, FP64, packed like execute's outputs). Asynchronous."""
+        rc = _lib.load().gla_plan_adjoint(self._h, C.c_void_p(w.data_ptr()), C.c_void_p(V.data_ptr()),
+                                          C.c_void_p(wbar.data_ptr()), C.c_void_p(Vbar.data_ptr()),
+                                          C.c_void_p(Abar.data_ptr()), float(gap_rel), _stream_ptr(stream))
+        return _lib.check(rc, "gla_plan_adjoint")
+
     def stats(self):
         """Work counters of the last execute (rotations, sweeps, row_rotations,
         refine_n3, passes)."""
@@ -280,6 +288,52 @@ def _tridiag(T, jobz, alg, tol):
     return d if on_dev else d.cpu().numpy()
 
 
+class _EighFunction:
+    """torch.autograd.Function for the batched eigen-decomposition of a list of
+    same-plan symmetric matrices (the Python counterpart of an rrule for
+    eigen): forward = gla_plan_execute, backward = gla_plan_adjoint."""
+
+    @staticmethod
+    def build():
+        torch = _torch()
+
+        class Eigh(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, A, plan):
+                w = torch.empty(plan.w_elems, dtype=torch.float64, device=A.device)
+                V = torch.empty(plan.a_elems, dtype=torch.float64, device=A.device)
+                info = torch.zeros(len(plan.ns), dtype=torch.int32, device=A.device)
+                plan.execute(A, w, V, info)
+                _raise_for_info(info.cpu().numpy())
+                ctx.plan = plan
+                ctx.save_for_backward(w, V)
+                return w, V
+
+            @staticmethod
+            def backward(ctx, wbar, Vbar):
+                w, V = ctx.saved_tensors
+                wbar = torch.zeros_like(w) if wbar is None else wbar.contiguous()
+                Vbar = torch.zeros_like(V) if Vbar is None else Vbar.contiguous()
+                Abar = torch.empty_like(V)
+                ctx.plan.adjoint(w, V, wbar, Vbar, Abar)
+                return Abar, None
+
+        return Eigh
+
+
+_eigh_fn = None
+
+
+def eigh_autograd(A, plan):
+    """Differentiable batched eigen-decomposition: A is the packed FP64 arena
+    (torch CUDA tensor, requires_grad allowed), plan a Plan with jobz 'V'.
+    Returns packed (w, V); gradients flow back through gla_plan_adjoint."""
+    global _eigh_fn
+    if _eigh_fn is None:
+        _eigh_fn = _EighFunction.build()
+    return _eigh_fn.apply(A, plan)
+
+
 def eigen(A, uplo="L", tol=None, precision="f64", alg="QL"):
     """eigen(Hermitian(A, uplo)) / eigen(SymTridiagonal): ascending values and
     the matching orthonormal eigenvectors (columns)."""
@@ -295,5 +349,5 @@ def eigvals(A, uplo="L", tol=None, precision="f64"):
     return eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
 
 
-__all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigvals", "eigen_batched", "eigvals_batched",
+__all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N"]

@@ -117,6 +117,21 @@ int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, voi
                           void* stream);
 
 /*
+ * Adjoint of the plan's eigen-decomposition (reverse mode; the kernel behind
+ * an rrule / autograd rule for eigen, no counterpart in the reference).
+ * Inputs, packed like the execute outputs (FP64, device): w and V, the
+ * eigenpairs; wbar and Vbar, the cotangents of the loss with respect to them.
+ * Output Abar (packed like A, full symmetric matrices):
+ *     Abar = V (diag(wbar) + sym(F o (V' Vbar))) V',  sym(X) = (X + X')/2,
+ *     F_ij = 1/(w_j - w_i) when |w_j - w_i| > gap_rel * max|w|, else 0.
+ * gap_rel <= 0 selects 1e-10. Products in double-float arithmetic (~1e-14).
+ * The first call allocates the adjoint workspace (32 bytes per arena
+ * element); later calls allocate nothing. Asynchronous on `stream`.
+ */
+int gla_plan_adjoint(gla_plan_t plan, const double* w, const double* V, const double* wbar, const double* Vbar,
+                     double* Abar, double gap_rel, void* stream);
+
+/*
  * Statistics of the last execute: total Givens rotations applied to the
  * eigenvectors, implicit-shift chases and chase passes. Synchronizes the
  * plan's last stream.

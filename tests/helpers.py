@@ -77,3 +77,21 @@ def vec_parity(A, V1, V2, w, tol_factor=1.0):
         err = min(np.linalg.norm(V1[:, j] - V2[:, j]), np.linalg.norm(V1[:, j] + V2[:, j]))
         worst = max(worst, err / max(bound, 1e-15))
     return worst
+
+
+def gapped_spectrum(n, rng, gap=1e-3):
+    """Sorted values in [-1, 1] with consecutive gaps >= gap (the adjoint configuration)."""
+    u = np.sort(rng.random(n))
+    return -1.0 + (2.0 - (n - 1) * gap) * u + gap * np.arange(n)
+
+
+def analytic_adjoint(V, w, wbar, Vbar, gap_rel=1e-10):
+    """Abar = V (diag(wbar) + sym(F o V'Vbar)) V' in numpy (FP64)."""
+    n = len(w)
+    G = V.T @ Vbar
+    dl = w[None, :] - w[:, None]  # lam_j - lam_i
+    with np.errstate(divide="ignore"):
+        F = np.where(np.abs(dl) > gap_rel * np.abs(w).max(), 1.0 / np.where(dl == 0, 1, dl), 0.0)
+    np.fill_diagonal(F, 0.0)
+    M = 0.5 * (F * G + (F * G).T) + np.diag(wbar)
+    return V @ M @ V.T
