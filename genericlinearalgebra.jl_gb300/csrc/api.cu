@@ -26,6 +26,7 @@
 #include "../../include/glagpu.h"
 #include "gla_launch.h"
 #include "gla_adjoint.h"
+#include "gla_large.h"
 #include "gla_refine.h"
 
 using namespace gla;
@@ -115,6 +116,10 @@ struct gla_plan_s {
   int* h_info = nullptr;
   int* pin_pending = nullptr;
   df64* d_adj = nullptr;  // adjoint workspace (allocated by the first gla_plan_adjoint)
+  // orders above GLA_MAX_SMALL_N: solved one at a time by the large path
+  std::vector<int> large_idx;           // batch indices, in batch order
+  std::map<int, LargeCtx*> large_ctx;   // one context per distinct order
+  int* h_large_info = nullptr;          // pinned, one word per large matrix
   cudaStream_t last_stream = nullptr;
   int last_passes = 0;
   cudaEvent_t fork = nullptr;
@@ -142,6 +147,7 @@ const char* gla_status_string(int status) {
   if (status == 0) return "success";
   if (status > 0) return "some matrices did not converge or held non-finite values (see info)";
   if (status == GLA_ERR_STATIC_TOO_LARGE) return "order exceeds GLA_STATIC_MAX_N (128) for gla_dsyev_static";
+  if (status == GLA_ERR_UNSUPPORTED) return "operation not supported for this plan (see glagpu.h)";
   if (status <= -1000) return cudaGetErrorString((cudaError_t)(-1000 - status));
   switch (status) {
     case -1: return "invalid argument 1";
@@ -168,8 +174,15 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   if (batch < 0) return -5;
   if (batch > 0 && !n) return -6;
   for (int64_t b = 0; b < batch; b++)
-    if (n[b] < 0 || n[b] > GLA_MAX_SMALL_N) return -6;
+    if (n[b] < 0 || n[b] > GLA_MAX_N) return -6;
   if (!(tol == tol)) return -7;
+  {
+    bool any_large = false;
+    for (int64_t b = 0; b < batch; b++) any_large |= n[b] > GLA_MAX_SMALL_N;
+    // large orders: no refinement and no capture-safe mode yet
+    if (any_large && precision == GLA_PREC_F32_REFINED) return -2;
+    if (any_large && (flags & GLA_FLAG_GRAPH)) return -8;
+  }
   if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH)) != 0 || (flags & 3) > GLA_ALG_QR)
     return -8;
   GLA_CUDA(ensure_init());
@@ -198,13 +211,17 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     d.w_off = woff;
     d.rot_off = roff;
     d.hdr_off = hoff;
-    d.rot_cap = (flags & GLA_FLAG_SMALL_LOG) ? nb * nb / 8 + nb : kRotPerN2 * nb * nb + 4;
-    d.hdr_cap = (flags & GLA_FLAG_SMALL_LOG) ? nb / 4 + 2 : kHdrPerN * nb + 4;
+    const bool large = nb > GLA_MAX_SMALL_N;
+    d.rot_cap = large ? 0 : (flags & GLA_FLAG_SMALL_LOG) ? nb * nb / 8 + nb : kRotPerN2 * nb * nb + 4;
+    d.hdr_cap = large ? 0 : (flags & GLA_FLAG_SMALL_LOG) ? nb / 4 + 2 : kHdrPerN * nb + 4;
     aoff += (int64_t)nb * nb;
     woff += nb;
     roff += d.rot_cap;
     hoff += d.hdr_cap;
-    p->nmax = std::max(p->nmax, nb);
+    if (large)
+      p->large_idx.push_back((int)b);
+    else
+      p->nmax = std::max(p->nmax, nb);
   }
   p->a_elems = aoff;
   p->w_elems = woff;
@@ -212,7 +229,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   // ---- size buckets (descending order inside each bucket), chase order
   std::vector<int> idx;
   for (int64_t b = 0; b < batch; b++)
-    if (n[b] >= 1) idx.push_back((int)b);
+    if (n[b] >= 1 && n[b] <= GLA_MAX_SMALL_N) idx.push_back((int)b);
   p->nwork = (int)idx.size();
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return n[a] > n[b]; });
   std::vector<int> perm_bucket;
@@ -293,6 +310,20 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&bk.stream, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&bk.join, cudaEventDisableTiming);
   }
+  if (err == cudaSuccess && !p->large_idx.empty())
+    err = cudaMallocHost((void**)&p->h_large_info, sizeof(int) * p->large_idx.size());
+  for (int b : p->large_idx) {
+    if (err != cudaSuccess) break;
+    const int nb = (int)n[b];
+    if (p->large_ctx.count(nb)) continue;
+    LargeCtx* c = nullptr;
+    int rc = large_create(&c, nb, precision == GLA_PREC_F64);
+    if (rc) {
+      gla_plan_destroy(p);
+      return rc;
+    }
+    p->large_ctx[nb] = c;
+  }
   if (p->timing)
     for (int b = 0; b < kMaxBuckets && err == cudaSuccess; b++)
       for (int ph = 0; ph < GLA_NUM_PHASES && err == cudaSuccess; ph++)
@@ -323,6 +354,8 @@ int gla_plan_destroy(gla_plan_t p) {
   cudaFree(p->h_info);
   cudaFreeHost(p->pin_pending);
   cudaFree(p->d_adj);
+  for (auto& kv : p->large_ctx) large_destroy(kv.second);
+  cudaFreeHost(p->h_large_info);
   delete p;
   return 0;
 }
@@ -386,10 +419,63 @@ int run_passes_sync(gla_plan_t p, int b, int tcode, void* V, void* wout, int* in
   return 0;
 }
 
+}  // namespace
+
+namespace gla {
+
+// Batched SymTridiagonal solve over a plan's buckets: (din, ein) in the
+// plan's arena layout (entry i of matrix b at w_off + i), eigenvectors into
+// Q, ascending eigenvalues into w. Synchronises st.
+int plan_stev_batched(gla_plan_s* p, int tcode, const void* din, const void* ein, void* Q, void* w, int* info,
+                      cudaStream_t st) {
+  const int work_t = tcode == kF64 ? kF64 : kF32;
+  GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
+  p->last_stream = st;
+  p->last_passes = 0;
+  for (size_t b = 0; b < p->buckets.size(); b++) {
+    const Bucket& bk = p->buckets[b];
+    GLA_CUDA(launch_init_tridiagonal(work_t, bk.count, st, p->d_desc, p->d_perm_bucket + bk.start, din, ein, p->d_d,
+                                     p->d_e, Q, info, p->d_cst, true));
+  }
+  for (size_t b = 0; b < p->buckets.size(); b++) {
+    int rc = run_passes_sync(p, (int)b, work_t, Q, w, info, nullptr, st, 0);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+}  // namespace gla
+
+namespace {
+
 int enqueue_refine(gla_plan_t p, int b, const void* A, int lower, void* Vout, void* w, int* info, cudaStream_t st) {
   const Bucket& bk = p->buckets[b];
   GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
                          lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats));
+  return 0;
+}
+
+// Matrices above the small-matrix limit, one at a time on the caller's
+// stream (each large solve uses the whole GPU).
+int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaStream_t st) {
+  const size_t ioe = p->io_elem();
+  for (size_t k = 0; k < p->large_idx.size(); k++) {
+    const int b = p->large_idx[k];
+    const int nb = (int)p->n[b];
+    // offsets of matrix b in the packed arenas
+    int64_t aoff = 0, woff = 0;
+    for (int q = 0; q < b; q++) {
+      aoff += p->n[q] * p->n[q];
+      woff += p->n[q];
+    }
+    const int tc = p->prec == GLA_PREC_F64 ? kF64 : kF32;
+    int inf = 0;
+    int rc = large_syev(p->large_ctx[nb], tc, p->jobz == 'V', p->uplo == 'L', (const char*)A + ioe * aoff, nb,
+                        (char*)w + ioe * woff, V ? (char*)V + ioe * aoff : nullptr, nb, &inf, st);
+    if (rc) return rc;
+    p->h_large_info[k] = inf;
+    GLA_CUDA(cudaMemcpyAsync(info + b, p->h_large_info + k, sizeof(int), cudaMemcpyHostToDevice, st));
+  }
   return 0;
 }
 
@@ -403,6 +489,8 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
     for (int ph = 0; ph < GLA_NUM_PHASES; ph++) p->tused[b][ph] = false;
   GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
   if (p->batch) GLA_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * p->batch, st));
+  int rc_large = execute_large(p, A, w, V, info, st);
+  if (rc_large) return rc_large;
   if (p->nwork == 0) return 0;
   const int lower = p->uplo == 'L';
   const bool refined = p->prec == GLA_PREC_F32_REFINED;
@@ -527,6 +615,7 @@ int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const doubl
   if (!Vbar && p->a_elems) return -5;
   if (!Abar && p->a_elems) return -6;
   if (!(gap_rel == gap_rel)) return -7;
+  if (!p->large_idx.empty()) return GLA_ERR_UNSUPPORTED;  // one-CTA adjoint: orders <= GLA_MAX_SMALL_N
   if (p->nwork == 0) return 0;
   if (!p->d_adj) GLA_CUDA(cudaMalloc((void**)&p->d_adj, adjoint_workspace_bytes(p->a_elems)));
   cudaStream_t st = (cudaStream_t)stream;
@@ -548,6 +637,15 @@ int gla_plan_phase_times(gla_plan_t p, float* ms) {
       GLA_CUDA(cudaEventElapsedTime(&t, p->tev[b][ph][0], p->tev[b][ph][1]));
       ms[ph] += t;
     }
+  // large matrices: tridiagonalisation, divide and conquer (reported as the
+  // chase phase), back-transformation (reported as apply)
+  for (int b : p->large_idx) {
+    float st[3];
+    large_stage_ms(p->large_ctx[(int)p->n[b]], st);
+    ms[GLA_PHASE_TRIDIAG] += st[0];
+    ms[GLA_PHASE_CHASE] += st[1];
+    ms[GLA_PHASE_APPLY] += st[2];
+  }
   return 0;
 }
 
@@ -619,7 +717,7 @@ template <class T>
 int syev_single(int prec, char jobz, char uplo, int64_t n, T* A, int64_t lda, T* w, int* info, void* stream) {
   if (jobz != 'V' && jobz != 'N') return -1;
   if (uplo != 'L' && uplo != 'U') return -2;
-  if (n < 0 || n > GLA_MAX_SMALL_N) return -3;
+  if (n < 0 || n > GLA_MAX_N) return -3;
   if (!A && n) return -4;
   if (lda < std::max<int64_t>(1, n)) return -5;
   if (!w && n) return -6;

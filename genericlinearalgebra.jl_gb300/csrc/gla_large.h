@@ -1,0 +1,79 @@
+// Internal interface of the large-matrix (n > 128) path: blocked
+// tridiagonalisation, divide-and-conquer tridiagonal eigensolver,
+// back-transformation and the drivers that chain them.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gemm_simt.cuh"
+
+struct gla_plan_s;
+
+namespace gla {
+
+constexpr int kLargeMaxN = 16384;
+constexpr int kSytrdNB = 32;    // panel width of the tridiagonalisation
+constexpr int kBacktrNB = 64;   // reflectors per compact-WY block of the back-transformation
+
+// ---- GEMM launchers (gemm_simt.cuh). With splits > 1, g.ksplit and
+// g.split_stride describe the split-K partial outputs written to g.C.
+cudaError_t gemm_launch(bool f64, bool ta, bool tb, bool lower, const GemmDesc& g, int splits, cudaStream_t st);
+// Problems whose sizes are only known on the device: one launch over
+// nprob descriptors, grid sized for max_m x max_n outputs (A, B not transposed).
+cudaError_t gemm_launch_grouped(bool f64, const GemmDesc* d_descs, int nprob, int max_m, int max_n, cudaStream_t st);
+
+// ---- stage plans (one order, one working precision)
+struct SytrdPlan;
+cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64);
+void sytrd_plan_destroy(SytrdPlan* p);
+cudaError_t sytrd_enqueue(SytrdPlan* p, void* A, long long lda, void* d, void* e, void* tau, cudaStream_t st);
+int* sytrd_error_word(SytrdPlan* p);
+
+struct DcPlan;
+int dc_plan_create(DcPlan** out, int n, bool f64);
+void dc_plan_destroy(DcPlan* p);
+// Z has leading dimension n; info gets one word per leaf.
+int dc_enqueue(DcPlan* p, void* d, const void* e, void* Z, int* leaf_info, cudaStream_t st);
+int* dc_fail_word(DcPlan* p);
+int dc_leaf_count(const DcPlan* p);
+size_t dc_plan_bytes(const DcPlan* p);
+
+struct BacktrPlan;
+int backtr_plan_create(BacktrPlan** out, int n, bool f64);
+void backtr_plan_destroy(BacktrPlan* p);
+int backtr_enqueue(BacktrPlan* p, const void* A, long long lda, const void* tau, void* Z, long long ldz,
+                   cudaStream_t st);
+
+// ---- large-path context: workspace for one order n and one working precision
+struct LargeCtx;
+int large_create(LargeCtx** out, int n, bool f64);
+void large_destroy(LargeCtx* c);
+size_t large_workspace_bytes(const LargeCtx* c);
+// Stage times of the last large_syev (ms): tridiagonalisation (with the
+// load), divide and conquer, back-transformation (with the store).
+void large_stage_ms(const LargeCtx* c, float* ms3);
+
+// Householder tridiagonalisation of the lower triangle of A (n x n, leading
+// dimension lda, working precision), in place: d, e, tau and the reflectors
+// below the subdiagonal (symtri! layout, unit element implicit).
+int large_sytrd(LargeCtx* c, void* A, long long lda, void* d, void* e, void* tau, cudaStream_t st);
+// Eigenpairs of the symmetric tridiagonal (d, e): d becomes the ascending
+// eigenvalues, Z (ldz) the eigenvectors. info: 0, or > 0 if a subproblem
+// did not converge.
+int large_stedc(LargeCtx* c, void* d, const void* e, void* Z, long long ldz, int* info, cudaStream_t st);
+// Z := Q Z with Q = H_0 H_1 ... H_{n-2} from large_sytrd.
+int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void* Z, long long ldz, cudaStream_t st);
+// Full eigen-decomposition of one matrix. tcode: kF64, kF32 or kF32FromF64
+// (double input solved in FP32; outputs float). Ain has leading dimension
+// lda and uplo 'L'/'U'; w gets the ascending eigenvalues, V (ldv) the
+// eigenvectors when wantv. *info_host: 0, -1 (non-finite input), > 0
+// unconverged. Synchronises st before returning.
+int large_syev(LargeCtx* c, int tcode, bool wantv, bool lower, const void* Ain, long long lda, void* w, void* V,
+               long long ldv, int* info_host, cudaStream_t st);
+
+// ---- leaf solves of the divide and conquer: a batched small-matrix plan
+// over the leaf orders, fed with tridiagonal (d, e) in its arena layout.
+int plan_stev_batched(gla_plan_s* p, int tcode, const void* din, const void* ein, void* Q, void* w, int* info,
+                      cudaStream_t st);
+
+}  // namespace gla

@@ -30,7 +30,7 @@ from collections import namedtuple
 import numpy as np
 
 from . import _lib
-from ._lib import GLA_ALG_QL, GLA_ALG_QR, GLA_MAX_SMALL_N, GLAError
+from ._lib import GLA_ALG_QL, GLA_ALG_QR, GLA_MAX_N, GLA_MAX_SMALL_N, GLAError
 
 Eigen = namedtuple("Eigen", ["values", "vectors"])
 
@@ -92,7 +92,8 @@ def _raise_for_info(info):
 
 
 class Plan:
-    """Batched solver plan over matrices of orders `ns` (each <= 128).
+    """Batched solver plan over matrices of orders `ns` (each <= GLA_MAX_N;
+    orders above GLA_MAX_SMALL_N = 128 run the blocked large-matrix path).
 
     Arena layout: matrix b is column-major n_b x n_b at offset sum(n_c^2, c<b);
     its eigenvalues at sum(n_c, c<b). precision: "f64", "f32", "f32_refined".
@@ -102,8 +103,8 @@ class Plan:
                  timing=False, graph=False):
         L = _lib.load()
         ns = np.ascontiguousarray(np.asarray(ns, dtype=np.int64))
-        if (ns < 0).any() or (ns > GLA_MAX_SMALL_N).any():
-            raise DimensionMismatch(f"orders must lie in [0, {GLA_MAX_SMALL_N}]")
+        if (ns < 0).any() or (ns > GLA_MAX_N).any():
+            raise DimensionMismatch(f"orders must lie in [0, {GLA_MAX_N}]")
         self.ns = ns
         self.precision = precision
         self.jobz = jobz
@@ -350,4 +351,4 @@ def eigvals(A, uplo="L", tol=None, precision="f64"):
 
 
 __all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
-           "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N"]
+           "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

@@ -16,8 +16,10 @@ GLA_PREC_F32_REFINED = 2
 GLA_ALG_QL = 0
 GLA_ALG_QR = 1
 GLA_MAX_SMALL_N = 128
+GLA_MAX_N = 16384
 GLA_STATIC_MAX_N = 128
 GLA_ERR_STATIC_TOO_LARGE = -2001
+GLA_ERR_UNSUPPORTED = -2002
 GLA_FLAG_SMALL_LOG = 4
 GLA_FLAG_TIMING = 8
 GLA_FLAG_GRAPH = 16

@@ -12,6 +12,7 @@
  *           <0  argument -status is invalid (LAPACK xerbla convention)
  *         -1000 - e  CUDA runtime error e (see gla_status_string)
  *         -2001 order above GLA_STATIC_MAX_N (gla_dsyev_static only)
+ *         -2002 operation not supported for this plan
  *           >0  number of matrices whose per-matrix info is nonzero
  *   info[b]  0  converged
  *           >0  number of off-diagonal entries still above the deflation
@@ -66,9 +67,12 @@ extern "C" {
 #define GLA_PHASE_REFINE 3  /* Ogita-Aishima refinement    */
 #define GLA_NUM_PHASES 4
 
-#define GLA_MAX_SMALL_N 128
+#define GLA_MAX_SMALL_N 128   /* largest order of the batched one-CTA-per-matrix path */
+#define GLA_MAX_N 16384       /* largest order accepted by plans (orders above
+                                 GLA_MAX_SMALL_N run the blocked large-matrix path) */
 #define GLA_STATIC_MAX_N 128
 #define GLA_ERR_STATIC_TOO_LARGE (-2001)
+#define GLA_ERR_UNSUPPORTED (-2002) /* e.g. gla_plan_adjoint on a plan with orders > GLA_MAX_SMALL_N */
 
 typedef struct gla_plan_s* gla_plan_t;
 
@@ -77,7 +81,14 @@ const char* gla_status_string(int status);
 
 /*
  * Batched plan over `batch` independent real symmetric matrices of orders
- * n[0..batch) (host array, 0 <= n[b] <= GLA_MAX_SMALL_N).
+ * n[0..batch) (host array, 0 <= n[b] <= GLA_MAX_N).
+ *
+ * Orders up to GLA_MAX_SMALL_N are solved together (one CTA per matrix,
+ * size-bucketed). Larger orders are solved one at a time with the whole GPU:
+ * blocked Householder tridiagonalisation, divide and conquer on the
+ * tridiagonal, compact-WY back-transformation; such plans synchronise the
+ * stream inside execute and do not support GLA_FLAG_GRAPH or
+ * GLA_PREC_F32_REFINED (those return -8 / -2).
  *
  * Packed arena layout used by the execute calls: matrix b is n[b] x n[b],
  * column-major with leading dimension n[b], at element offset

@@ -1,0 +1,178 @@
+"""Large-order path (n > 128: blocked tridiagonalisation, divide and conquer,
+compact-WY back-transformation) against the CPU oracle (the reference's QL
+algorithm restated) and LAPACK (numpy), on GOE, prescribed-spectrum,
+clustered (deflation-heavy) and diagonal inputs, in FP64 and FP32."""
+import numpy as np
+import pytest
+
+from helpers import goe, orth, prescribed, residual, sym_from
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import glagpu
+    return glagpu
+
+
+def solve(G, mats, precision="f64", uplo="L", jobz="V"):
+    import torch
+    plan = G.Plan([m.shape[0] for m in mats], precision=precision, jobz=jobz, uplo=uplo)
+    dt = torch.float32 if precision == "f32" else torch.float64
+    A = plan.pack(mats, device="cuda").to(dt)
+    w = torch.empty(plan.w_elems, dtype=dt, device="cuda")
+    V = torch.empty(plan.a_elems, dtype=dt, device="cuda") if jobz == "V" else None
+    info = torch.zeros(len(mats), dtype=torch.int32, device="cuda")
+    plan.execute(A, w, V, info)
+    torch.cuda.synchronize()
+    ws, Vs = plan.unpack(w.cpu().numpy().astype(np.float64), V.cpu().numpy().astype(np.float64) if V is not None else None)
+    return ws, Vs, info.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [129, 200, 257, 300])
+def test_f64_goe_vs_oracle(G, n):
+    A = goe(n, 1000 + n)
+    ws, Vs, info = solve(G, [A])
+    assert info[0] == 0
+    wo, Vo, _ = O.syev(A)
+    nA = np.linalg.norm(A, 2)
+    assert np.max(np.abs(ws[0] - wo)) <= 1e-13 * nA
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+    # eigenvectors equal the oracle's up to sign (the spectrum is simple)
+    dots = np.abs(np.sum(Vs[0] * Vo, axis=0))
+    gaps = np.minimum(np.diff(wo, prepend=-np.inf), np.diff(wo, append=np.inf))
+    ok = gaps > 1e-8 * nA
+    assert np.all(np.abs(dots[ok] - 1) <= 1e-6)
+
+
+@pytest.mark.parametrize("n", [513, 1024])
+def test_f64_goe_vs_lapack(G, n):
+    A = goe(n, 2000 + n)
+    ws, Vs, info = solve(G, [A])
+    assert info[0] == 0
+    wl = np.linalg.eigvalsh(A)
+    nA = np.linalg.norm(A, 2)
+    assert np.max(np.abs(ws[0] - wl)) <= 1e-13 * nA
+    assert residual(A, Vs[0], ws[0]) <= 2e-13
+    assert orth(Vs[0]) <= 2e-13
+
+
+def test_f64_prescribed_cond1e6(G):
+    n = 512
+    rng = np.random.default_rng(3)
+    lam = np.logspace(-6, 0, n) * rng.choice([-1.0, 1.0], n)
+    A = prescribed(lam, 7)
+    ws, Vs, info = solve(G, [A])
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.sort(lam))) <= 1e-13
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+def test_f64_clustered_deflation(G):
+    # multiplicities and near-multiplicities: exercises both deflation kinds
+    n = 300
+    rng = np.random.default_rng(5)
+    lam = np.concatenate([np.full(100, 1.0), np.full(80, -2.0), 1.0 + 1e-13 * rng.standard_normal(20),
+                          rng.uniform(-3, 3, n - 200)])
+    A = prescribed(lam, 9)
+    ws, Vs, info = solve(G, [A])
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.sort(lam))) <= 1e-13 * 3
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+def test_f64_diagonal_and_split_tridiagonal(G):
+    n = 200
+    D = np.diag(np.linspace(-1, 1, n)[np.random.default_rng(1).permutation(n)])
+    ws, Vs, info = solve(G, [D])
+    assert info[0] == 0
+    assert np.array_equal(ws[0], np.sort(np.diag(D)))
+    assert residual(D, Vs[0], ws[0]) == 0.0
+    assert orth(Vs[0]) <= 1e-15
+    # block-diagonal: the tridiagonal has exact zeros inside
+    B = np.zeros((260, 260))
+    B[:130, :130] = goe(130, 4)
+    B[130:, 130:] = goe(130, 5)
+    ws, Vs, info = solve(G, [B])
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.linalg.eigvalsh(B))) <= 1e-13 * np.linalg.norm(B, 2)
+    assert residual(B, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_f64_uplo_reads_one_triangle(G, uplo):
+    n = 170
+    A = goe(n, 77)
+    junk = A.copy()
+    if uplo == "L":
+        junk[np.triu_indices(n, 1)] = np.nan
+    else:
+        junk[np.tril_indices(n, -1)] = np.nan
+    ws, Vs, info = solve(G, [junk], uplo=uplo)
+    assert info[0] == 0
+    S = sym_from(A, uplo)
+    assert np.max(np.abs(ws[0] - np.linalg.eigvalsh(S))) <= 1e-13 * np.linalg.norm(S, 2)
+    assert residual(S, Vs[0], ws[0]) <= 1e-13
+
+
+def test_mixed_small_and_large_plan(G):
+    mats = [goe(50, 1), goe(300, 2), goe(7, 3), goe(129, 4), goe(128, 5)]
+    ws, Vs, info = solve(G, mats)
+    assert (info == 0).all()
+    for A, w, V in zip(mats, ws, Vs):
+        assert np.max(np.abs(w - np.linalg.eigvalsh(A))) <= 1e-13 * np.linalg.norm(A, 2)
+        assert residual(A, V, w) <= 1e-13
+        assert orth(V) <= 1e-13
+
+
+def test_eigvals_only_large(G):
+    A = goe(400, 8)
+    ws, _, info = solve(G, [A], jobz="N")
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.linalg.eigvalsh(A))) <= 1e-13 * np.linalg.norm(A, 2)
+
+
+@pytest.mark.parametrize("n", [129, 333, 800])
+def test_f32_goe(G, n):
+    A = goe(n, 3000 + n)
+    ws, Vs, info = solve(G, [A.astype(np.float32)], precision="f32")
+    assert info[0] == 0
+    A32 = A.astype(np.float32).astype(np.float64)
+    nA = np.linalg.norm(A32, 2)
+    # FP32 working precision: ~n^0.5 ulps of residual and orthogonality
+    assert np.max(np.abs(ws[0] - np.linalg.eigvalsh(A32))) <= 1e-5 * nA
+    assert residual(A32, Vs[0], ws[0]) <= 1e-5
+    assert orth(Vs[0]) <= 1e-5
+
+
+def test_large_nonfinite_input(G):
+    A = goe(150, 9)
+    A[70, 3] = np.inf
+    ws, Vs, info = solve(G, [A])
+    assert info[0] == -1
+    assert np.isnan(ws[0]).all()
+
+
+def test_large_deterministic(G):
+    A = goe(260, 10)
+    r1 = solve(G, [A])
+    r2 = solve(G, [A])
+    assert np.array_equal(r1[0][0], r2[0][0]) and np.array_equal(r1[1][0], r2[1][0])
+
+
+def test_large_adjoint_unsupported(G):
+    import torch
+    plan = G.Plan([200])
+    z = torch.zeros(plan.a_elems, dtype=torch.float64, device="cuda")
+    zw = torch.zeros(plan.w_elems, dtype=torch.float64, device="cuda")
+    with pytest.raises(G.GLAError):
+        plan.adjoint(zw, z, zw, z, z)
