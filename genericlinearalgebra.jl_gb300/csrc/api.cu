@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <map>
 #include <mutex>
 #include <new>
@@ -119,6 +120,10 @@ struct gla_plan_s {
   // orders above GLA_MAX_SMALL_N: solved one at a time by the large path
   std::vector<int> large_idx;           // batch indices, in batch order
   std::map<int, LargeCtx*> large_ctx;   // one context per distinct order
+  std::map<int, RefineLarge*> large_ref;  // F32_REFINED: refinement per distinct order
+  int large_iters = 0;                  // refinement iterations of the last execute (max)
+  double large_refine_n3 = 0;           // sum over large matrices of iterations * n^3
+  float large_refine_ms = 0.f;          // host-timed refinement of the last execute
   int* h_large_info = nullptr;          // pinned, one word per large matrix
   cudaStream_t last_stream = nullptr;
   int last_passes = 0;
@@ -179,8 +184,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   {
     bool any_large = false;
     for (int64_t b = 0; b < batch; b++) any_large |= n[b] > GLA_MAX_SMALL_N;
-    // large orders: no refinement and no capture-safe mode yet
-    if (any_large && precision == GLA_PREC_F32_REFINED) return -2;
+    // large orders: no capture-safe mode (their solves synchronise)
     if (any_large && (flags & GLA_FLAG_GRAPH)) return -8;
   }
   if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH)) != 0 || (flags & 3) > GLA_ALG_QR)
@@ -323,6 +327,15 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
       return rc;
     }
     p->large_ctx[nb] = c;
+    if (precision == GLA_PREC_F32_REFINED) {
+      RefineLarge* r = nullptr;
+      rc = refine_large_create(&r, nb);
+      if (rc) {
+        gla_plan_destroy(p);
+        return rc;
+      }
+      p->large_ref[nb] = r;
+    }
   }
   if (p->timing)
     for (int b = 0; b < kMaxBuckets && err == cudaSuccess; b++)
@@ -355,6 +368,7 @@ int gla_plan_destroy(gla_plan_t p) {
   cudaFreeHost(p->pin_pending);
   cudaFree(p->d_adj);
   for (auto& kv : p->large_ctx) large_destroy(kv.second);
+  for (auto& kv : p->large_ref) refine_large_destroy(kv.second);
   cudaFreeHost(p->h_large_info);
   delete p;
   return 0;
@@ -459,6 +473,9 @@ int enqueue_refine(gla_plan_t p, int b, const void* A, int lower, void* Vout, vo
 // stream (each large solve uses the whole GPU).
 int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaStream_t st) {
   const size_t ioe = p->io_elem();
+  p->large_iters = 0;
+  p->large_refine_n3 = 0;
+  p->large_refine_ms = 0.f;
   for (size_t k = 0; k < p->large_idx.size(); k++) {
     const int b = p->large_idx[k];
     const int nb = (int)p->n[b];
@@ -468,11 +485,36 @@ int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cuda
       aoff += p->n[q] * p->n[q];
       woff += p->n[q];
     }
-    const int tc = p->prec == GLA_PREC_F64 ? kF64 : kF32;
+    const void* Ab = (const char*)A + ioe * aoff;
+    void* wb = (char*)w + ioe * woff;
+    void* Vb = (p->jobz == 'V' && V) ? (char*)V + ioe * aoff : nullptr;
     int inf = 0;
-    int rc = large_syev(p->large_ctx[nb], tc, p->jobz == 'V', p->uplo == 'L', (const char*)A + ioe * aoff, nb,
-                        (char*)w + ioe * woff, V ? (char*)V + ioe * aoff : nullptr, nb, &inf, st);
-    if (rc) return rc;
+    int rc;
+    if (p->prec == GLA_PREC_F32_REFINED) {
+      // FP32 solve of the rounded matrix straight into the refinement's
+      // buffers, then refinement against the FP64 input
+      RefineLarge* r = p->large_ref[nb];
+      rc = large_syev(p->large_ctx[nb], kF32FromF64, true, p->uplo == 'L', Ab, nb, refine_large_wbuf(r),
+                      refine_large_xbuf(r), nb, &inf, st);
+      if (rc) return rc;
+      if (inf == 0) {
+        const auto t0 = std::chrono::steady_clock::now();
+        rc = refine_large_run(r, (const double*)Ab, nb, p->uplo == 'L', refine_large_xbuf(r), nb,
+                              refine_large_wbuf(r), (double*)wb, (double*)Vb, nb, st);
+        p->large_refine_ms +=
+            std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        p->large_refine_n3 += (double)refine_large_iters(r) * nb * (double)nb * nb;
+        if (rc == -1)
+          inf = -1;
+        else if (rc)
+          return rc;
+        p->large_iters = std::max(p->large_iters, refine_large_iters(r));
+      }
+    } else {
+      const int tc = p->prec == GLA_PREC_F64 ? kF64 : kF32;
+      rc = large_syev(p->large_ctx[nb], tc, p->jobz == 'V', p->uplo == 'L', Ab, nb, wb, Vb, nb, &inf, st);
+      if (rc) return rc;
+    }
     p->h_large_info[k] = inf;
     GLA_CUDA(cudaMemcpyAsync(info + b, p->h_large_info + k, sizeof(int), cudaMemcpyHostToDevice, st));
   }
@@ -646,6 +688,7 @@ int gla_plan_phase_times(gla_plan_t p, float* ms) {
     ms[GLA_PHASE_CHASE] += st[1];
     ms[GLA_PHASE_APPLY] += st[2];
   }
+  ms[GLA_PHASE_REFINE] += p->large_refine_ms;
   return 0;
 }
 
@@ -668,7 +711,7 @@ int gla_plan_counters(gla_plan_t p, int64_t* c) {
   c[GLA_COUNTER_ROTATIONS] = (int64_t)h[0];
   c[GLA_COUNTER_SWEEPS] = (int64_t)h[1];
   c[GLA_COUNTER_ROW_ROTATIONS] = (int64_t)h[2];
-  c[GLA_COUNTER_REFINE_N3] = (int64_t)h[3];
+  c[GLA_COUNTER_REFINE_N3] = (int64_t)h[3] + (int64_t)p->large_refine_n3;
   c[GLA_COUNTER_PASSES] = p->last_passes;
   return 0;
 }

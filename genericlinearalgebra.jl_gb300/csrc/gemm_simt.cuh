@@ -54,7 +54,9 @@ struct Vec16<float> {
   using type = float4;
 };
 
-template <class T, bool TA, bool TB, bool LOWER>
+// REMAP: honour a_kidx / b_kidx / c_nidx (plain GEMMs skip the index loads
+// and their registers).
+template <class T, bool TA, bool TB, bool LOWER, bool REMAP>
 __device__ __forceinline__ void gemm_body(const GemmDesc& g, int tile, int split) {
   using Cf = GemmCfg<T>;
   constexpr int BM = Cf::BM, BN = Cf::BN, BK = Cf::BK, TM = Cf::TM, TN = Cf::TN;
@@ -84,11 +86,36 @@ __device__ __forceinline__ void gemm_body(const GemmDesc& g, int tile, int split
   const T* A = (const T*)g.A;
   const T* B = (const T*)g.B;
   const long long lda = g.lda, ldb = g.ldb;
-  const int* akx = g.a_kidx;
-  const int* bkx = g.b_kidx;
+  const int* akx = REMAP ? g.a_kidx : nullptr;
+  const int* bkx = REMAP ? g.b_kidx : nullptr;
 
   T ra[LA], rb[LB];
+  // Without remaps every load of a thread sits at a fixed offset from one
+  // moving pointer (advanced by one k-slab per step).
+  const int i_a0 = TA ? t / BK : t % BM, k_a0 = TA ? t % BK : t / BM;  // element r: e = t + r NT
+  const int j_b0 = TB ? t % BN : t / BK, k_b0 = TB ? t / BN : t % BK;
+  constexpr int DI_A = TA ? NT / BK : 0, DK_A = TA ? 0 : NT / BM;     // per-r steps
+  constexpr int DJ_B = TB ? 0 : NT / BK, DK_B = TB ? NT / BN : 0;
+  const T* pa = A + (TA ? (long long)(row0 + i_a0) * lda + (kbeg + k_a0) : (row0 + i_a0) + (long long)(kbeg + k_a0) * lda);
+  const T* pb = B + (TB ? (col0 + j_b0) + (long long)(kbeg + k_b0) * ldb : (long long)(col0 + j_b0) * ldb + (kbeg + k_b0));
+  const long long step_a = TA ? BK : (long long)BK * lda, step_b = TB ? (long long)BK * ldb : BK;
   auto load = [&](int k0) {
+    if (!REMAP) {
+      const int kofs = k0 - kbeg;
+#pragma unroll
+      for (int r = 0; r < LA; r++) {
+        const int gi = row0 + i_a0 + r * DI_A, gk = k0 + k_a0 + r * DK_A;
+        const long long off = TA ? (long long)r * DI_A * lda : (long long)r * DK_A * lda;
+        ra[r] = (gi < m && gk < kend) ? pa[off + (TA ? kofs : (long long)kofs * lda)] : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < LB; r++) {
+        const int gj = col0 + j_b0 + r * DJ_B, gk = k0 + k_b0 + r * DK_B;
+        const long long off = TB ? (long long)r * DK_B * ldb : (long long)r * DJ_B * ldb;
+        rb[r] = (gj < n && gk < kend) ? pb[off + (TB ? (long long)kofs * ldb : kofs)] : T(0);
+      }
+      return;
+    }
 #pragma unroll
     for (int r = 0; r < LA; r++) {
       const int e = t + r * NT;
@@ -97,7 +124,7 @@ __device__ __forceinline__ void gemm_body(const GemmDesc& g, int tile, int split
       const int gi = row0 + i, gk = k0 + kk;
       T v = T(0);
       if (gi < m && gk < kend) {
-        const long long pk = akx ? (long long)akx[gk] : (long long)gk;
+        const long long pk = (REMAP && akx) ? (long long)akx[gk] : (long long)gk;
         v = TA ? A[pk + (long long)gi * lda] : A[gi + pk * lda];
       }
       ra[r] = v;
@@ -110,12 +137,14 @@ __device__ __forceinline__ void gemm_body(const GemmDesc& g, int tile, int split
       const int gj = col0 + j, gk = k0 + kk;
       T v = T(0);
       if (gj < n && gk < kend) {
-        const long long pk = bkx ? (long long)bkx[gk] : (long long)gk;
+        const long long pk = (REMAP && bkx) ? (long long)bkx[gk] : (long long)gk;
         v = TB ? B[gj + pk * ldb] : B[pk + (long long)gj * ldb];
       }
       rb[r] = v;
     }
   };
+  (void)step_a;
+  (void)step_b;
   auto store = [&](int buf) {
 #pragma unroll
     for (int r = 0; r < LA; r++) {
@@ -177,27 +206,48 @@ __device__ __forceinline__ void gemm_body(const GemmDesc& g, int tile, int split
 
   const T alpha = (T)g.alpha, beta = (T)g.beta;
   const bool split_out = g.ksplit > 0;
+  // rows r0 .. r0+VW-1 of an output column are contiguous: one 16-byte
+  // access when the column start is aligned
+  const bool vec = ((reinterpret_cast<unsigned long long>(C) & 15) == 0) && (g.ldc % VW == 0);
 #pragma unroll
-  for (int v = 0; v < NVM; v++)
+  for (int v = 0; v < NVM; v++) {
+    const int r0 = row0 + v * (BM / NVM) + ty * VW;
+    if (r0 >= m) continue;
 #pragma unroll
-    for (int q = 0; q < VW; q++) {
-      const int r = row0 + v * (BM / NVM) + ty * VW + q;
-      if (r >= m) continue;
+    for (int w = 0; w < NVN; w++)
 #pragma unroll
-      for (int w = 0; w < NVN; w++)
+      for (int s = 0; s < VW; s++) {
+        const int c = col0 + w * (BN / NVN) + tx * VW + s;
+        if (c >= n) continue;
+        const long long pc = (REMAP && g.c_nidx) ? (long long)g.c_nidx[c] : (long long)c;
+        T* p = C + r0 + pc * g.ldc;
+        if (vec && r0 + VW <= m && (!LOWER || r0 >= c)) {
+          V out;
+          T* o = reinterpret_cast<T*>(&out);
+          if (split_out || beta == T(0)) {
 #pragma unroll
-        for (int s = 0; s < VW; s++) {
-          const int c = col0 + w * (BN / NVN) + tx * VW + s;
-          if (c >= n || (LOWER && r < c)) continue;
-          const long long pc = g.c_nidx ? (long long)g.c_nidx[c] : (long long)c;
-          T* p = C + r + pc * g.ldc;
-          const T x = acc[v * VW + q][w * VW + s];
-          if (split_out)
-            *p = x;
-          else
-            *p = beta == T(0) ? alpha * x : fma(alpha, x, beta * *p);
+            for (int q = 0; q < VW; q++) o[q] = (split_out ? T(1) : alpha) * acc[v * VW + q][w * VW + s];
+          } else {
+            const V old = *reinterpret_cast<const V*>(p);
+            const T* po = reinterpret_cast<const T*>(&old);
+#pragma unroll
+            for (int q = 0; q < VW; q++) o[q] = fma(alpha, acc[v * VW + q][w * VW + s], beta * po[q]);
+          }
+          *reinterpret_cast<V*>(p) = out;
+        } else {
+#pragma unroll
+          for (int q = 0; q < VW; q++) {
+            const int r = r0 + q;
+            if (r >= m || (LOWER && r < c)) continue;
+            const T x = acc[v * VW + q][w * VW + s];
+            if (split_out)
+              p[q] = x;
+            else
+              p[q] = beta == T(0) ? alpha * x : fma(alpha, x, beta * p[q]);
+          }
         }
-    }
+      }
+  }
 }
 
 }  // namespace gla

@@ -22,6 +22,24 @@ cudaError_t gemm_launch(bool f64, bool ta, bool tb, bool lower, const GemmDesc& 
 // nprob descriptors, grid sized for max_m x max_n outputs (A, B not transposed).
 cudaError_t gemm_launch_grouped(bool f64, const GemmDesc* d_descs, int nprob, int max_m, int max_n, cudaStream_t st);
 
+// ---- double-float GEMM (dfgemm.cu): C = op(A) B with A = Ahi + Alo and
+// B = Bhi + Blo (Alo / Blo may be null), column-major; lower: write only the
+// lower triangle of C.
+struct DfGemmDesc {
+  int m, n, k;
+  int lower;
+  const float* Ahi;
+  const float* Alo;
+  long long lda;
+  const float* Bhi;
+  const float* Blo;
+  long long ldb;
+  float* Chi;
+  float* Clo;
+  long long ldc;
+};
+cudaError_t dfgemm_launch(const DfGemmDesc& g, bool ta, cudaStream_t st);
+
 // ---- stage plans (one order, one working precision)
 struct SytrdPlan;
 cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64);
@@ -70,6 +88,22 @@ int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void
 // unconverged. Synchronises st before returning.
 int large_syev(LargeCtx* c, int tcode, bool wantv, bool lower, const void* Ain, long long lda, void* w, void* V,
                long long ldv, int* info_host, cudaStream_t st);
+
+// ---- refinement of FP32 eigenpairs of one large matrix (large_refine.cu)
+struct RefineLarge;
+int refine_large_create(RefineLarge** out, int n);
+void refine_large_destroy(RefineLarge* r);
+// Buffers the FP32 solve can write straight into: eigenvectors (n x n,
+// leading dimension n) and eigenvalues (n).
+float* refine_large_xbuf(RefineLarge* r);
+float* refine_large_wbuf(RefineLarge* r);
+// A: FP64 input (uplo triangle, leading dimension lda); X32/w32: FP32
+// eigenpairs (ascending); outputs w (FP64, ascending) and V (ldv, may be
+// null). Synchronises st. Returns 0, -1 for non-finite input, or a status.
+int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower, const float* X32, long long ldx,
+                     const float* w32, double* w, double* V, long long ldv, cudaStream_t st);
+int refine_large_iters(const RefineLarge* r);
+int refine_large_rotations(const RefineLarge* r);  // cluster Rayleigh-Ritz steps of the last run
 
 // ---- leaf solves of the divide and conquer: a batched small-matrix plan
 // over the leaf orders, fed with tridiagonal (d, e) in its arena layout.

@@ -183,15 +183,19 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, lon
   const int bk = f64 ? GemmCfg<double>::BK : GemmCfg<float>::BK;
   for (int b = p.nblk - 1; b >= 0; b--) {
     const int j0 = b * kBT, kb = std::min(kBT, n - 1 - j0);
-    const int mrows = n - j0 - 1;
-    // W = Y_b' Z[j0+1:, :]
+    // rows from r0 (j0 + 1 rounded down to a 16-byte boundary: Y is zero
+    // above its unit diagonal, so the extra rows add nothing) keep Z's
+    // column segments aligned for vector access
+    const int r0 = (j0 + 1) & ~(16 / (int)sizeof(T) - 1);
+    const int mrows = n - r0;
+    // W = Y_b' Z[r0:, :]
     GemmDesc g{};
     g.m = kb;
     g.n = n;
     g.k = mrows;
-    g.A = Y + (j0 + 1) + (long long)j0 * n;
+    g.A = Y + r0 + (long long)j0 * n;
     g.lda = n;
-    g.B = Z + (j0 + 1);
+    g.B = Z + r0;
     g.ldb = ldz;
     g.C = p.Wp;
     g.ldc = kb;
@@ -205,16 +209,16 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, lon
     k_tw<T><<<(n + 15) / 16, 256, 0, st>>>((const T*)p.Wp, splits, (long long)kb * n, (const T*)p.Tm + (long long)b * kBT * kBT,
                                            (T*)p.W2, kb, n);
     if ((err = cudaGetLastError()) != cudaSuccess) return -1000 - (int)err;
-    // Z[j0+1:, :] -= Y_b W2
+    // Z[r0:, :] -= Y_b W2
     GemmDesc h{};
     h.m = mrows;
     h.n = n;
     h.k = kb;
-    h.A = Y + (j0 + 1) + (long long)j0 * n;
+    h.A = Y + r0 + (long long)j0 * n;
     h.lda = n;
     h.B = p.W2;
     h.ldb = kb;
-    h.C = Z + (j0 + 1);
+    h.C = Z + r0;
     h.ldc = ldz;
     h.alpha = -1.0;
     h.beta = 1.0;

@@ -2,25 +2,28 @@
 // triangle), blocked in panels of kSytrdNB columns: the LAPACK dsytrd/dlatrd
 // organisation of the reference's symtriLower! (src/eigenSelfAdjoint.jl:450-504).
 //
-// Column j of a panel (c = j - k0 columns into it):
-//   x  = A[j+1:, j] after the panel's earlier rank-2 terms
+// Column j of a panel (c = j - k0 columns into it), s = j + 1:
+//   x  = A[s:, j] after the panel's earlier rank-2 terms
 //   reflector H_j = I - tau v v' from x (reflector! convention: beta = -sign(x1)|x|,
-//   v[j+1] = 1, v stored in A[j+2:, j] like the reference)
-//   y  = A_t v - V (W' v) - W (V' v)     A_t = A[j+1:, j+1:] without this panel
+//   v[s] = 1, v stored in A[s+1:, j] like the reference)
+//   y  = A_t v - V (W' v) - W (V' v)     A_t = A[s:, s:] without this panel
 //   w  = tau y - (tau^2 / 2)(y' v) v     (so A_t - v w' - w v' = H A_t H)
 // and after the panel one rank-2k update A_t -= V W' + W V' (a GEMM over
 // the lower tiles). Every panel is one cooperative launch over all SMs with
 // two grid barriers per column:
-//   phase 2 (all CTAs): reflector scalars from the norm partials, then the
-//     SYMV in warp units of 32 columns x 256 rows of the trailing lower
-//     triangle (each unit adds A_IJ v_J to its rows and A_IJ' v_I to its
-//     columns, into deterministic partial buffers), the dot products V'v,
-//     W'v and the quadratic form v'A_t v;
-//   phase 3 (rows split over CTAs): y from the partials, w, the reflector
-//     stored, and the next column updated with this column's terms plus its
-//     norm partial.
-// The barrier is a counter/generation pair in global memory whose waits are
-// bounded: a wait that runs out sets the error word and every CTA leaves.
+//   phase A (all CTAs): the SYMV of A_t with the raw column a (a_i = x_i
+//     below row s, so it needs no reflector scalars and starts at once), in
+//     warp units of 32 columns x 64 rows of the lower triangle (each unit
+//     adds A_IJ a_J to its rows and A_IJ' a_I to its columns, into
+//     deterministic partial buffers), the dot products V'a, W'a,
+//     a'A[:, s] and the quadratic form a'A_t a;
+//   phase B (rows split over CTAs): the reflector scalars from the norm
+//     partials, v = scale a + e_s applied to the phase A results by
+//     linearity, y, w, the reflector stored, and the next column updated
+//     with this column's terms plus its norm partial.
+// Each phase issues all of its global loads before its first reduction:
+// on GB300 an L2 round trip costs about a microsecond and is the unit of
+// cost at the small trailing orders.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,7 +35,8 @@
 namespace gla {
 
 constexpr int kTW = 32;        // SYMV unit width (columns)
-constexpr int kRC = 256;       // SYMV unit height (rows): 8 rows per lane
+constexpr int kRC = 64;        // SYMV unit height (rows): 2 rows per lane
+constexpr int kMaxTC = 16384 / kTW;  // tile columns at the largest order
 constexpr int kDotRows = 1024; // rows per dot-product unit
 constexpr int kPT = 256;       // threads per CTA
 constexpr long long kSpinLimit = 1ll << 26;
@@ -52,122 +56,123 @@ struct SytrdArgs {
   T* Qp;             // column partials [nCH][n]
   T* normp;          // [G]
   T* qfp;            // [G]
-  T* dots;           // [2][kSytrdNB][nDCH]
+  T* dots;           // [3][kSytrdNB][nDCH]
   int nDCH;
-  const int2* units; // (tile column, chunk), ordered by tile column
-  const int* ustart; // first unit of each tile column; ustart[nTC] = total
+  const int* ustart; // first SYMV unit of each tile column; ustart[nTC] = total
   int nTC;
-  unsigned* bar;     // [0] arrivals, [1] generation
+  unsigned* bar;     // arrival counter (monotonic over the launches of one tridiagonalisation)
+  unsigned bar_base; // counter value when this launch starts
   int* err;
 };
 
-// Returns the same verdict to every thread of the CTA (thread 0 decides and
-// broadcasts it), so a CTA never splits at an early return.
-GLA_DEV bool grid_sync(unsigned* bar, int* err) {
+// Grid barrier on a monotonic arrival counter: barrier number k of a launch
+// completes when the counter reaches (k + 1) * gridDim.x. Thread 0 of each
+// CTA arrives with a release add and polls with acquire loads; the wait is
+// bounded (kSpinLimit polls) and a timeout sets the error word, which every
+// waiting CTA also watches. The verdict is broadcast through shared memory
+// so that all threads of a CTA return the same value.
+GLA_DEV bool grid_sync(unsigned* bar, int* err, unsigned& target) {
   __shared__ int s_ok;
+  target += gridDim.x;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* vgen = bar + 1;
-    volatile int* verr = err;
-    const unsigned gen = *vgen;
     __threadfence();
-    const unsigned arrived = atomicAdd(bar, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      long long it = 0;
-      while (*vgen == gen) {
-        if (*verr) break;
-        if (++it > kSpinLimit) {
-          atomicExch(err, 1);
-          break;
-        }
-        __nanosleep(32);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+    volatile int* verr = err;
+    long long it = 0;
+    for (;;) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if ((int)(v - target) >= 0) break;
+      if (*verr) break;
+      if (++it > kSpinLimit) {
+        atomicExch(err, 1);
+        break;
       }
     }
-    __threadfence();
     s_ok = *verr == 0;
   }
   __syncthreads();
   return s_ok != 0;
 }
 
-// Deterministic block sum (every CTA gets the same bits for the same inputs).
-template <class T>
-GLA_DEV T block_sum_all(T v, T* sred) {
+// Deterministic block sum of up to 4 values (every CTA gets the same bits
+// for the same inputs). `buf` alternates between two shared slots so that
+// consecutive calls need a single __syncthreads each.
+template <class T, int K>
+GLA_DEV void block_sum(T (&v)[K], T (*sred)[kPT / 32][4], int& buf) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = v;
-  __syncthreads();
-  T s = 0;
+  for (int k = 0; k < K; k++)
 #pragma unroll
-  for (int i = 0; i < kPT / 32; i++) s += sred[i];
-  return s;
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) sred[buf][threadIdx.x >> 5][k] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    T s = T(0);
+#pragma unroll
+    for (int i = 0; i < kPT / 32; i++) s += sred[buf][i][k];
+    v[k] = s;
+  }
+  buf ^= 1;
 }
 
+// a_i = A[i, j] below row s (the raw reflector column), 0 elsewhere. The
+// SYMV runs on a (no reflector scalars needed yet); phase B restores
+// v = scale a + e_s by linearity.
 template <class T>
-struct StepScalars {
-  int j, s;
-  T scale;  // v_i = A[i, j] * scale for i > s, v_s = 1
-};
-
-template <class T>
-GLA_DEV T v_at(const T* __restrict__ A, long long ld, const StepScalars<T>& st, int i) {
-  if (i == st.s) return T(1);
-  if (i < st.s) return T(0);
-  return A[i + (long long)st.j * ld] * st.scale;
+GLA_DEV T a_at(const T* __restrict__ A, long long ld, int j, int s, int i) {
+  return i > s ? A[i + (long long)j * ld] : T(0);
 }
 
-// One warp: SYMV unit (tile column J, chunk ch). Adds rowacc to P[J][r] and
-// the column sums to Qp[ch][c]; returns the unit's part of v'A_t v.
+// One warp: SYMV unit (tile column J, chunk ch) of the trailing lower
+// triangle on the raw column a, row by row (lane l holds row r0 + l + 32 q);
+// all loads of the unit are issued before its FMAs. Adds the row sums to
+// P[J][r] and the column sums to Qp[ch][c]; returns the unit's part of a'A_t a.
 template <class T>
-__device__ T symv_unit(const SytrdArgs<T>& a, const StepScalars<T>& st, int J, int ch, T* svcol) {
+__device__ T symv_unit(const SytrdArgs<T>& a, int j, int s, int J, int ch, T* svcol) {
+  constexpr int NQ = kRC / 32;
   const int lane = threadIdx.x & 31, n = a.n;
   const long long ld = a.ld;
   const T* __restrict__ A = a.A;
   const int c0 = J * kTW, r0 = c0 + ch * kRC;
   const int cc = c0 + lane;
-  const T vc = cc < n ? v_at(A, ld, st, cc) : T(0);
+  const T vc = cc < n ? a_at(A, ld, j, s, cc) : T(0);
+  const T* __restrict__ base = A + (long long)c0 * ld + r0 + lane;
+  const int ncol = min(kTW, n - c0);
+  T x[NQ][kTW], vr[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; q++) {
+    const int r = r0 + lane + 32 * q;
+    const bool rin = r < n;
+    const T* rowp = base + 32 * q;
+#pragma unroll
+    for (int ci = 0; ci < kTW; ci++) x[q][ci] = (rin && ci < ncol) ? rowp[(long long)ci * ld] : T(0);
+    vr[q] = rin ? a_at(A, ld, j, s, r) : T(0);
+  }
   svcol[lane] = vc;
   __syncwarp();
-  T vr[8], rowacc[8];
-#pragma unroll
-  for (int q = 0; q < 8; q++) {
-    const int r = r0 + lane + 32 * q;
-    vr[q] = r < n ? v_at(A, ld, st, r) : T(0);
-    rowacc[q] = T(0);
-  }
-  const bool diag = ch == 0;
   T colacc[kTW];
 #pragma unroll
-  for (int ci = 0; ci < kTW; ci++) {
-    const T vcv = svcol[ci];
-    const bool cin = c0 + ci < n;
-    const T* __restrict__ col = A + (long long)(c0 + ci) * ld;
-    T ca = T(0);
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int r = r0 + lane + 32 * q;
-      T x = (cin && r < n) ? col[r] : T(0);
-      T xr = x, xc = x;
-      if (q == 0 && diag) {  // diagonal tile: lower part only (row >= column)
-        xr = lane >= ci ? x : T(0);
-        xc = lane > ci ? x : T(0);
-      }
-      rowacc[q] = fma(xr, vcv, rowacc[q]);
-      ca = fma(xc, vr[q], ca);
-    }
-    colacc[ci] = ca;
-  }
+  for (int ci = 0; ci < kTW; ci++) colacc[ci] = T(0);
   T qf = T(0);
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
+  for (int q = 0; q < NQ; q++) {
+    if (r0 + 32 * q >= n) break;  // warp-uniform
+    const bool diag = ch == 0 && q == 0;  // diagonal tile: lower part only (row >= column)
+    T rowacc = T(0);
+#pragma unroll
+    for (int ci = 0; ci < kTW; ci++) {
+      const T xr = (diag && lane < ci) ? T(0) : x[q][ci];
+      const T xc = (diag && lane <= ci) ? T(0) : x[q][ci];
+      rowacc = fma(xr, svcol[ci], rowacc);
+      colacc[ci] = fma(xc, vr[q], colacc[ci]);
+    }
     const int r = r0 + lane + 32 * q;
-    if (r < n) a.P[(long long)J * n + r] = rowacc[q];
-    qf = fma(rowacc[q], vr[q], qf);
+    if (r < n) a.P[(long long)J * n + r] = rowacc;
+    qf = fma(rowacc, vr[q], qf);
   }
   // reduce-scatter the 32 column sums across the warp: lane l keeps column l
 #pragma unroll
@@ -194,175 +199,211 @@ GLA_DEV void own_rows(int s, int n, int& lo, int& hi) {
   hi = min(n, lo + R);
 }
 
+// Dot-product unit kinds, in work-list order after the SYMV units.
+constexpr int kDotA = 0;  // sum_r a_r A[r, s]        (cross term of v'A_t v)
+constexpr int kDotV = 1;  // sum_r a_r V[r, q], q < c
+constexpr int kDotW = 2;  // sum_r a_r W[r, q]
+
 template <class T>
 __global__ void __launch_bounds__(kPT, 1) k_sytrd_panel(const SytrdArgs<T> a) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int n = a.n, G = gridDim.x, g = blockIdx.x;
   const long long ld = a.ld, ldv = a.ldv;
   T* __restrict__ A = a.A;
-  __shared__ T sred[kPT / 32];
+  __shared__ T sred[2][kPT / 32][4];
   __shared__ T svcol[kPT / 32][32];
-  __shared__ T sdotV[kSytrdNB], sdotW[kSytrdNB], sVs[kSytrdNB + 1], sWs[kSytrdNB + 1];
-  __shared__ T sys[2];
+  __shared__ T sdotV[kSytrdNB], sdotW[kSytrdNB], sVs[kSytrdNB], sWs[kSytrdNB];
+  __shared__ int sust[kMaxTC + 1];
+  __shared__ T sscal[4];
+  int rb = 0;
+  unsigned bar_target = a.bar_base;
+  for (int i = tid; i <= a.nTC; i += kPT) sust[i] = a.ustart[i];
 
   // panel start: norm partial of column k0 below the subdiagonal
   {
     const int j = a.k0, s = j + 1;
     int lo, hi;
     own_rows(s, n, lo, hi);
-    T part = T(0);
+    T part[1] = {T(0)};
     for (int i = lo + tid; i < hi; i += kPT)
       if (i > s) {
         const T x = A[i + (long long)j * ld];
-        part = fma(x, x, part);
+        part[0] = fma(x, x, part[0]);
       }
-    part = block_sum_all(part, sred);
-    if (tid == 0) a.normp[g] = part;
+    block_sum(part, sred, rb);
+    if (tid == 0) a.normp[g] = part[0];
   }
-  if (!grid_sync(a.bar, a.err)) return;
+  if (!grid_sync(a.bar, a.err, bar_target)) return;
 
   for (int c = 0; c < a.nbp; c++) {
     const int j = a.k0 + c, s = j + 1, m = n - s;
-    // ---------------- phase 2: reflector scalars (redundant per CTA), SYMV, dots
-    T sigma = T(0);
-    for (int i = tid; i < G; i += kPT) sigma += a.normp[i];
-    sigma = block_sum_all(sigma, sred);
-    const T alpha = A[s + (long long)j * ld];
-    T beta, tau, scale;
-    if (sigma == T(0)) {
-      beta = alpha;
-      tau = T(0);
-      scale = T(0);
-    } else {
-      const T nrm2 = fma(alpha, alpha, sigma);
-      const T nrm = nrm2 * prec<T>::rsqrt(nrm2);
-      beta = -copysign(nrm, alpha);
-      const T rb = prec<T>::rcp(beta);
-      tau = (beta - alpha) * rb;
-      scale = prec<T>::rcp(alpha - beta);
-    }
-    if (g == 0 && tid == 0) {
-      a.d[j] = A[j + (long long)j * ld];
-      a.e[j] = beta;
-      a.tau[j] = tau;
-    }
-    StepScalars<T> st;
-    st.j = j;
-    st.s = s;
-    st.scale = scale;
     const int J0 = s / kTW;
-    const int usym0 = a.ustart[J0], nsym = a.ustart[a.nTC] - usym0;
-    const int ndch = (m + kDotRows - 1) / kDotRows;
-    const int ndot = 2 * c * ndch;
-    T qf = T(0);
-    for (int u = g * (kPT / 32) + wid; u < nsym + ndot; u += G * (kPT / 32)) {
-      if (u < nsym) {
-        const int2 jc = a.units[usym0 + u];
-        qf += symv_unit(a, st, jc.x, jc.y, svcol[wid]);
-      } else {
-        const int du = u - nsym;
-        const int which = du / (c * ndch), rem = du % (c * ndch);
-        const int q = rem / ndch, chn = rem % ndch;
-        const T* __restrict__ X = (which == 0 ? a.V : a.W) + (long long)q * ldv;
-        const int r0 = s + chn * kDotRows, r1 = min(n, r0 + kDotRows);
-        T acc = T(0);
-        for (int r = r0 + lane; r < r1; r += 32) acc = fma(X[r], v_at(A, ld, st, r), acc);
+    // ---------------- phase A: SYMV and dot products on the raw column a
+    {
+      const int usym0 = sust[J0], nsym = sust[a.nTC] - usym0;
+      const int ndch = (m + kDotRows - 1) / kDotRows;
+      const int ndot = (2 * c + 1) * ndch;
+      T qf[1] = {T(0)};
+      // unit u goes to CTA u % G, so every CTA gets an even share
+      for (int k = wid;; k += kPT / 32) {
+        const int u = g + G * k;
+        if (u >= nsym + ndot) break;
+        if (u < nsym) {
+          const int ug = usym0 + u;
+          int lo = J0, hi = a.nTC - 1;  // tile column: last J with sust[J] <= ug
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sust[mid] <= ug) lo = mid; else hi = mid - 1;
+          }
+          qf[0] += symv_unit(a, j, s, lo, ug - sust[lo], svcol[wid]);
+        } else {
+          const int du = u - nsym;
+          const int kind = du < ndch ? kDotA : (du - ndch) / (c * ndch) + 1;
+          const int rem = du < ndch ? du : (du - ndch) % (c * ndch);
+          const int q = rem / ndch, chn = rem % ndch;
+          const T* __restrict__ X = kind == kDotA ? A + (long long)s * ld
+                                                  : (kind == kDotV ? a.V : a.W) + (long long)q * ldv;
+          const int r0 = s + 1 + chn * kDotRows, r1 = min(n, r0 + kDotRows);
+          T acc = T(0);
+          for (int r = r0 + lane; r < r1; r += 32) acc = fma(X[r], A[r + (long long)j * ld], acc);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) a.dots[((long long)which * kSytrdNB + q) * a.nDCH + chn] = acc;
+          for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          if (lane == 0) a.dots[((long long)kind * kSytrdNB + q) * a.nDCH + chn] = acc;
+        }
       }
+      block_sum(qf, sred, rb);
+      if (tid == 0) a.qfp[g] = qf[0];
     }
-    qf = block_sum_all(qf, sred);
-    if (tid == 0) a.qfp[g] = qf;
-    if (!grid_sync(a.bar, a.err)) return;
+    if (!grid_sync(a.bar, a.err, bar_target)) return;
 
-    // ---------------- phase 3: y, w, reflector store, next column
-    for (int q = tid; q < c; q += kPT) {
-      T sv = T(0), sw = T(0);
-      for (int k = 0; k < ndch; k++) {
-        sv += a.dots[((long long)0 * kSytrdNB + q) * a.nDCH + k];
-        sw += a.dots[((long long)1 * kSytrdNB + q) * a.nDCH + k];
-      }
-      sdotV[q] = sv;
-      sdotW[q] = sw;
-      sVs[q] = a.V[s + (long long)q * ldv];
-      sWs[q] = a.W[s + (long long)q * ldv];
-    }
-    T qsum = T(0);
-    for (int i = tid; i < G; i += kPT) qsum += a.qfp[i];
-    qsum = block_sum_all(qsum, sred);  // (its barriers also publish sdotV/sdotW)
-    T pq = T(0);
-    for (int q = tid; q < c; q += kPT) pq = fma(sdotV[q], sdotW[q], pq);
-    pq = block_sum_all(pq, sred);
-    const T ytv = qsum - T(2) * pq;
-    const T hw = T(0.5) * tau * tau * ytv;  // w = tau y - hw v
-    // y_s and w_s (every CTA; warp 0)
-    if (wid == 0) {
-      T ys = T(0);
-      const int Js = s / kTW;
-      const int nch = (n - Js * kTW + kRC - 1) / kRC;
-      if (lane == 0) ys += a.P[(long long)Js * n + s];
-      for (int k = lane; k < nch; k += 32) ys += a.Qp[(long long)k * n + s];
-      for (int q = lane; q < c; q += 32) ys -= sVs[q] * sdotW[q] + sWs[q] * sdotV[q];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) ys += __shfl_xor_sync(0xffffffffu, ys, o);
-      if (lane == 0) sys[0] = tau * ys - hw;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      sVs[c] = T(1);
-      sWs[c] = sys[0];
-    }
-    __syncthreads();
-    const bool last_in_panel = c + 1 == a.nbp;
-    const bool update_next = !last_in_panel || s == n - 1;
+    // ---------------- phase B: reflector scalars, y, w, reflector store, next column
+    const int ndch = (m + kDotRows - 1) / kDotRows;
+    const int Js = s / kTW;
+    const int nchs = (n - Js * kTW + kRC - 1) / kRC;
     int lo, hi;
     own_rows(s, n, lo, hi);
     const int R = hi - lo;
     int tpr = 1;
     while (tpr < 32 && tpr * 2 * R <= kPT) tpr *= 2;
-    const int sub = tid % tpr, rpp = kPT / tpr;
-    T npart = T(0);
-    for (int base = lo; base < hi; base += rpp) {
-      const int i = base + tid / tpr;
-      const bool act = i < hi;
-      const int ii = act ? i : lo;
-      // y_i from the partial buffers, minus the panel terms
-      T y = T(0);
-      const int Ji = ii / kTW;
-      for (int Jx = J0 + sub; Jx <= Ji; Jx += tpr) y += a.P[(long long)Jx * n + ii];
-      const int nch = (n - Ji * kTW + kRC - 1) / kRC;
-      for (int k = sub; k < nch; k += tpr) y += a.Qp[(long long)k * n + ii];
-      for (int q = sub; q < c; q += tpr)
-        y -= a.V[ii + (long long)q * ldv] * sdotW[q] + a.W[ii + (long long)q * ldv] * sdotV[q];
-      for (int o = tpr / 2; o > 0; o >>= 1) y += __shfl_xor_sync(0xffffffffu, y, o, tpr);
-      const T vi = v_at(A, ld, st, ii);
-      const T wi = tau * y - hw * vi;
-      T xn = T(0);
-      if (update_next) {
-        for (int q = sub; q < c; q += tpr)
-          xn += a.V[ii + (long long)q * ldv] * sWs[q] + a.W[ii + (long long)q * ldv] * sVs[q];
-        for (int o = tpr / 2; o > 0; o >>= 1) xn += __shfl_xor_sync(0xffffffffu, xn, o, tpr);
-        xn += vi * sWs[c] + wi * sVs[c];
+    const int sub = tid % tpr;
+    const int i = lo + tid / tpr;
+    const bool act = i < hi;
+    const int ii = act ? i : s;  // idle threads read row s (always in range)
+    // (1) every load of the phase, independent of the reductions
+    T red[4] = {T(0), T(0), T(0), T(0)};  // sigma, a'A_t a, sum a_r A[r,s], y_s raw
+    for (int t = tid; t < G; t += kPT) {
+      red[0] += a.normp[t];
+      red[1] += a.qfp[t];
+    }
+    for (int k = tid; k < ndch; k += kPT) red[2] += a.dots[((long long)kDotA * kSytrdNB) * a.nDCH + k];
+    if (tid < c) {
+      T sv = T(0), sw = T(0);
+      for (int k = 0; k < ndch; k++) {
+        sv += a.dots[((long long)kDotV * kSytrdNB + tid) * a.nDCH + k];
+        sw += a.dots[((long long)kDotW * kSytrdNB + tid) * a.nDCH + k];
       }
-      // all reads of column j (v_at) are done by every thread of the group before the store
-      __syncwarp();
-      if (act && sub == 0) {
-        a.V[ii + (long long)c * ldv] = vi;
-        a.W[ii + (long long)c * ldv] = wi;
-        if (ii > s) A[ii + (long long)j * ld] = vi;
-        if (update_next) {
-          const T x = A[ii + (long long)s * ld] - xn;
-          A[ii + (long long)s * ld] = x;
-          if (ii > s + 1) npart = fma(x, x, npart);
-          if (s == n - 1) a.d[n - 1] = x;
+      sdotV[tid] = sv;
+      sdotW[tid] = sw;
+      sVs[tid] = a.V[s + (long long)tid * ldv];
+      sWs[tid] = a.W[s + (long long)tid * ldv];
+    }
+    for (int k = tid - 64; k >= 0 && k < nchs; k += kPT - 64) red[3] += a.Qp[(long long)k * n + s];
+    if (tid == 63) red[3] += a.P[(long long)Js * n + s];
+    const T alpha = A[s + (long long)j * ld];
+    const T Ass = A[s + (long long)s * ld];
+    T yraw = T(0);
+    {
+      const int Ji = ii / kTW;
+      for (int Jx = J0 + sub; Jx <= Ji; Jx += tpr) yraw += a.P[(long long)Jx * n + ii];
+      const int nch = (n - Ji * kTW + kRC - 1) / kRC;
+      for (int k = sub; k < nch; k += tpr) yraw += a.Qp[(long long)k * n + ii];
+    }
+    const T ai = a_at(A, ld, j, s, ii);
+    const T Ais = A[ii + (long long)s * ld];
+    block_sum(red, sred, rb);  // also publishes sdotV/sdotW/sVs/sWs
+    // (2) reflector scalars and the q-sums once, in warp 0 (lanes over q;
+    // FP64 work repeated by every warp would queue on the FP64 pipe)
+    if (wid == 0) {
+      const T sigma = red[0];
+      T beta, tau, scale;
+      if (sigma == T(0)) {
+        beta = alpha;
+        tau = T(0);
+        scale = T(0);
+      } else {
+        const T nrm2 = fma(alpha, alpha, sigma);
+        const T nrm = nrm2 * prec<T>::rsqrt(nrm2);
+        beta = -copysign(nrm, alpha);
+        tau = (beta - alpha) * prec<T>::rcp(beta);
+        scale = prec<T>::rcp(alpha - beta);
+      }
+      // p = V'v, q = W'v with v = scale a + e_s; y_s and v'A_t v by linearity
+      T pq = T(0), corr = T(0);
+      if (lane < c) {
+        const T pv = fma(scale, sdotV[lane], sVs[lane]), qv = fma(scale, sdotW[lane], sWs[lane]);
+        pq = pv * qv;
+        corr = sVs[lane] * qv + sWs[lane] * pv;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        pq += __shfl_xor_sync(0xffffffffu, pq, o);
+        corr += __shfl_xor_sync(0xffffffffu, corr, o);
+      }
+      if (lane == 0) {
+        const T vAv = scale * scale * red[1] + T(2) * scale * red[2] + Ass;
+        const T hw = T(0.5) * tau * tau * (vAv - T(2) * pq);  // w = tau y - hw v
+        const T y_s = scale * red[3] + Ass - corr;
+        sscal[0] = tau;
+        sscal[1] = scale;
+        sscal[2] = hw;
+        sscal[3] = tau * y_s - hw;  // w_s
+        if (g == 0) {
+          if (c == 0) a.d[j] = A[j + (long long)j * ld];  // later columns: written by the previous step
+          a.e[j] = beta;
+          a.tau[j] = tau;
         }
       }
     }
-    npart = block_sum_all(npart, sred);
-    if (tid == 0) a.normp[g] = npart;
+    __syncthreads();
+    const T tau = sscal[0], scale = sscal[1], hw = sscal[2], w_s = sscal[3];
+    const bool last_in_panel = c + 1 == a.nbp;
+    const bool update_next = !last_in_panel || s == n - 1;
+    // (3) own rows
+    T y = T(0), xn = T(0);
+    for (int q = sub; q < c; q += tpr) {
+      const T vq = a.V[ii + (long long)q * ldv], wq = a.W[ii + (long long)q * ldv];
+      const T pv = fma(scale, sdotV[q], sVs[q]), qv = fma(scale, sdotW[q], sWs[q]);
+      y -= vq * qv + wq * pv;
+      xn += vq * sWs[q] + wq * sVs[q];
+    }
+    if (sub == 0) y += scale * yraw + Ais;
+    else y += scale * yraw;
+    for (int o = tpr / 2; o > 0; o >>= 1) {
+      y += __shfl_xor_sync(0xffffffffu, y, o, tpr);
+      xn += __shfl_xor_sync(0xffffffffu, xn, o, tpr);
+    }
+    const T vi = ii == s ? T(1) : scale * ai;
+    const T wi = tau * y - hw * vi;
+    xn += vi * w_s + wi;  // the q = c term: v_s = 1, w_s
+    T npart[1] = {T(0)};
+    if (act && sub == 0) {
+      a.V[ii + (long long)c * ldv] = vi;
+      a.W[ii + (long long)c * ldv] = wi;
+      if (ii > s) A[ii + (long long)j * ld] = vi;
+      if (update_next) {
+        // A[s, s] is read by every CTA in this phase: its new value goes to d[s]
+        const T x = Ais - xn;
+        if (ii == s)
+          a.d[s] = x;
+        else
+          A[ii + (long long)s * ld] = x;
+        if (ii > s + 1) npart[0] = x * x;
+      }
+    }
+    block_sum(npart, sred, rb);
+    if (tid == 0) a.normp[g] = npart[0];
     if (c + 1 < a.nbp)
-      if (!grid_sync(a.bar, a.err)) return;
+      if (!grid_sync(a.bar, a.err, bar_target)) return;
   }
 }
 
@@ -371,7 +412,6 @@ __global__ void __launch_bounds__(kPT, 1) k_sytrd_panel(const SytrdArgs<T> a) {
 struct SytrdPlan {
   int n = 0, G = 0;
   int nTC = 0, nCH = 0, nDCH = 0;
-  int2* units = nullptr;
   int* ustart = nullptr;
   void* P = nullptr;
   void* Qp = nullptr;
@@ -410,12 +450,12 @@ cudaError_t sytrd_run(SytrdPlan& sp, T* A, long long lda, T* d, T* e, T* tau, cu
   a.qfp = (T*)sp.qfp;
   a.dots = (T*)sp.dots;
   a.nDCH = sp.nDCH;
-  a.units = sp.units;
   a.ustart = sp.ustart;
   a.nTC = sp.nTC;
   a.bar = sp.bar;
   a.err = sp.err;
   T* VW = (T*)sp.VW;
+  unsigned bar_base = 0;
   const int nsteps = n - 1;  // reflectors 0 .. n-2
   for (int k0 = 0; k0 < nsteps; k0 += kSytrdNB) {
     const int nbp = std::min(kSytrdNB, nsteps - k0);
@@ -423,6 +463,8 @@ cudaError_t sytrd_run(SytrdPlan& sp, T* A, long long lda, T* d, T* e, T* tau, cu
     a.nbp = nbp;
     a.V = VW;
     a.W = VW + (long long)nbp * n;
+    a.bar_base = bar_base;
+    bar_base += 2u * (unsigned)nbp * (unsigned)sp.G;  // barriers per launch: 1 + nbp + (nbp - 1)
     void* args[] = {(void*)&a};
     err = cudaLaunchCooperativeKernel((const void*)k_sytrd_panel<T>, dim3(sp.G), dim3(kPT), args, 0, st);
     if (err != cudaSuccess) return err;
@@ -472,14 +514,13 @@ cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64) {
   sp->nTC = (n + kTW - 1) / kTW;
   sp->nCH = (n + kRC - 1) / kRC;
   sp->nDCH = (n + kDotRows - 1) / kDotRows;
-  std::vector<int2> units;
   std::vector<int> ustart(sp->nTC + 1);
+  int total = 0;
   for (int J = 0; J < sp->nTC; J++) {
-    ustart[J] = (int)units.size();
-    const int nch = (n - J * kTW + kRC - 1) / kRC;
-    for (int ch = 0; ch < nch; ch++) units.push_back(make_int2(J, ch));
+    ustart[J] = total;
+    total += (n - J * kTW + kRC - 1) / kRC;  // chunks of tile column J
   }
-  ustart[sp->nTC] = (int)units.size();
+  ustart[sp->nTC] = total;
   std::vector<int> bk(4 * kSytrdNB);
   const int last = (n - 1) % kSytrdNB == 0 ? kSytrdNB : (n - 1) % kSytrdNB;
   for (int kk = 0; kk < 2 * kSytrdNB; kk++) bk[kk] = kk < kSytrdNB ? kSytrdNB + kk : kk - kSytrdNB;
@@ -488,19 +529,16 @@ cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64) {
   auto alloc = [&](void** p, size_t bytes) {
     if (err == cudaSuccess) err = cudaMalloc(p, std::max<size_t>(bytes, 16));
   };
-  alloc((void**)&sp->units, sizeof(int2) * units.size());
   alloc((void**)&sp->ustart, sizeof(int) * ustart.size());
   alloc(&sp->P, el * (size_t)sp->nTC * n);
   alloc(&sp->Qp, el * (size_t)sp->nCH * n);
   alloc(&sp->normp, el * sp->G);
   alloc(&sp->qfp, el * sp->G);
-  alloc(&sp->dots, el * 2 * kSytrdNB * sp->nDCH);
+  alloc(&sp->dots, el * 3 * kSytrdNB * sp->nDCH);
   alloc(&sp->VW, el * (size_t)n * 2 * kSytrdNB);
   alloc((void**)&sp->bkidx, sizeof(int) * bk.size());
   alloc((void**)&sp->bar, 2 * sizeof(unsigned));
   alloc((void**)&sp->err, sizeof(int));
-  if (err == cudaSuccess)
-    err = cudaMemcpy(sp->units, units.data(), sizeof(int2) * units.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess)
     err = cudaMemcpy(sp->ustart, ustart.data(), sizeof(int) * ustart.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMemcpy(sp->bkidx, bk.data(), sizeof(int) * bk.size(), cudaMemcpyHostToDevice);
@@ -515,7 +553,6 @@ cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64) {
 
 void sytrd_plan_destroy(SytrdPlan* sp) {
   if (!sp) return;
-  cudaFree(sp->units);
   cudaFree(sp->ustart);
   cudaFree(sp->P);
   cudaFree(sp->Qp);

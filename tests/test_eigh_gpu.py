@@ -225,7 +225,7 @@ def test_dimension_mismatch(G):
     with pytest.raises(G.DimensionMismatch):
         G.SymTridiagonal(np.zeros(4), np.zeros(4))
     with pytest.raises(G.DimensionMismatch):
-        G.eigen(np.zeros((129, 129)))
+        G.Plan([G.GLA_MAX_N + 1])
 
 
 def test_empty_batch_and_zero_order(G):

@@ -141,7 +141,7 @@ def test_eigvals_only_large(G):
     assert np.max(np.abs(ws[0] - np.linalg.eigvalsh(A))) <= 1e-13 * np.linalg.norm(A, 2)
 
 
-@pytest.mark.parametrize("n", [129, 333, 800])
+@pytest.mark.parametrize("n", [129, 333, 800, 1500])
 def test_f32_goe(G, n):
     A = goe(n, 3000 + n)
     ws, Vs, info = solve(G, [A.astype(np.float32)], precision="f32")
@@ -162,10 +162,15 @@ def test_large_nonfinite_input(G):
     assert np.isnan(ws[0]).all()
 
 
-def test_large_deterministic(G):
-    A = goe(260, 10)
-    r1 = solve(G, [A])
-    r2 = solve(G, [A])
+@pytest.mark.parametrize("precision,n", [("f64", 260), ("f32", 1100)])
+def test_large_deterministic(G, precision, n):
+    # bitwise repeatable: every reduction has a fixed order (no atomics), and a
+    # cross-CTA race would show up as run-to-run differences
+    A = goe(n, 10)
+    if precision == "f32":
+        A = A.astype(np.float32)
+    r1 = solve(G, [A], precision=precision)
+    r2 = solve(G, [A], precision=precision)
     assert np.array_equal(r1[0][0], r2[0][0]) and np.array_equal(r1[1][0], r2[1][0])
 
 
@@ -176,3 +181,55 @@ def test_large_adjoint_unsupported(G):
     zw = torch.zeros(plan.w_elems, dtype=torch.float64, device="cuda")
     with pytest.raises(G.GLAError):
         plan.adjoint(zw, z, zw, z, z)
+
+
+# ---------------------------------------------------------------- FP32 solve + refinement
+
+def solve_refined(G, mats):
+    return solve(G, mats, precision="f32_refined")
+
+
+@pytest.mark.parametrize("n", [200, 600])
+def test_refined_goe_reaches_1e13(G, n):
+    A = goe(n, 4000 + n)
+    ws, Vs, info = solve_refined(G, [A])
+    assert info[0] == 0
+    nA = np.linalg.norm(A, 2)
+    assert np.max(np.abs(ws[0] - np.linalg.eigvalsh(A))) <= 1e-13 * nA
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+def test_refined_prescribed_cond1e6_clusters(G):
+    # lam = +-logspace(-6, 0): the FP32 solve cannot separate the small
+    # eigenvalues, so the refinement runs nested cluster Rayleigh-Ritz steps
+    n = 700
+    rng = np.random.default_rng(3)
+    lam = np.logspace(-6, 0, n) * rng.choice([-1.0, 1.0], n)
+    A = prescribed(lam, 7)
+    ws, Vs, info = solve_refined(G, [A])
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.sort(lam))) <= 1e-13
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+def test_refined_multiplicities(G):
+    n = 260
+    rng = np.random.default_rng(11)
+    lam = np.concatenate([np.full(60, 0.5), np.full(40, -1.0), rng.uniform(-2, 2, n - 100)])
+    A = prescribed(lam, 13)
+    ws, Vs, info = solve_refined(G, [A])
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.sort(lam))) <= 2e-13
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+def test_refined_mixed_batch(G):
+    mats = [goe(40, 1), goe(260, 2), goe(128, 3)]
+    ws, Vs, info = solve_refined(G, mats)
+    assert (info == 0).all()
+    for A, w, V in zip(mats, ws, Vs):
+        assert np.max(np.abs(w - np.linalg.eigvalsh(A))) <= 1e-13 * np.linalg.norm(A, 2)
+        assert residual(A, V, w) <= 1e-13
