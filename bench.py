@@ -11,6 +11,11 @@ Paths timed: plain FP64 (the reference's arithmetic), plain FP32, and FP32 +
 FP64 Ogita-Aishima refinement (the headline `value`, eigh/s, when it meets
 residual and eigenvalue error <= 1e-13 ||A|| on the checked sample).
 
+The single-matrix half of the metric ("large"): n = 4096, FP64 GPU path vs
+FP32 solve + refinement, on the prescribed-spectrum matrix Q diag(lam) Q'
+(lam = +-logspace(-6, 0), cond 1e6, Haar Q, seed 3) and on a GOE matrix,
+time per solve and accuracy of each result (best of 2 after a warm-up).
+
 --impl reference times the reference algorithm on the host cores instead:
 the CPU restatement of GenericLinearAlgebra.jl's eigen!(Hermitian)
 (oracle/, one matrix per OpenMP thread) — Julia itself is not installed.
@@ -29,7 +34,7 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "genericlinearalgebra.jl_gb300")
-for _p in (ROOT, PKG):
+for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
@@ -283,6 +288,7 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         el_e2e = float(t.item())
     peak = measured_dgemm_tflops(torch) if rank == 0 else None
+    large = run_large(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
 
     if rank == 0:
         def meets(r):
@@ -332,10 +338,76 @@ def run_ours(args):
             "paths": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} for k, v in results.items()},
             "graph": graph_res,
             "speedup_f32refined_vs_f64": graph_res["f32_refined"]["eigh_per_s"] / graph_res["f64"]["eigh_per_s"],
+            "large": large,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def large_case(kind, n):
+    """Single large matrix: 'c3' = Q diag(lam) Q', Q Haar (seed 3), lam = +-logspace(-6, 0, n)
+    with random signs (cond 1e6); 'goe' = (B + B')/2, seed 4."""
+    from helpers import goe, prescribed
+    if kind == "c3":
+        rng = np.random.default_rng(3)
+        lam = np.logspace(-6, 0, n) * rng.choice([-1.0, 1.0], n)
+        return prescribed(lam, 3), np.sort(lam)
+    return goe(n, 4), None
+
+
+def run_large(torch, glagpu, dev, n=4096, reps=2):
+    """n x n solves (the large half of the headline metric): plain FP64 GPU
+    path vs FP32 solve + FP64 refinement, time per solve (CUDA events; each
+    execute synchronises), accuracy of every result."""
+    out = {}
+    for kind in ("c3", "goe"):
+        A, lam = large_case(kind, n)
+        nA = np.linalg.norm(A, 2) if lam is None else np.abs(lam).max()
+        dA = torch.from_numpy(A.ravel(order="F").copy()).to(dev)
+        res = {}
+        wref = None
+        for path in ("f64", "f32_refined"):
+            plan = glagpu.Plan([n], precision=path, timing=True)
+            w = torch.empty(n, dtype=torch.float64, device=dev)
+            V = torch.empty(n * n, dtype=torch.float64, device=dev)
+            info = torch.zeros(1, dtype=torch.int32, device=dev)
+            plan.execute(dA, w, V, info)  # warm-up (first-touch of the plan)
+            torch.cuda.synchronize()
+            best = 1e30
+            phases = None
+            for _ in range(reps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                plan.execute(dA, w, V, info)
+                e1.record()
+                e1.synchronize()
+                t = e0.elapsed_time(e1)
+                if t < best:
+                    best, phases = t, plan.phase_times()
+            iters = plan.stats()["refine_n3"] / float(n) ** 3
+            wh = w.cpu().numpy()
+            Vh = V.cpu().numpy().reshape(n, n, order="F")
+            R = A @ Vh - Vh * wh
+            acc = {"residual": float(np.linalg.norm(R, 2) / nA),
+                   "orthogonality": float(np.linalg.norm(Vh.T @ Vh - np.eye(n), 2))}
+            if lam is not None:
+                acc["eig_err_vs_exact"] = float(np.abs(wh - lam).max() / nA)
+            elif wref is not None:
+                acc["eig_err_vs_f64_gpu"] = float(np.abs(wh - wref).max() / nA)
+            if path == "f64":
+                wref = wh
+            res[path] = {"ms": best, "phases_ms": phases, "info": int(info.item()), "accuracy": acc,
+                         "refine_iterations": iters}
+            plan.close()
+            del w, V
+        res["speedup_f32refined_vs_f64"] = res["f64"]["ms"] / res["f32_refined"]["ms"]
+        ok = res["f32_refined"]["info"] == 0 and all(
+            v <= 1e-13 for k, v in res["f32_refined"]["accuracy"].items() if k != "orthogonality")
+        res["refined_meets_1e13"] = bool(ok)
+        out[f"n{n}_{kind}"] = res
+    return out
 
 
 def plan_buckets(ns):
@@ -416,6 +488,7 @@ def main():
     ap.add_argument("--paths", default="f64,f32,f32_refined", help="paths to time (profiling)")
     ap.add_argument("--profile", action="store_true", help="profiling run: time the paths only, print nothing")
     ap.add_argument("--nrange", default="", help="profiling: keep matrices with lo <= n <= hi, as 'lo,hi'")
+    ap.add_argument("--no-large", action="store_true", help="skip the n = 4096 single-matrix section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -17,21 +17,22 @@
 // (T. Ogita, K. Aishima, JJIAM 35 (2018) Alg. 1, rewritten on the residual;
 // t_ij - t_ji = r_ij (lam_j - lam_i) carries the orthogonality correction of
 // separated pairs, so X'X is only formed inside clusters).
-// Clusters are runs of the sorted lam joined wherever some pair (i, j) with
+// Clusters are runs of the sorted lam joined wherever a gap is below ten
+// times the residual norms of its two columns, some pair (i, j) with
 // |i - j| <= kWin has |t_ij| > kTheta |lam_j - lam_i| (the first-order update
 // would not be small), or the gap is at rounding level. Each cluster J is
 // rotated to the Ritz vectors of its projected matrix, which to first order is
 //   C_J = diag(lam_J - mu) + (T_JJ + T_JJ') / 2     (mu the cluster mean)
 // (JJIAM 36 (2019)); C_J is solved in FP32 by this library's own solvers
 // (batched small path up to 128, large path above) and X_J <- X_J W_J in
-// double-float, which keeps the span of X_J exact; a cluster whose C_J is
+// double-float, which keeps the span of X_J exact (columns are re-sorted
+// afterwards when an update moved an eigenvalue past a neighbour); a cluster whose C_J is
 // already diagonal to 1e-15 ||A|| is not rotated (an FP32 rotation would
-// bring back 1e-7 non-orthogonality). When nothing was rotated and the next
-// correction ~ emax^2 ||A|| / gap_min is below 1e-14 (quadratic
-// convergence), one last "polishing" iteration forms the full double-float
-// Gram matrix and uses the symmetric form E = R/2 + sym(T)/(lam_j - lam_i):
-// the residual form recovers r_ij only to ~u ||A|| / gap_ij, the symmetric
-// form to u.
+// bring back 1e-7 non-orthogonality). When nothing was rotated and the
+// corrections are below 1e-7 (or at their rounding floor), one last
+// "polishing" iteration forms the full double-float Gram matrix and uses the
+// symmetric form E = R/2 + sym(T)/(lam_j - lam_i): the residual form
+// recovers r_ij only to ~u ||A|| / gap_ij, the symmetric form to u.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,6 +51,7 @@ namespace gla {
 constexpr int kRefMaxIters = 10;
 constexpr int kWin = 32;
 constexpr float kTheta = 0.05f;
+constexpr double kResTheta = 0.1;
 
 struct RefineLarge {
   int n = 0;
@@ -64,6 +66,7 @@ struct RefineLarge {
   int* cid = nullptr;      // per column: cluster id (or -1)
   float* scal = nullptr;   // [0] max |E| outside clusters, [2] max column norm of Rres (float bits)
   float* offmax = nullptr; // per cluster: max |off-diagonal| of C_J
+  float* rn = nullptr;     // per column: residual norm
   unsigned long long* amax = nullptr;
   int* flags = nullptr;    // [0] non-finite, [1] scale exponent
   int* cinfo = nullptr;
@@ -72,6 +75,7 @@ struct RefineLarge {
   std::vector<int> h_couple;
   int iters = 0;
   int rotated = 0;  // cluster rotations of the last run
+  int reorders = 0;
 };
 
 namespace {
@@ -148,11 +152,12 @@ __global__ void k_ref_colstats(const float* __restrict__ Xhi, const float* __res
   }
 }
 
-// Rres = P - X diag(lam), double-float, rounded to FP32; the largest column
-// norm goes to scal[2] (it bounds the FP32 error of T = X' Rres).
+// Rres = P - X diag(lam), double-float, rounded to FP32; column norms into
+// rn[j] (residual norms) and their maximum into *rmax.
 __global__ void k_ref_rres(const float* __restrict__ Xhi, const float* __restrict__ Xlo,
                            const float* __restrict__ Phi, const float* __restrict__ Plo,
-                           const double* __restrict__ lam, int n, float* __restrict__ R, float* colnorm) {
+                           const double* __restrict__ lam, int n, float* __restrict__ R, float* __restrict__ rn,
+                           float* rmax) {
   const int j = blockIdx.x;
   const df64 l = df_from(-lam[j]);
   float ss = 0.f;
@@ -171,17 +176,23 @@ __global__ void k_ref_rres(const float* __restrict__ Xhi, const float* __restric
   if (threadIdx.x == 0) {
     float t = 0.f;
     for (int w = 0; w < (int)(blockDim.x / 32); w++) t += red[w];
-    atomicMax(reinterpret_cast<int*>(colnorm), __float_as_int(sqrtf(t)));
+    rn[j] = sqrtf(t);
+    atomicMax(reinterpret_cast<int*>(rmax), __float_as_int(sqrtf(t)));
   }
 }
 
-// couple[p] = 1 joins sorted columns p and p+1 into one cluster.
-__global__ void k_ref_couple(const float* __restrict__ T, const double* __restrict__ lam, int n,
-                             int* __restrict__ couple) {
+// couple[p] = 1 joins sorted columns p and p+1 into one cluster: the gap is
+// below kResTheta^-1 times their residual norms (an eigenvector error bound
+// of the Davis-Kahan kind would then not be small), some pair (i, j) across
+// p with |i - j| <= kWin has |t_ij| > kTheta |lam_j - lam_i|, or the gap is
+// at rounding level.
+__global__ void k_ref_couple(const float* __restrict__ T, const double* __restrict__ lam,
+                             const float* __restrict__ rn, int n, int* __restrict__ couple) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n - 1) return;
   const double lmax = fmax(fabs(lam[0]), fabs(lam[n - 1]));
-  int c = fabs(lam[p + 1] - lam[p]) <= 64.0 * 0x1p-52 * lmax;
+  const double gp = fabs(lam[p + 1] - lam[p]);
+  int c = gp <= 64.0 * 0x1p-52 * lmax || gp * kResTheta <= (double)fmaxf(rn[p], rn[p + 1]);
   for (int i = max(0, p - kWin + 1); i <= p && !c; i++)
     for (int j = p + 1; j <= min(n - 1, i + kWin) && !c; j++) {
       const float gap = (float)fabs(lam[j] - lam[i]);
@@ -189,6 +200,14 @@ __global__ void k_ref_couple(const float* __restrict__ T, const double* __restri
       c = t > kTheta * gap;
     }
   couple[p] = c;
+}
+
+// dst[:, j] = src[:, perm[j]] (n x n, leading dimension n).
+__global__ void k_ref_gather(const float* __restrict__ src, float* __restrict__ dst, const int* __restrict__ perm,
+                             int n) {
+  const int j = blockIdx.y;
+  const long long s0 = (long long)perm[j] * n, d0 = (long long)j * n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[d0 + i] = src[s0 + i];
 }
 
 __device__ __forceinline__ void atomic_max_pos(float* a, float v) {
@@ -312,6 +331,7 @@ int refine_large_create(RefineLarge** out, int n) {
   alloc((void**)&r->cid, sizeof(int) * n);
   alloc((void**)&r->scal, sizeof(float) * 4);
   alloc((void**)&r->offmax, sizeof(float) * n);
+  alloc((void**)&r->rn, sizeof(float) * n);
   alloc((void**)&r->amax, sizeof(unsigned long long));
   alloc((void**)&r->flags, sizeof(int) * 4);
   alloc((void**)&r->cinfo, sizeof(int) * n);
@@ -337,6 +357,7 @@ void refine_large_destroy(RefineLarge* r) {
   cudaFree(r->cid);
   cudaFree(r->scal);
   cudaFree(r->offmax);
+  cudaFree(r->rn);
   cudaFree(r->amax);
   cudaFree(r->flags);
   cudaFree(r->cinfo);
@@ -434,8 +455,10 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
   RF_CUDA(cudaStreamSynchronize(st));
   r->iters = 0;
   r->rotated = 0;
+  r->reorders = 0;
   if (hflags[0] == 0) {
     bool polish = false;
+    double emax_prev = 1e300;
     for (int it = 0; it < kRefMaxIters; it++) {
       r->iters = it + 1;
       if (it == kRefMaxIters - 1) polish = true;
@@ -457,7 +480,7 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       k_ref_colstats<<<(n + 7) / 8, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, n, r->lam, r->gdiag);
       RF_CUDA(cudaGetLastError());
       RF_CUDA(cudaMemsetAsync(r->scal, 0, sizeof(float) * 4, st));
-      k_ref_rres<<<n, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, r->lam, n, r->Rres, r->scal + 2);
+      k_ref_rres<<<n, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, r->lam, n, r->Rres, r->rn, r->scal + 2);
       RF_CUDA(cudaGetLastError());
       // T = X' Rres (FP32)
       GemmDesc t{};
@@ -473,7 +496,7 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       t.alpha = 1.0;
       t.beta = 0.0;
       RF_CUDA(gemm_launch(false, true, false, false, t, 1, st));
-      k_ref_couple<<<(n + 255) / 256, 256, 0, st>>>(r->T, r->lam, n, r->couple);
+      k_ref_couple<<<(n + 255) / 256, 256, 0, st>>>(r->T, r->lam, r->rn, n, r->couple);
       RF_CUDA(cudaGetLastError());
       RF_CUDA(cudaMemcpyAsync(r->h_lam.data(), r->lam, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaMemcpyAsync(r->h_couple.data(), r->couple, sizeof(int) * (n - 1), cudaMemcpyDeviceToHost, st));
@@ -494,7 +517,7 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
           off += (long long)(q - p + 1) * (q - p + 1);
           for (int i = p; i <= q; i++) hcid[i] = (int)cs.size() - 1;
         }
-        if (q + 1 < n) gmin = std::min(gmin, r->h_lam[q + 1] - r->h_lam[q]);
+        if (q + 1 < n) gmin = std::min(gmin, std::fabs(r->h_lam[q + 1] - r->h_lam[q]));
         p = q + 1;
       }
       RF_CUDA(cudaMemcpyAsync(r->cid, hcid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
@@ -609,12 +632,38 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       }
       r->rotated += (int)rs.size();
       if (polish) break;
-      // the residual has converged (nothing rotated, the next eigenvector
-      // correction ~ emax^2 ||A|| / gap_min below 1e-14): one more iteration
-      // with the full Gram matrix restores orthogonality to working accuracy
-      // (the residual form recovers r_ij only to ~u ||A|| / gap_ij)
+      // the eigenvectors have (nearly) converged: nothing rotated, and the
+      // corrections are below 1e-7 (the polishing iteration, quadratically
+      // convergent, leaves ~emax^2 ||A|| in the residual) or have stopped
+      // falling (the rounding floor of the residual form, u ||A|| / gap, at
+      // the tightest gaps). One more iteration with the full Gram matrix then
+      // restores orthogonality to working accuracy (the residual form
+      // recovers r_ij only to ~u ||A|| / gap_ij).
       const double emax = hs[0];
-      if (rs.empty() && emax * emax * lmax < 1e-14 * gmin) polish = true;
+      if (rs.empty() && (emax < 1e-7 || (emax < 1e-5 && emax > 0.25 * emax_prev))) polish = true;
+      emax_prev = emax;
+      // keep the columns in ascending order (cluster updates can move an
+      // eigenvalue past a neighbour that was not in its cluster)
+      RF_CUDA(cudaMemcpyAsync(r->h_lam.data(), r->lam, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+      RF_CUDA(cudaStreamSynchronize(st));
+      bool ordered = true;
+      for (int i = 0; i + 1 < n; i++) ordered &= r->h_lam[i] <= r->h_lam[i + 1];
+      if (!ordered) {
+        std::vector<int> perm(n);
+        for (int i = 0; i < n; i++) perm[i] = i;
+        std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return r->h_lam[a] < r->h_lam[b]; });
+        std::vector<double> l2(n);
+        for (int i = 0; i < n; i++) l2[i] = r->h_lam[perm[i]];
+        RF_CUDA(cudaMemcpyAsync(r->cid, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        k_ref_gather<<<g2, 256, 0, st>>>(r->Xhi, r->Phi, r->cid, n);
+        k_ref_gather<<<g2, 256, 0, st>>>(r->Xlo, r->Plo, r->cid, n);
+        RF_CUDA(cudaGetLastError());
+        RF_CUDA(cudaMemcpyAsync(r->Xhi, r->Phi, sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+        RF_CUDA(cudaMemcpyAsync(r->Xlo, r->Plo, sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+        RF_CUDA(cudaMemcpyAsync(r->lam, l2.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        RF_CUDA(cudaStreamSynchronize(st));
+        r->reorders++;
+      }
     }
   }
   // final order (cluster updates keep it, but guard against swaps of
