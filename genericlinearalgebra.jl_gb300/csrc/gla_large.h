@@ -40,6 +40,20 @@ struct DfGemmDesc {
 };
 cudaError_t dfgemm_launch(const DfGemmDesc& g, bool ta, cudaStream_t st);
 
+// ---- tcgen05 Ozaki GEMM (ozaki.cuh / ozaki.cu): C = A B to double-float
+// accuracy on the bf16 tensor cores. Operands are sliced first: the A operand
+// from the columns of a float-pair matrix (its rows after transposition, or
+// the rows of a symmetric matrix), the B operand from its columns; S slices
+// of 7 bits each (S = 7 for ~48-bit inputs, 4 for exact floats).
+struct OzWork;
+int oz_create(OzWork** out, int m, int n, int K);
+void oz_destroy(OzWork* w);
+cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo, long long ld, int count, int len,
+                     int S, cudaStream_t st);
+cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
+                    cudaStream_t st);
+int* oz_error_word(OzWork* w);
+
 // ---- stage plans (one order, one working precision)
 struct SytrdPlan;
 cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64);

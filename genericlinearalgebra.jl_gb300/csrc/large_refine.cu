@@ -4,7 +4,7 @@
 //
 // Iteration on X (double-float columns, ascending lam), with A scaled by an
 // exact power of two:
-//   P    = A X                              double-float GEMM (dfgemm.cu)
+//   P    = A X                              tcgen05 Ozaki GEMM (ozaki.cuh)
 //   lam  = diag(X'P) / diag(X'X)            double-float column dots
 //   Rres = P - X diag(lam)                  double-float, rounded to FP32
 //   T    = X' Rres                          FP32 GEMM
@@ -71,6 +71,7 @@ struct RefineLarge {
   int* flags = nullptr;    // [0] non-finite, [1] scale exponent
   int* cinfo = nullptr;
   std::map<int, LargeCtx*> big;  // FP32 solvers for clusters above the small limit
+  OzWork* oz = nullptr;          // tcgen05 double-float GEMM (A X and the Gram matrix)
   std::vector<double> h_lam;
   std::vector<int> h_couple;
   int iters = 0;
@@ -339,6 +340,11 @@ int refine_large_create(RefineLarge** out, int n) {
     refine_large_destroy(r);
     return -1000 - (int)err;
   }
+  int orc = oz_create(&r->oz, n, n, n);
+  if (orc) {
+    refine_large_destroy(r);
+    return orc;
+  }
   r->h_lam.resize(n);
   r->h_couple.resize(n);
   *out = r;
@@ -362,6 +368,7 @@ void refine_large_destroy(RefineLarge* r) {
   cudaFree(r->flags);
   cudaFree(r->cinfo);
   for (auto& kv : r->big) large_destroy(kv.second);
+  oz_destroy(r->oz);
   delete r;
 }
 
@@ -450,6 +457,9 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
   k_ref_load<<<g2, 256, 0, st>>>(A, lda, n, lower, r->amax, r->flags, r->Ahi, r->Alo, X32, ldx, r->Xhi, r->Xlo, w32,
                                  r->lam);
   RF_CUDA(cudaGetLastError());
+  // A is symmetric: its rows are the columns of the (hi, lo) storage
+  RF_CUDA(oz_slice(r->oz, true, r->Ahi, r->Alo, n, n, n, 7, st));
+  RF_CUDA(cudaMemsetAsync(oz_error_word(r->oz), 0, sizeof(int), st));
   int hflags[2] = {0, 0};
   RF_CUDA(cudaMemcpyAsync(hflags, r->flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
   RF_CUDA(cudaStreamSynchronize(st));
@@ -462,21 +472,10 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
     for (int it = 0; it < kRefMaxIters; it++) {
       r->iters = it + 1;
       if (it == kRefMaxIters - 1) polish = true;
-      // P = A X
-      DfGemmDesc g{};
-      g.m = n;
-      g.n = n;
-      g.k = n;
-      g.Ahi = r->Ahi;
-      g.Alo = r->Alo;
-      g.lda = n;
-      g.Bhi = r->Xhi;
-      g.Blo = it == 0 ? nullptr : r->Xlo;  // the FP32 eigenvectors are exact floats
-      g.ldb = n;
-      g.Chi = r->Phi;
-      g.Clo = r->Plo;
-      g.ldc = n;
-      RF_CUDA(dfgemm_launch(g, false, st));
+      // P = A X on the tensor cores (Ozaki slices; the FP32 eigenvectors of
+      // the first iteration are exact floats, X_lo = 0)
+      RF_CUDA(oz_slice(r->oz, false, r->Xhi, it == 0 ? nullptr : r->Xlo, n, n, n, 7, st));
+      RF_CUDA(oz_gemm(r->oz, n, n, n, r->Phi, r->Plo, n, false, st));
       k_ref_colstats<<<(n + 7) / 8, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, n, r->lam, r->gdiag);
       RF_CUDA(cudaGetLastError());
       RF_CUDA(cudaMemsetAsync(r->scal, 0, sizeof(float) * 4, st));
@@ -524,21 +523,10 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       // Gram blocks of the clusters (before the update); the polishing
       // iteration forms the whole Gram matrix
       if (polish) {
-        DfGemmDesc gg{};
-        gg.m = n;
-        gg.n = n;
-        gg.k = n;
-        gg.lower = 1;
-        gg.Ahi = r->Xhi;
-        gg.Alo = r->Xlo;
-        gg.lda = n;
-        gg.Bhi = r->Xhi;
-        gg.Blo = r->Xlo;
-        gg.ldb = n;
-        gg.Chi = r->Ghi;
-        gg.Clo = r->Glo;
-        gg.ldc = n;
-        RF_CUDA(dfgemm_launch(gg, true, st));
+        // X'X: the A operand slices X's columns (A's own slices are no longer
+        // needed: this is the last iteration); X's B-operand slices are current
+        RF_CUDA(oz_slice(r->oz, true, r->Xhi, r->Xlo, n, n, n, 7, st));
+        RF_CUDA(oz_gemm(r->oz, n, n, n, r->Ghi, r->Glo, n, true, st));
       }
       for (size_t k = 0; k < cs.size() && !polish; k++) {
         DfGemmDesc gg{};
@@ -593,7 +581,10 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       if (!cs.empty())
         RF_CUDA(cudaMemcpyAsync(hoff.data(), r->offmax, sizeof(float) * cs.size(), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaMemcpyAsync(hs, r->scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
+      int oz_err = 0;
+      RF_CUDA(cudaMemcpyAsync(&oz_err, oz_error_word(r->oz), sizeof(int), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaStreamSynchronize(st));
+      if (oz_err) return -1000 - (int)cudaErrorLaunchTimeout;  // a bounded wait of the tensor-core GEMM ran out
       std::vector<int> rs, rcnt;
       std::vector<long long> roff;
       std::vector<double> rmu;
