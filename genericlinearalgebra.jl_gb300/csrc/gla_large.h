@@ -44,7 +44,9 @@ cudaError_t dfgemm_launch(const DfGemmDesc& g, bool ta, cudaStream_t st);
 // accuracy on the bf16 tensor cores. Operands are sliced first: the A operand
 // from the columns of a float-pair matrix (its rows after transposition, or
 // the rows of a symmetric matrix), the B operand from its columns; S slices
-// of 7 bits each (S = 7 for ~48-bit inputs, 4 for exact floats).
+// of 7 bits each, relative to the largest entry of the row or column (7 for
+// double-float accuracy whatever the spread of the entries). oz_create with
+// m = 0 or n = 0 allocates only the other operand.
 struct OzWork;
 int oz_create(OzWork** out, int m, int n, int K);
 void oz_destroy(OzWork* w);
@@ -52,6 +54,9 @@ cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo
                      int S, cudaStream_t st);
 cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
                     cudaStream_t st);
+// A operand from wa, B operand from wb (error word of wa).
+cudaError_t oz_gemm2(OzWork* wa, OzWork* wb, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
+                     cudaStream_t st);
 int* oz_error_word(OzWork* w);
 
 // ---- stage plans (one order, one working precision)

@@ -16,7 +16,8 @@
 //   X   <- X + X E                          FP32 GEMM, added in double-float
 // (T. Ogita, K. Aishima, JJIAM 35 (2018) Alg. 1, rewritten on the residual;
 // t_ij - t_ji = r_ij (lam_j - lam_i) carries the orthogonality correction of
-// separated pairs, so X'X is only formed inside clusters).
+// separated pairs, so X'X is only formed when clusters need it and in the
+// final polishing iteration, by the same tensor-core GEMM).
 // Clusters are runs of the sorted lam joined wherever a gap is below ten
 // times the residual norms of its two columns, some pair (i, j) with
 // |i - j| <= kWin has |t_ij| > kTheta |lam_j - lam_i| (the first-order update
@@ -71,7 +72,8 @@ struct RefineLarge {
   int* flags = nullptr;    // [0] non-finite, [1] scale exponent
   int* cinfo = nullptr;
   std::map<int, LargeCtx*> big;  // FP32 solvers for clusters above the small limit
-  OzWork* oz = nullptr;          // tcgen05 double-float GEMM (A X and the Gram matrix)
+  OzWork* oz = nullptr;          // tcgen05 double-float GEMM: A slices (A operand), X slices (B operand)
+  OzWork* ozx = nullptr;         // X slices as the A operand (the Gram matrix X'X)
   std::vector<double> h_lam;
   std::vector<int> h_couple;
   int iters = 0;
@@ -341,6 +343,7 @@ int refine_large_create(RefineLarge** out, int n) {
     return -1000 - (int)err;
   }
   int orc = oz_create(&r->oz, n, n, n);
+  if (!orc) orc = oz_create(&r->ozx, n, 0, n);
   if (orc) {
     refine_large_destroy(r);
     return orc;
@@ -369,6 +372,7 @@ void refine_large_destroy(RefineLarge* r) {
   cudaFree(r->cinfo);
   for (auto& kv : r->big) large_destroy(kv.second);
   oz_destroy(r->oz);
+  oz_destroy(r->ozx);
   delete r;
 }
 
@@ -520,30 +524,14 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
         p = q + 1;
       }
       RF_CUDA(cudaMemcpyAsync(r->cid, hcid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
-      // Gram blocks of the clusters (before the update); the polishing
-      // iteration forms the whole Gram matrix
-      if (polish) {
-        // X'X: the A operand slices X's columns (A's own slices are no longer
-        // needed: this is the last iteration); X's B-operand slices are current
-        RF_CUDA(oz_slice(r->oz, true, r->Xhi, r->Xlo, n, n, n, 7, st));
-        RF_CUDA(oz_gemm(r->oz, n, n, n, r->Ghi, r->Glo, n, true, st));
-      }
-      for (size_t k = 0; k < cs.size() && !polish; k++) {
-        DfGemmDesc gg{};
-        gg.m = cc[k];
-        gg.n = cc[k];
-        gg.k = n;
-        gg.lower = 1;
-        gg.Ahi = r->Xhi + (long long)cs[k] * n;
-        gg.Alo = r->Xlo + (long long)cs[k] * n;
-        gg.lda = n;
-        gg.Bhi = gg.Ahi;
-        gg.Blo = gg.Alo;
-        gg.ldb = n;
-        gg.Chi = r->Ghi + cs[k] + (long long)cs[k] * n;
-        gg.Clo = r->Glo + cs[k] + (long long)cs[k] * n;
-        gg.ldc = n;
-        RF_CUDA(dfgemm_launch(gg, true, st));
+      // the Gram matrix X'X (lower triangle, before the update) when some
+      // pair needs it: the polishing iteration, or clusters (pairs inside a
+      // cluster take E_ij = -(X'X)_ij / 2). One tensor-core GEMM; X's
+      // B-operand slices are current.
+      if (polish || !cs.empty()) {
+        RF_CUDA(oz_slice(r->ozx, true, r->Xhi, r->Xlo, n, n, n, 7, st));
+        RF_CUDA(cudaMemsetAsync(oz_error_word(r->ozx), 0, sizeof(int), st));
+        RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Ghi, r->Glo, n, true, st));
       }
       k_ref_e<<<g2, 256, 0, st>>>(r->T, r->Ghi, r->Glo, r->lam, r->gdiag, r->cid, n, polish ? 1 : 0, r->E, r->scal);
       RF_CUDA(cudaGetLastError());
@@ -581,10 +569,11 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       if (!cs.empty())
         RF_CUDA(cudaMemcpyAsync(hoff.data(), r->offmax, sizeof(float) * cs.size(), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaMemcpyAsync(hs, r->scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
-      int oz_err = 0;
-      RF_CUDA(cudaMemcpyAsync(&oz_err, oz_error_word(r->oz), sizeof(int), cudaMemcpyDeviceToHost, st));
+      int oz_err[2] = {0, 0};
+      RF_CUDA(cudaMemcpyAsync(&oz_err[0], oz_error_word(r->oz), sizeof(int), cudaMemcpyDeviceToHost, st));
+      RF_CUDA(cudaMemcpyAsync(&oz_err[1], oz_error_word(r->ozx), sizeof(int), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaStreamSynchronize(st));
-      if (oz_err) return -1000 - (int)cudaErrorLaunchTimeout;  // a bounded wait of the tensor-core GEMM ran out
+      if (oz_err[0] || oz_err[1]) return -1000 - (int)cudaErrorLaunchTimeout;  // a bounded wait of the tensor-core GEMM ran out
       std::vector<int> rs, rcnt;
       std::vector<long long> roff;
       std::vector<double> rmu;

@@ -34,10 +34,10 @@ int oz_create(OzWork** out, int m, int n, int K) {
   *out = nullptr;
   OzWork* w = new (std::nothrow) OzWork();
   if (!w) return -1000 - (int)cudaErrorMemoryAllocation;
-  init_sliced(w->A, m, K, oz::kBM);
-  init_sliced(w->B, n, K, oz::kBN);
-  w->abytes = sliced_bytes(m, K, oz::kBM, oz::kMaxSlices);
-  w->bbytes = sliced_bytes(n, K, oz::kBN, oz::kMaxSlices);
+  init_sliced(w->A, std::max(m, 1), K, oz::kBM);
+  init_sliced(w->B, std::max(n, 1), K, oz::kBN);
+  w->abytes = m > 0 ? sliced_bytes(m, K, oz::kBM, oz::kMaxSlices) : 16;
+  w->bbytes = n > 0 ? sliced_bytes(n, K, oz::kBN, oz::kMaxSlices) : 16;
   cudaError_t e = cudaMalloc((void**)&w->A.base, w->abytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&w->B.base, w->bbytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&w->A.exps, sizeof(int) * w->A.nblk * oz::kBM);
@@ -81,11 +81,17 @@ cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo
 
 cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
                     cudaStream_t st) {
+  return oz_gemm2(w, w, M, N, K, Chi, Clo, ldc, lower, st);
+}
+
+cudaError_t oz_gemm2(OzWork* wa, OzWork* wb, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
+                     cudaStream_t st) {
   if (M <= 0 || N <= 0) return cudaSuccess;
-  if (w->A.S < 1 || w->B.S < 1 || w->A.nks != w->B.nks) return cudaErrorInvalidValue;
+  if (wa->A.S < 1 || wb->B.S < 1 || wa->A.nks != wb->B.nks) return cudaErrorInvalidValue;
   oz::GemmArgs g;
-  g.A = w->A;
-  g.B = w->B;
+  g.A = wa->A;
+  g.B = wb->B;
+  OzWork* w = wa;
   g.M = M;
   g.N = N;
   g.K = K;

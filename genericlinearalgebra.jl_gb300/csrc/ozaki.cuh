@@ -9,7 +9,7 @@
 // multiplication and its applications", Numer. Algorithms 59 (2012)):
 // every row i of A is scaled by sigma_i = 2^e_i >= max_k |a_ik| and split
 // into integer slices, a_ik / sigma_i = sum_s d_s 2^(-7 s) (|d_1| <= 128,
-// |d_s| <= 64 after), likewise every column of B; all slices are exact in
+// |d_s| <= 65 after), likewise every column of B; all slices are exact in
 // bf16. A slice product sum_k d_s e_t is a sum of integers of at most 2^14,
 // so an FP32 accumulator holds it exactly while the running sum stays below
 // 2^24. Pairs with s + t = L share one TMEM accumulator per "level" L
@@ -152,38 +152,51 @@ struct GemmArgs {
 
 // Column c of a float-pair matrix (len entries, leading dimension ld; for a
 // symmetric A its column c is its row c) -> S integer slices of the scaled
-// values, written as row c of a tiled operand. One CTA per column.
+// values, written as row c of a tiled operand. One CTA per column. The
+// slicing runs in double-float arithmetic on the FP32 pipe: the remainder
+// r = (hi, lo) 2^-e is kept exactly (scalings by powers of two, TwoSum), the
+// next slice is rint of its leading float (|d_1| <= 128, |d_s| <= 65 after).
 __global__ void __launch_bounds__(256) k_oz_slice(const float* __restrict__ hi, const float* __restrict__ lo,
                                                   long long ld, int len, int ncols, Sliced out) {
   const int c = blockIdx.x;
-  __shared__ double red[8];
+  __shared__ float red[8];
   const float* h = hi + (long long)c * ld;
   const float* l = lo ? lo + (long long)c * ld : nullptr;
-  double m = 0.0;
+  float m = 0.f;
   if (c < ncols)
-    for (int k = threadIdx.x; k < len; k += 256) m = fmax(m, fabs((double)h[k] + (l ? (double)l[k] : 0.0)));
+    for (int k = threadIdx.x; k < len; k += 256) m = fmaxf(m, fabsf(h[k]));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
-  m = 0.0;
-  for (int w = 0; w < 8; w++) m = fmax(m, red[w]);
-  const int e = m > 0.0 ? ilogb(m) + 1 : 0;  // |v| 2^-e < 1
+  m = 0.f;
+  for (int w = 0; w < 8; w++) m = fmaxf(m, red[w]);
+  // |hi + lo| < 2^(ilogb(m) + 1) up to the last ulp: |value| 2^-e < 1 (an
+  // edge value reaching 1 gives d_1 = 129, still exact in bf16 and inside
+  // the accumulation bound)
+  const int e = m > 0.f ? ilogbf(m) + 1 : 0;
   if (threadIdx.x == 0) out.exps[c] = e;
   const int b = c / out.H, r = c % out.H;
   const size_t bb = (size_t)block_bytes(out.H);
   char* base = reinterpret_cast<char*>(out.base);
   const int kpad = out.nks * kKS;
   for (int k = threadIdx.x; k < kpad; k += 256) {
-    double v = 0.0;
-    if (c < ncols && k < len) v = ldexp((double)h[k] + (l ? (double)l[k] : 0.0), -e);
+    float vh = 0.f, vl = 0.f;
+    if (c < ncols && k < len) {
+      vh = ldexpf(h[k], -e);
+      vl = l ? ldexpf(l[k], -e) : 0.f;
+    }
     const int q = k / kKS, kk = k % kKS;
+    char* blk = base + (((size_t)b * out.nks + q) * bb) + tile_off(r, kk);
+    const size_t sstride = (size_t)out.nblk * out.nks * bb;
     for (int s = 0; s < out.S; s++) {
-      const double t = v * 128.0;
-      const double d = rint(t);
-      v = t - d;
-      char* blk = base + (((size_t)s * out.nblk + b) * out.nks + q) * bb;
-      *reinterpret_cast<__nv_bfloat16*>(blk + tile_off(r, kk)) = __float2bfloat16_rn((float)d);
+      const float th = vh * 128.f, tl = vl * 128.f;
+      const float d = rintf(th);
+      float sh, se;
+      two_sum(th - d, tl, sh, se);  // th - d is exact (|th - d| <= 1/2, same binade scale)
+      vh = sh;
+      vl = se;
+      *reinterpret_cast<__nv_bfloat16*>(blk + s * sstride) = __float2bfloat16_rn(d);
     }
   }
 }
