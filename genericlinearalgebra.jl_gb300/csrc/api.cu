@@ -737,6 +737,8 @@ struct SingleEntry {
 };
 std::mutex g_single_mu;
 std::map<SingleKey, SingleEntry> g_single;
+std::mutex g_gemm_mu;
+OzWork* g_gemm_w = nullptr;  // slice buffers of gla_gemm_df
 
 int single_entry(int prec, char jobz, char uplo, int64_t n, int flags, SingleEntry** out) {
   SingleKey k{prec, jobz, uplo, n, flags};
@@ -793,6 +795,48 @@ int gla_dsyev(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w
 
 int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, int* info, void* stream) {
   return syev_single<float>(GLA_PREC_F32, jobz, uplo, n, A, lda, w, info, stream);
+}
+
+int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* Alo, int64_t lda, const float* Bhi,
+                const float* Blo, int64_t ldb, float* Chi, float* Clo, int64_t ldc, void* stream) {
+  if (m < 0 || m > (1 << 24)) return -1;
+  if (n < 0 || n > (1 << 24)) return -2;
+  if (k < 0 || k > (1 << 24)) return -3;
+  if (!Ahi && m && k) return -4;
+  if (lda < std::max<int64_t>(1, m)) return -6;
+  if (!Bhi && n && k) return -7;
+  if (ldb < std::max<int64_t>(1, k)) return -9;
+  if ((!Chi || !Clo) && m && n) return -10;
+  if (ldc < std::max<int64_t>(1, m)) return -12;
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (k == 0) {
+    GLA_CUDA(cudaMemset2DAsync(Chi, sizeof(float) * ldc, 0, sizeof(float) * m, n, st));
+    GLA_CUDA(cudaMemset2DAsync(Clo, sizeof(float) * ldc, 0, sizeof(float) * m, n, st));
+    return 0;
+  }
+  std::lock_guard<std::mutex> lk(g_gemm_mu);
+  if (g_gemm_w) {
+    int h = 0;
+    GLA_CUDA(cudaMemcpy(&h, oz_error_word(g_gemm_w), sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+      GLA_CUDA(cudaMemset(oz_error_word(g_gemm_w), 0, sizeof(int)));
+      return -1000 - (int)cudaErrorLaunchTimeout;
+    }
+  }
+  if (!g_gemm_w || !oz_fits(g_gemm_w, (int)m, (int)n, (int)k)) {
+    if (g_gemm_w) {
+      GLA_CUDA(cudaDeviceSynchronize());
+      oz_destroy(g_gemm_w);
+      g_gemm_w = nullptr;
+    }
+    int rc = oz_create(&g_gemm_w, (int)m, (int)n, (int)k);
+    if (rc) return rc;
+  }
+  GLA_CUDA(oz_slice_rows(g_gemm_w, Ahi, Alo, lda, (int)m, (int)k, 7, st));
+  GLA_CUDA(oz_slice(g_gemm_w, false, Bhi, Blo, ldb, (int)n, (int)k, 7, st));
+  GLA_CUDA(oz_gemm(g_gemm_w, (int)m, (int)n, (int)k, Chi, Clo, ldc, false, st));
+  return 0;
 }
 
 int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz, int flags, int* info,

@@ -58,6 +58,10 @@ cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long
 cudaError_t oz_gemm2(OzWork* wa, OzWork* wb, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
                      cudaStream_t st);
 int* oz_error_word(OzWork* w);
+// A operand from the rows of a column-major matrix (element (r, k) at r + k ld).
+cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long ld, int rows, int len, int S,
+                          cudaStream_t st);
+bool oz_fits(const OzWork* w, int m, int n, int K);
 
 // ---- stage plans (one order, one working precision)
 struct SytrdPlan;

@@ -79,6 +79,20 @@ cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo
   return cudaGetLastError();
 }
 
+cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long ld, int rows, int len, int S,
+                          cudaStream_t st) {
+  oz::Sliced& s = w->A;
+  if (S < 1 || S > oz::kMaxSlices || rows > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks)
+    return cudaErrorInvalidValue;
+  s.S = S;
+  oz::k_oz_slice_rows<<<s.nblk, 256, 0, st>>>(hi, lo, ld, len, rows, s);
+  return cudaGetLastError();
+}
+
+bool oz_fits(const OzWork* w, int m, int n, int K) {
+  return w->A.nblk * w->A.H >= m && w->B.nblk * w->B.H >= n && w->A.nks == (K + oz::kKS - 1) / oz::kKS;
+}
+
 cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
                     cudaStream_t st) {
   return oz_gemm2(w, w, M, N, K, Chi, Clo, ldc, lower, st);

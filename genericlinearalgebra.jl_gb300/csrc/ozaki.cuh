@@ -201,6 +201,49 @@ __global__ void __launch_bounds__(256) k_oz_slice(const float* __restrict__ hi, 
   }
 }
 
+// Rows of a column-major float-pair matrix (element (c, k) at c + k ld) ->
+// tiled operand rows, same slicing as k_oz_slice. One CTA per block of
+// out.H rows; for each k the block's rows are read contiguously.
+__global__ void __launch_bounds__(256) k_oz_slice_rows(const float* __restrict__ hi, const float* __restrict__ lo,
+                                                       long long ld, int len, int nrows, Sliced out) {
+  const int b = blockIdx.x, H = out.H, tid = threadIdx.x;
+  const int per = 256 / H;            // threads per row (2 for H = 128, 4 for H = 64)
+  const int r = tid % H, part = tid / H;
+  const int c = b * H + r;
+  __shared__ float smax[256];
+  float m = 0.f;
+  if (c < nrows)
+    for (int k = part; k < len; k += per) m = fmaxf(m, fabsf(hi[c + (long long)k * ld]));
+  smax[tid] = m;
+  __syncthreads();
+  m = 0.f;
+  for (int q = 0; q < per; q++) m = fmaxf(m, smax[q * H + r]);
+  const int e = m > 0.f ? ilogbf(m) + 1 : 0;
+  if (part == 0) out.exps[c] = e;
+  const size_t bb = (size_t)block_bytes(H);
+  const size_t sstride = (size_t)out.nblk * out.nks * bb;
+  char* base = reinterpret_cast<char*>(out.base);
+  const int kpad = out.nks * kKS;
+  for (int k = part; k < kpad; k += per) {
+    float vh = 0.f, vl = 0.f;
+    if (c < nrows && k < len) {
+      vh = ldexpf(hi[c + (long long)k * ld], -e);
+      vl = lo ? ldexpf(lo[c + (long long)k * ld], -e) : 0.f;
+    }
+    const int q = k / kKS, kk = k % kKS;
+    char* blk = base + (((size_t)b * out.nks + q) * bb) + tile_off(r, kk);
+    for (int s = 0; s < out.S; s++) {
+      const float th = vh * 128.f, tl = vl * 128.f;
+      const float d = rintf(th);
+      float sh, se;
+      two_sum(th - d, tl, sh, se);
+      vh = sh;
+      vl = se;
+      *reinterpret_cast<__nv_bfloat16*>(blk + s * sstride) = __float2bfloat16_rn(d);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- GEMM
 
 __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {

@@ -34,6 +34,7 @@ _int = C.c_int
 _d = C.c_double
 SIGNATURES = {
     "gla_version": ([], _int),
+    "gla_gemm_df": ([_i64, _i64, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp], _int),
     "gla_status_string": ([_int], C.c_char_p),
     "gla_plan_create": ([C.POINTER(_vp), _int, _ch, _ch, _i64, C.POINTER(_i64), _d, _int], _int),
     "gla_plan_destroy": ([_vp], _int),

@@ -196,6 +196,22 @@ int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, 
 int gla_dsyev_static(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, int* info, void* stream);
 
 /*
+ * Double-float-accurate GEMM on the tcgen05 tensor cores (the product the
+ * FP32 + refinement path runs on): C = A B with A (m x k) and B (k x n) as
+ * float pairs A = Ahi + Alo, B = Bhi + Blo (column-major device arrays with
+ * leading dimensions lda, ldb; Alo / Blo may be NULL), returned as
+ * C = Chi + Clo (ldc). Ozaki scheme: every row of A and column of B is split
+ * into seven 7-bit integer slices relative to its largest entry (exact in
+ * bf16); the 28 slice products with s + t <= 8 are accumulated exactly in
+ * TMEM and summed in double-float, ~2^-47 of sum |a_ik||b_kj|. Slice
+ * buffers (~28 (m + n) k bytes) are allocated by the first call of a given
+ * size and kept for later calls. Asynchronous on `stream`; returns -1000 -
+ * cudaErrorLaunchTimeout at the next call if a bounded wait ran out.
+ */
+int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* Alo, int64_t lda, const float* Bhi,
+                const float* Blo, int64_t ldb, float* Chi, float* Clo, int64_t ldc, void* stream);
+
+/*
  * eigen!/eigvals! of SymTridiagonal(d, e) (src/eigenSelfAdjoint.jl:581,
  * :602-612, :623): d (n), e (n-1) device arrays, overwritten; on return d
  * holds the ascending eigenvalues and Z (n x n, ldz) the eigenvectors
