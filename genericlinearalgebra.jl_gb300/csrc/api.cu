@@ -117,6 +117,7 @@ struct gla_plan_s {
   int* h_info = nullptr;
   int* pin_pending = nullptr;
   df64* d_adj = nullptr;  // adjoint workspace (allocated by the first gla_plan_adjoint)
+  double* h_adj = nullptr;  // device staging of gla_plan_adjoint_host
   // orders above GLA_MAX_SMALL_N: solved one at a time by the large path
   std::vector<int> large_idx;           // batch indices, in batch order
   std::map<int, LargeCtx*> large_ctx;   // one context per distinct order
@@ -367,6 +368,7 @@ int gla_plan_destroy(gla_plan_t p) {
   cudaFree(p->h_info);
   cudaFreeHost(p->pin_pending);
   cudaFree(p->d_adj);
+  cudaFree(p->h_adj);
   for (auto& kv : p->large_ctx) large_destroy(kv.second);
   for (auto& kv : p->large_ref) refine_large_destroy(kv.second);
   cudaFreeHost(p->h_large_info);
@@ -666,6 +668,37 @@ int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const doubl
   return 0;
 }
 
+int gla_plan_adjoint_host(gla_plan_t p, const double* w, const double* V, const double* wbar, const double* Vbar,
+                          double* Abar, double gap_rel, void* stream) {
+  if (!p) return -1;
+  if (p->prec == GLA_PREC_F32) return -1;
+  if (!w && p->w_elems) return -2;
+  if (!V && p->a_elems) return -3;
+  if (!wbar && p->w_elems) return -4;
+  if (!Vbar && p->a_elems) return -5;
+  if (!Abar && p->a_elems) return -6;
+  if (!(gap_rel == gap_rel)) return -7;
+  if (!p->large_idx.empty()) return GLA_ERR_UNSUPPORTED;
+  if (p->nwork == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t ab = sizeof(double) * p->a_elems, wb = sizeof(double) * p->w_elems;
+  if (!p->h_adj) GLA_CUDA(cudaMalloc((void**)&p->h_adj, 3 * ab + 2 * wb));
+  double* dV = p->h_adj;
+  double* dVbar = dV + p->a_elems;
+  double* dAbar = dVbar + p->a_elems;
+  double* dw = dAbar + p->a_elems;
+  double* dwbar = dw + p->w_elems;
+  GLA_CUDA(cudaMemcpyAsync(dV, V, ab, cudaMemcpyHostToDevice, st));
+  GLA_CUDA(cudaMemcpyAsync(dVbar, Vbar, ab, cudaMemcpyHostToDevice, st));
+  GLA_CUDA(cudaMemcpyAsync(dw, w, wb, cudaMemcpyHostToDevice, st));
+  GLA_CUDA(cudaMemcpyAsync(dwbar, wbar, wb, cudaMemcpyHostToDevice, st));
+  int rc = gla_plan_adjoint(p, dw, dV, dwbar, dVbar, dAbar, gap_rel, stream);
+  if (rc) return rc;
+  GLA_CUDA(cudaMemcpyAsync(Abar, dAbar, ab, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
 int gla_plan_phase_times(gla_plan_t p, float* ms) {
   if (!p) return -1;
   if (!ms) return -2;
@@ -739,6 +772,7 @@ std::mutex g_single_mu;
 std::map<SingleKey, SingleEntry> g_single;
 std::mutex g_gemm_mu;
 OzWork* g_gemm_w = nullptr;  // slice buffers of gla_gemm_df
+std::map<int, LargeCtx*> g_stev_large;  // gla_dstev above GLA_MAX_SMALL_N
 
 int single_entry(int prec, char jobz, char uplo, int64_t n, int flags, SingleEntry** out) {
   SingleKey k{prec, jobz, uplo, n, flags};
@@ -842,7 +876,30 @@ int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* 
 int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz, int flags, int* info,
               void* stream) {
   if (jobz != 'V' && jobz != 'N') return -1;
-  if (n < 0 || n > GLA_MAX_SMALL_N) return -2;
+  if (n < 0 || n > GLA_MAX_N) return -2;
+  if (n > GLA_MAX_SMALL_N) {  // divide and conquer
+    if (!d) return -3;
+    if (!e) return -4;
+    if (jobz == 'V' && !Z) return -5;
+    if (jobz == 'V' && ldz < n) return -6;
+    if ((flags & ~3) != 0 || (flags & 3) > GLA_ALG_QR) return -7;
+    if (!info) return -8;
+    std::lock_guard<std::mutex> lk(g_single_mu);
+    auto it = g_stev_large.find((int)n);
+    if (it == g_stev_large.end()) {
+      LargeCtx* c = nullptr;
+      int rc = large_create(&c, (int)n, true);
+      if (rc) return rc;
+      it = g_stev_large.emplace((int)n, c).first;
+    }
+    int inf = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    // eigenvalues are written over d (LAPACK dstev convention, like the small path)
+    int rc = large_stev(it->second, d, e, d, jobz == 'V' ? Z : nullptr, ldz, &inf, st);
+    if (rc) return rc;
+    *info = inf;
+    return inf != 0;
+  }
   if (!d && n) return -3;
   if (!e && n > 1) return -4;
   if (jobz == 'V' && !Z && n) return -5;

@@ -43,9 +43,10 @@ cudaError_t dfgemm_launch(const DfGemmDesc& g, bool ta, cudaStream_t st);
 // ---- tcgen05 Ozaki GEMM (ozaki.cuh / ozaki.cu): C = A B to double-float
 // accuracy on the bf16 tensor cores. Operands are sliced first: the A operand
 // from the columns of a float-pair matrix (its rows after transposition, or
-// the rows of a symmetric matrix), the B operand from its columns; S slices
-// of 7 bits each, relative to the largest entry of the row or column (7 for
-// double-float accuracy whatever the spread of the entries). oz_create with
+// the rows of a symmetric matrix), the B operand from its columns; S = 7
+// slices of 7 bits each (the only count accepted), relative to the largest
+// entry of the row or column: double-float accuracy whatever the spread of
+// the entries. oz_create with
 // m = 0 or n = 0 allocates only the other operand.
 struct OzWork;
 int oz_create(OzWork** out, int m, int n, int K);
@@ -111,6 +112,12 @@ int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void
 // unconverged. Synchronises st before returning.
 int large_syev(LargeCtx* c, int tcode, bool wantv, bool lower, const void* Ain, long long lda, void* w, void* V,
                long long ldv, int* info_host, cudaStream_t st);
+
+// SymTridiagonal (d, e) of the context's order (FP64 context): ascending
+// eigenvalues into w, eigenvectors into Z (ldz, may be null). *info_host: 0,
+// -1 (non-finite input), > 0 unconverged. Synchronises st.
+int large_stev(LargeCtx* c, const double* d, const double* e, double* w, double* Z, long long ldz, int* info_host,
+               cudaStream_t st);
 
 // ---- refinement of FP32 eigenpairs of one large matrix (large_refine.cu)
 struct RefineLarge;

@@ -266,4 +266,36 @@ int large_syev(LargeCtx* c, int tcode, bool wantv, bool lower, const void* Ain, 
   return 0;
 }
 
+// SymTridiagonal input (the reference's eigen!(::SymTridiagonal),
+// src/eigenSelfAdjoint.jl:602-612): divide and conquer on (d, e) as given
+// (FP64 context), eigenvalues ascending into w, eigenvectors into Z (ldz)
+// when wanted. Synchronises st.
+int large_stev(LargeCtx* c, const double* d, const double* e, double* w, double* Z, long long ldz, int* info_host,
+               cudaStream_t st) {
+  const int n = c->n;
+  if (!c->f64) return -1000 - (int)cudaErrorInvalidValue;
+  LG_CUDA(cudaMemcpyAsync(c->d, d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  LG_CUDA(cudaMemsetAsync(c->e, 0, sizeof(double) * n, st));
+  if (n > 1) LG_CUDA(cudaMemcpyAsync(c->e, e, sizeof(double) * (n - 1), cudaMemcpyDeviceToDevice, st));
+  int rc = dc_enqueue(c->dc, c->d, c->e, c->Z, c->leaf_info, st);
+  if (rc) return rc;
+  LG_CUDA(cudaMemcpyAsync(w, c->d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (Z)
+    LG_CUDA(cudaMemcpy2DAsync(Z, sizeof(double) * ldz, c->Z, sizeof(double) * n, sizeof(double) * n, n,
+                              cudaMemcpyDeviceToDevice, st));
+  LG_CUDA(cudaMemcpyAsync(c->h_stat + 1, dc_fail_word(c->dc), sizeof(int), cudaMemcpyDeviceToHost, st));
+  const int nleaf = dc_leaf_count(c->dc);
+  std::vector<int> li(nleaf);
+  LG_CUDA(cudaMemcpyAsync(li.data(), c->leaf_info, sizeof(int) * nleaf, cudaMemcpyDeviceToHost, st));
+  LG_CUDA(cudaStreamSynchronize(st));
+  int bad = c->h_stat[1] ? 1 : 0;
+  bool nonfinite = false;
+  for (int x : li) {
+    if (x < 0) nonfinite = true;
+    if (x > 0) bad += x;
+  }
+  *info_host = nonfinite ? -1 : bad;
+  return 0;
+}
+
 }  // namespace gla

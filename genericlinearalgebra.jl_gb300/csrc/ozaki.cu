@@ -72,7 +72,7 @@ void oz_destroy(OzWork* w) {
 cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo, long long ld, int count, int len,
                      int S, cudaStream_t st) {
   oz::Sliced& s = a_operand ? w->A : w->B;
-  if (S < 1 || S > oz::kMaxSlices || count > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks)
+  if (S != oz::kMaxSlices || count > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks)
     return cudaErrorInvalidValue;
   s.S = S;
   oz::k_oz_slice<<<s.nblk * s.H, 256, 0, st>>>(hi, lo, ld, len, count, s);
@@ -82,7 +82,7 @@ cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo
 cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long ld, int rows, int len, int S,
                           cudaStream_t st) {
   oz::Sliced& s = w->A;
-  if (S < 1 || S > oz::kMaxSlices || rows > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks)
+  if (S != oz::kMaxSlices || rows > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks)
     return cudaErrorInvalidValue;
   s.S = S;
   oz::k_oz_slice_rows<<<s.nblk, 256, 0, st>>>(hi, lo, ld, len, rows, s);
@@ -101,7 +101,7 @@ cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long
 cudaError_t oz_gemm2(OzWork* wa, OzWork* wb, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
                      cudaStream_t st) {
   if (M <= 0 || N <= 0) return cudaSuccess;
-  if (wa->A.S < 1 || wb->B.S < 1 || wa->A.nks != wb->B.nks) return cudaErrorInvalidValue;
+  if (wa->A.S != oz::kMaxSlices || wb->B.S != oz::kMaxSlices || wa->A.nks != wb->B.nks) return cudaErrorInvalidValue;
   oz::GemmArgs g;
   g.A = wa->A;
   g.B = wb->B;

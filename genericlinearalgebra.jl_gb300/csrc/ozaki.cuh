@@ -14,20 +14,22 @@
 // so an FP32 accumulator holds it exactly while the running sum stays below
 // 2^24. Pairs with s + t = L share one TMEM accumulator per "level" L
 // (L = 2 .. 8, the pairs with s + t <= 8: 2^-47 of the scaled product), and
-// every 128 k the accumulators are drained into double-float registers
-// (at most 7 pairs x 128 products x 2^14 < 2^24: exact).
+// every 256 k the accumulators are drained into double-float registers.
+// Exactness of a 256-k group: |d_1| <= 129, |d_s| <= 65 (s >= 2), so a level
+// adds per k at most 129^2 (L = 2) or 2 x 129 x 65 + 5 x 65^2 = 37,895
+// (L = 8, the largest), and 256 x 37,895 < 2^24.
 //
-// Kernel layout: CTA tile 128 x 64 of C, 6 warps. Warp 0 (one lane) streams
-// the slices of each 32-wide k slab with 1D bulk copies into a two-stage
-// shared-memory ring (the slices are stored pre-tiled in the MMA's
-// canonical no-swizzle K-major layout, so a slab of one slice is one
-// contiguous block); warp 1 (one lane) issues tcgen05.mma (M = 128, N = 64,
-// K = 16, bf16 -> f32) into the level accumulators and commits to
-// mbarriers; warps 2-5 drain TMEM (tcgen05.ld) after each 128-k group and
-// keep the double-float sums of their row, then scale and store. Every
-// mbarrier wait is bounded: a wait that runs out sets the error word, the
-// CTA stops issuing work, waits (bounded) for its own copies and MMAs, frees
-// its TMEM and returns.
+// Kernel layout: CTA tile 128 x 64 of C, 10 warps. Warp 0 (one lane)
+// streams each 32-wide k slab with two 1D bulk copies (all A slices, all B
+// slices; they are stored pre-tiled in the MMA's canonical no-swizzle
+// K-major layout, slab-major) into a two-stage shared-memory ring; warp 1
+// (one lane) issues tcgen05.mma (M = 128, N = 64, K = 16, bf16 -> f32) into
+// the level accumulators, the 28 pairs unrolled with constant descriptor
+// offsets, and commits to mbarriers; warps 2-9 drain TMEM (tcgen05.ld)
+// after each 256-k group, each thread keeping the double-float sums of 32
+// columns of its row, then scale and store. Every mbarrier wait is bounded:
+// a wait that runs out sets the error word, the CTA stops issuing work,
+// waits (bounded) for its own copies and MMAs, frees its TMEM and returns.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -40,16 +42,18 @@ namespace oz {
 
 constexpr int kBM = 128;        // C tile rows (MMA M)
 constexpr int kBN = 64;         // C tile columns (MMA N)
-constexpr int kKS = 32;         // k per pipeline stage
+constexpr int kKS = 32;         // k per pipeline stage (two K = 16 MMAs per slice pair)
 constexpr int kStages = 2;
-constexpr int kGroupK = 128;    // k per TMEM drain (exactness bound)
+constexpr int kGroupK = 256;    // k per TMEM drain (exactness bound)
 constexpr int kMaxSlices = 7;
 constexpr int kMaxLevel = 8;    // pairs with s + t <= kMaxLevel
 constexpr int kLevels = kMaxLevel - 1;  // levels 2 .. 8
-constexpr int kThreads = 192;
+constexpr int kDrainWarps = 8;  // two per TMEM lane quarter, 32 columns each
+constexpr int kThreads = 64 + 32 * kDrainWarps;
+constexpr int kDrainCols = kBN / (kDrainWarps / 4);
 constexpr long long kWaitLimit = 1ll << 26;
 
-// Bytes of one tiled slab block: rows x 32 k, bf16.
+// Bytes of one tiled slab block: rows x kKS k, bf16.
 __host__ __device__ constexpr int block_bytes(int rows) { return rows * kKS * 2; }
 constexpr int kABlock = block_bytes(kBM);  // 8 KB
 constexpr int kBBlock = block_bytes(kBN);  // 4 KB
@@ -57,17 +61,19 @@ __host__ __device__ constexpr size_t stage_bytes(int sa, int sb) { return (size_
 
 // Byte offset of element (r, kk) inside a tiled slab block (8-row x 8-k core
 // matrices of 128 contiguous bytes; K-neighbours 128 B apart = LBO, row
-// groups 512 B apart = SBO).
+// groups kSBO = 512 B apart = SBO).
+constexpr int kSBO = kKS * 16;
 __host__ __device__ __forceinline__ int tile_off(int r, int kk) {
-  return (r >> 3) * 512 + (kk >> 3) * 128 + (r & 7) * 16 + (kk & 7) * 2;
+  return (r >> 3) * kSBO + (kk >> 3) * 128 + (r & 7) * 16 + (kk & 7) * 2;
 }
 
 // Sliced operand: slice s, row block b (height H rows), k slab q at
-// base + ((s * nblk + b) * nks + q) * block_bytes(H).
+// base + ((b * nks + q) * kMaxSlices + s) * block_bytes(H): the slices of one
+// slab are adjacent, so one bulk copy moves all of them.
 struct Sliced {
   __nv_bfloat16* base;
   int* exps;   // per row: scale exponent e (rows scaled by 2^-e)
-  int rows, nblk, nks, H, S;
+  int rows, nblk, nks, H, S;  // S: kMaxSlices once sliced, 0 before
 };
 
 GLA_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -76,7 +82,7 @@ GLA_DEV uint64_t make_desc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr >> 4) & 0x3FFF);
   d |= (uint64_t)((128u >> 4) & 0x3FFF) << 16;  // LBO: K-neighbour core matrices
-  d |= (uint64_t)((512u >> 4) & 0x3FFF) << 32;  // SBO: next 8-row group
+  d |= (uint64_t)(((uint32_t)kSBO >> 4) & 0x3FFF) << 32;  // SBO: next 8-row group
   d |= (uint64_t)1 << 46;                        // descriptor version (tcgen05)
   return d;                                      // base offset 0, no swizzle
 }
@@ -187,16 +193,15 @@ __global__ void __launch_bounds__(256) k_oz_slice(const float* __restrict__ hi, 
       vl = l ? ldexpf(l[k], -e) : 0.f;
     }
     const int q = k / kKS, kk = k % kKS;
-    char* blk = base + (((size_t)b * out.nks + q) * bb) + tile_off(r, kk);
-    const size_t sstride = (size_t)out.nblk * out.nks * bb;
-    for (int s = 0; s < out.S; s++) {
+    char* blk = base + (((size_t)b * out.nks + q) * kMaxSlices * bb) + tile_off(r, kk);
+    for (int s = 0; s < kMaxSlices; s++) {
       const float th = vh * 128.f, tl = vl * 128.f;
       const float d = rintf(th);
       float sh, se;
       two_sum(th - d, tl, sh, se);  // th - d is exact (|th - d| <= 1/2, same binade scale)
       vh = sh;
       vl = se;
-      *reinterpret_cast<__nv_bfloat16*>(blk + s * sstride) = __float2bfloat16_rn(d);
+      *reinterpret_cast<__nv_bfloat16*>(blk + s * bb) = __float2bfloat16_rn(d);
     }
   }
 }
@@ -221,7 +226,6 @@ __global__ void __launch_bounds__(256) k_oz_slice_rows(const float* __restrict__
   const int e = m > 0.f ? ilogbf(m) + 1 : 0;
   if (part == 0) out.exps[c] = e;
   const size_t bb = (size_t)block_bytes(H);
-  const size_t sstride = (size_t)out.nblk * out.nks * bb;
   char* base = reinterpret_cast<char*>(out.base);
   const int kpad = out.nks * kKS;
   for (int k = part; k < kpad; k += per) {
@@ -231,15 +235,15 @@ __global__ void __launch_bounds__(256) k_oz_slice_rows(const float* __restrict__
       vl = lo ? ldexpf(lo[c + (long long)k * ld], -e) : 0.f;
     }
     const int q = k / kKS, kk = k % kKS;
-    char* blk = base + (((size_t)b * out.nks + q) * bb) + tile_off(r, kk);
-    for (int s = 0; s < out.S; s++) {
+    char* blk = base + (((size_t)b * out.nks + q) * kMaxSlices * bb) + tile_off(r, kk);
+    for (int s = 0; s < kMaxSlices; s++) {
       const float th = vh * 128.f, tl = vl * 128.f;
       const float d = rintf(th);
       float sh, se;
       two_sum(th - d, tl, sh, se);
       vh = sh;
       vl = se;
-      *reinterpret_cast<__nv_bfloat16*>(blk + s * sstride) = __float2bfloat16_rn(d);
+      *reinterpret_cast<__nv_bfloat16*>(blk + s * bb) = __float2bfloat16_rn(d);
     }
   }
 }
@@ -256,7 +260,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
   const int tm = blockIdx.x / g.ntn, tn = blockIdx.x % g.ntn;
   const int row0 = tm * kBM, col0 = tn * kBN;
   if (g.lower && row0 + kBM <= col0) return;  // (uniform) no TMEM touched yet
-  const int SA = g.A.S, SB = g.B.S;
   const int nks = g.A.nks;
   const int ngroups = (nks * kKS + kGroupK - 1) / kGroupK;
   const int spg = kGroupK / kKS;  // stages per drain group
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
       mbar_init(&empty_bar[i], 1);
     }
     mbar_init(&drain_full, 1);
-    mbar_init(&drain_empty, 128);
+    mbar_init(&drain_empty, 32 * kDrainWarps);
     mbar_init(&fin_bar, 1);
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
@@ -281,7 +284,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
-  const size_t stB = stage_bytes(SA, SB);
+  constexpr size_t stB = stage_bytes(kMaxSlices, kMaxSlices);
+  constexpr uint32_t kAAll = kMaxSlices * kABlock, kBAll = kMaxSlices * kBBlock;
 
   if (wid == 0) {
     // ---- producer: slabs of every slice into the stage ring
@@ -298,11 +302,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
         issued = q + 1;
         unsigned char* dst = sm + st * stB;
         mbar_expect_tx(&full_bar[st], (uint32_t)stB);
-        for (int s = 0; s < SA; s++)
-          bulk_g2s(dst + s * kABlock, Ab + (((size_t)s * g.A.nblk + tm) * nks + q) * kABlock, kABlock, &full_bar[st]);
-        for (int t = 0; t < SB; t++)
-          bulk_g2s(dst + SA * kABlock + t * kBBlock, Bb + (((size_t)t * g.B.nblk + tn) * nks + q) * kBBlock, kBBlock,
-                   &full_bar[st]);
+        bulk_g2s(dst, Ab + ((size_t)tm * nks + q) * kAAll, kAAll, &full_bar[st]);
+        bulk_g2s(dst + kAAll, Bb + ((size_t)tn * nks + q) * kBAll, kBAll, &full_bar[st]);
       }
       // before the CTA may exit, its last copies must have landed (bounded;
       // already true unless the CTA aborted)
@@ -311,16 +312,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
         }
     }
   } else if (wid == 1) {
-    // ---- MMA issuer
+    // ---- MMA issuer: per slab the 28 slice pairs, unrolled with constant
+    // descriptor offsets (the descriptor's address field is addr >> 4 and
+    // shared-memory offsets stay below 2^18, so adding offset >> 4 is exact)
     if (lane == 0) {
-      bool fresh[kLevels + 2];
       for (int gi = 0; gi < ngroups && !*s_abort; gi++) {
         if (gi > 0 && !mbar_wait(&drain_empty, (gi - 1) & 1, err)) {  // the drain of group gi-1 is done
           *s_abort = 1;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        for (int L = 0; L < kLevels + 2; L++) fresh[L] = true;
         for (int qq = 0; qq < spg; qq++) {
           const int q = gi * spg + qq;
           if (q >= nks) break;
@@ -330,31 +331,36 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t abase = smem_u32(sm + st * stB), bbase = abase + SA * kABlock;
-          for (int s = 1; s <= SA; s++)
-            for (int t = 1; t <= SB && s + t <= kMaxLevel; t++) {
-              const int L = s + t;
-              const uint32_t dcol = tmem + (uint32_t)((L - 2) * kBN);
+          const uint64_t a0 = make_desc(smem_u32(sm + st * stB));
+          const uint64_t b0 = a0 + (uint64_t)(kAAll >> 4);
 #pragma unroll
-              for (int ks = 0; ks < kKS / 16; ks++) {  // K = 16 per instruction: 2 K-core matrices = 256 B
-                const uint64_t ad = make_desc(abase + (s - 1) * kABlock + ks * 256);
-                const uint64_t bd = make_desc(bbase + (t - 1) * kBBlock + ks * 256);
-                mma_f16(dcol, ad, bd, fresh[L] ? 0u : 1u);
-                fresh[L] = false;
+          for (int ks = 0; ks < kKS / 16; ks++)  // K = 16 per instruction: 2 K-core matrices = 256 B
+#pragma unroll
+            for (int s = 1; s <= kMaxSlices; s++)
+#pragma unroll
+              for (int t = 1; t <= kMaxSlices; t++) {
+                if (s + t > kMaxLevel) continue;
+                // in this order (s = 1 first) the group's first MMA into
+                // level s + t has s = 1 and starts the accumulator from zero
+                const uint32_t accumulate = (qq == 0 && ks == 0 && s == 1) ? 0u : 1u;
+                mma_f16(tmem + (uint32_t)((s + t - 2) * kBN),
+                        a0 + (uint64_t)(((s - 1) * kABlock + ks * 256) >> 4),
+                        b0 + (uint64_t)(((t - 1) * kBBlock + ks * 256) >> 4), accumulate);
               }
-            }
           mma_commit(&empty_bar[st]);  // stage buffer reusable once these MMAs finish
         }
         mma_commit(&drain_full);  // the group's accumulators are complete
       }
     }
   } else {
-    // ---- drain warps: TMEM lanes 32 (wid % 4) .. +31 = C rows of this thread
+    // ---- drain warps: TMEM lanes 32 (wid % 4) .. +31 = C rows of this
+    // thread; columns cbase .. cbase + kDrainCols - 1 of the tile
     const int quarter = wid & 3;
+    const int cbase = ((wid - 2) / 4) * kDrainCols;
     const int r = row0 + quarter * 32 + lane;
-    df64 acc[kBN];
+    df64 acc[kDrainCols];
 #pragma unroll
-    for (int c = 0; c < kBN; c++) acc[c] = df_make(0.f, 0.f);
+    for (int c = 0; c < kDrainCols; c++) acc[c] = df_make(0.f, 0.f);
     bool ok = true;
     for (int gi = 0; gi < ngroups && ok; gi++) {
       if (!mbar_wait(&drain_full, gi & 1, err)) {
@@ -364,15 +370,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       // level values of each column, exact integers; combine small to large
 #pragma unroll
-      for (int c0 = 0; c0 < kBN; c0 += 16) {
+      for (int c0 = 0; c0 < kDrainCols; c0 += 16) {
         float part_hi[16], part_lo[16];
 #pragma unroll
         for (int q = 0; q < 16; q++) part_hi[q] = part_lo[q] = 0.f;
 #pragma unroll 1
         for (int L = kMaxLevel; L >= 2; L--) {
-          if (L > SA + SB) continue;  // no slice pair at this level
           uint32_t v[16];
-          tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((L - 2) * kBN + c0), v);
+          tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((L - 2) * kBN + cbase + c0), v);
           asm volatile("tcgen05.wait::ld.sync.aligned;");
           const float sc = ldexpf(1.f, -7 * L);
 #pragma unroll
@@ -392,8 +397,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
     if (ok && !*err) {
       const int ei = r < g.M ? g.A.exps[r] : 0;
 #pragma unroll
-      for (int c = 0; c < kBN; c++) {
-        const int col = col0 + c;
+      for (int c = 0; c < kDrainCols; c++) {
+        const int col = col0 + cbase + c;
         if (r >= g.M || col >= g.N || (g.lower && r < col)) continue;
         const int e = ei + g.B.exps[col];
         const long long idx = (long long)r + (long long)col * g.ldc;

@@ -183,6 +183,17 @@ class Plan:
                                           C.c_void_p(Abar.data_ptr()), float(gap_rel), _stream_ptr(stream))
         return _lib.check(rc, "gla_plan_adjoint")
 
+    def adjoint_host(self, w, V, wbar, Vbar, Abar, gap_rel=0.0, stream=None):
+        """adjoint() on host numpy arenas (float64, C-contiguous); the library
+        stages them on the device and synchronizes."""
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (w, V, wbar, Vbar)]
+        if not (Abar.dtype == np.float64 and Abar.flags.c_contiguous):
+            raise ValueError("Abar must be a C-contiguous float64 array")
+        rc = _lib.load().gla_plan_adjoint_host(self._h, *[C.c_void_p(x.ctypes.data) for x in arrs],
+                                               C.c_void_p(Abar.ctypes.data), float(gap_rel),
+                                               _stream_ptr(stream) if stream is not None else None)
+        return _lib.check(rc, "gla_plan_adjoint_host")
+
     def stats(self):
         """Work counters of the last execute (rotations, sweeps, row_rotations,
         refine_n3, passes)."""
@@ -350,5 +361,21 @@ def eigvals(A, uplo="L", tol=None, precision="f64"):
     return eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
 
 
-__all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
+def eigen2(A, uplo="L", tol=None, precision="f64", alg="QL"):
+    """eigen2 (src/eigenSelfAdjoint.jl:633-668): ascending eigenvalues and the
+    FIRST and LAST rows of the eigenvector matrix (a 2 x n array; for n = 1
+    both rows are the single entry). The rows are those of eigen(A) on the
+    same input: the reference accumulates only these two rows of the
+    rotations, the device path forms the full matrix and keeps two rows."""
+    r = eigen(A, uplo=uplo, tol=tol, precision=precision, alg=alg)
+    vals, vecs = r
+    n = vecs.shape[0]
+    rows = [0, n - 1]
+    if _is_torch(vecs):
+        torch = _torch()
+        return Eigen(vals, vecs[torch.tensor(rows, device=vecs.device)].clone())
+    return Eigen(vals, vecs[rows].copy())
+
+
+__all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigen2", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

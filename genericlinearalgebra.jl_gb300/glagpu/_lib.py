@@ -46,6 +46,7 @@ SIGNATURES = {
     "gla_plan_phase_times": ([_vp, C.POINTER(C.c_float)], _int),
     "gla_plan_counters": ([_vp, C.POINTER(_i64)], _int),
     "gla_plan_adjoint": ([_vp, _vp, _vp, _vp, _vp, _vp, _d, _vp], _int),
+    "gla_plan_adjoint_host": ([_vp, _vp, _vp, _vp, _vp, _vp, _d, _vp], _int),
     "gla_dsyev": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
     "gla_ssyev": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
     "gla_dstev": ([_ch, _i64, _vp, _vp, _vp, _i64, _int, C.POINTER(_int), _vp], _int),

@@ -143,4 +143,47 @@ end
 eigvals!(S::SymTridiagonal{Float64}; tol = eps(Float64), sortby = LinearAlgebra.eigsortby) =
     eigvals_batched([Matrix(S)])[1]
 
+# Non-mutating forms.
+eigen(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; kw...) where {T<:Union{Float32,Float64}} =
+    eigen!(copy(A); kw...)
+eigen(S::SymTridiagonal{Float64}; kw...) = eigen!(copy(S); kw...)
+
+# eigen2 (:633-668): ascending eigenvalues and rows 1 and n of the eigenvector
+# matrix (2 x n). The reference accumulates only those two rows of the
+# rotations; the device path forms the whole matrix and keeps two rows, so
+# eigen2(A).vectors == eigen(A).vectors[[1, n], :] exactly, as
+# test/eigenselfadjoint.jl:18-24 checks.
+function eigen2(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; tol = eps(T)) where {T<:Union{Float32,Float64}}
+    E = eigen!(copy(A); tol)
+    n = size(E.vectors, 1)
+    return LinearAlgebra.Eigen(E.values, E.vectors[[1, n], :])
+end
+function eigen2(S::SymTridiagonal{Float64}; tol = eps(Float64))
+    E = eigen!(copy(S))
+    n = size(E.vectors, 1)
+    return LinearAlgebra.Eigen(E.values, E.vectors[[1, n], :])
+end
+
+"""
+    eigen_adjoint(E, wbar, Vbar; gap_rel = 0.0) -> Abar
+
+Reverse-mode adjoint of `E = eigen(A)` for a real symmetric `A` of order
+n <= $(GLA_MAX_SMALL_N) (gla_plan_adjoint_host): the full symmetric cotangent
+`V (diag(wbar) + sym(F .* (V'Vbar))) V'` with `F_ij = 1/(w_j - w_i)` above
+the gap threshold. `nothing` stands for a zero cotangent.
+"""
+function eigen_adjoint(E::LinearAlgebra.Eigen, wbar, Vbar; gap_rel = 0.0)
+    n = length(E.values)
+    p = Plan(Int64[n]; jobz = 'V')
+    w = Vector{Float64}(E.values)
+    V = vec(Matrix{Float64}(E.vectors))
+    wb = wbar === nothing ? zeros(Float64, n) : Vector{Float64}(wbar)
+    Vb = Vbar === nothing ? zeros(Float64, n * n) : vec(Matrix{Float64}(Vbar))
+    Abar = Vector{Float64}(undef, max(n * n, 1))
+    check(ccall((:gla_plan_adjoint_host, libglagpu), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cdouble, Ptr{Cvoid}),
+                p.handle, w, V, wb, Vb, Abar, Float64(gap_rel), C_NULL))
+    return reshape(Abar[1:n*n], n, n)
+end
+
 end # module

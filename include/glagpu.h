@@ -141,6 +141,10 @@ int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, voi
  */
 int gla_plan_adjoint(gla_plan_t plan, const double* w, const double* V, const double* wbar, const double* Vbar,
                      double* Abar, double gap_rel, void* stream);
+/* Same, from and to HOST buffers (the library stages them on the device;
+ * synchronizes `stream`). For host-language glue without device arrays. */
+int gla_plan_adjoint_host(gla_plan_t plan, const double* w, const double* V, const double* wbar, const double* Vbar,
+                          double* Abar, double gap_rel, void* stream);
 
 /*
  * Statistics of the last execute: total Givens rotations applied to the
@@ -213,9 +217,11 @@ int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* 
 
 /*
  * eigen!/eigvals! of SymTridiagonal(d, e) (src/eigenSelfAdjoint.jl:581,
- * :602-612, :623): d (n), e (n-1) device arrays, overwritten; on return d
- * holds the ascending eigenvalues and Z (n x n, ldz) the eigenvectors
- * (jobz 'V'). flags selects QL (default) or QR. Synchronizes.
+ * :602-612, :623): d (n), e (n-1) device arrays; on return d holds the
+ * ascending eigenvalues (e may be overwritten) and Z (n x n, ldz) the
+ * eigenvectors (jobz 'V'). Orders up to GLA_MAX_SMALL_N run the QL (default)
+ * or QR chase selected by flags; larger orders (up to GLA_MAX_N) the divide
+ * and conquer of the large-matrix path (flags ignored). Synchronizes.
  */
 int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz, int flags, int* info,
               void* stream);

@@ -1,0 +1,148 @@
+"""eigen2 (src/eigenSelfAdjoint.jl:633-668, tested at
+test/eigenselfadjoint.jl:18-24 and :45-51), the host-buffer adjoint entry and
+the tridiagonal entry gla_dstev at orders above the batched bound (the
+divide-and-conquer path), against the CPU oracle.
+Tolerances: eigen2 rows are bit-identical to eigen's rows; eigenvalues within
+8 n eps64 ||T|| of the oracle's, residual and ||V'V - I|| <= 1e-13."""
+import numpy as np
+import pytest
+
+from helpers import goe, golden, orth, residual, sym_from
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+EPS64 = 2.0 ** -52
+
+
+@pytest.fixture(scope="module")
+def G():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import glagpu
+    return glagpu
+
+
+def tridiag_dense(d, e):
+    return np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+
+
+def test_eigen2_symtridiagonal_rows_equal(G):
+    # test/eigenselfadjoint.jl:18-24: vecs[[1, n], :] == vecs2, vecs2 vecs2' ~ I
+    g = golden()["symtridiagonal"]
+    dv = np.array([float.fromhex(v) for v in g["dv"]])
+    ev = np.array([float.fromhex(v) for v in g["ev"]])
+    n = len(dv)
+    r = G.eigen(G.SymTridiagonal(dv, ev))
+    r2 = G.eigen2(G.SymTridiagonal(dv, ev))
+    assert np.all(np.diff(r2.values) >= 0)
+    assert np.array_equal(r.values, r2.values)
+    assert r2.vectors.shape == (2, n)
+    assert np.array_equal(r.vectors[[0, n - 1]], r2.vectors)
+    assert np.abs(r2.vectors @ r2.vectors.T - np.eye(2)).max() < 1e-13
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_eigen2_symmetric_rows_equal(G, uplo):
+    # test/eigenselfadjoint.jl:45-51 on a full symmetric matrix
+    for n in (1, 2, 7, 50, 128, 200):
+        A = goe(n, 700 + n)
+        r = G.eigen(A, uplo=uplo)
+        r2 = G.eigen2(A, uplo=uplo)
+        assert r2.vectors.shape == (2, n)
+        assert np.array_equal(r.values, r2.values)
+        assert np.array_equal(r.vectors[[0, n - 1]], r2.vectors)
+        if n > 1:
+            assert np.abs(r2.vectors @ r2.vectors.T - np.eye(2)).max() < 1e-13
+        wo, _, _ = O.syev(sym_from(A, uplo), jobz="N")
+        assert np.abs(r2.values - wo).max() <= 8 * n * EPS64 * max(np.linalg.norm(A, 2), 1.0)
+
+
+def test_eigen2_device_tensor(G):
+    import torch
+    A = goe(60, 11)
+    At = torch.tensor(A, device="cuda")
+    r = G.eigen(At)
+    r2 = G.eigen2(At)
+    assert r2.vectors.shape == (2, 60) and r2.vectors.is_cuda
+    assert torch.equal(r.vectors[[0, 59]], r2.vectors)
+
+
+def test_adjoint_host_matches_device(G):
+    import torch
+    rng = np.random.default_rng(5)
+    mats = [goe(int(n), 900 + i) for i, n in enumerate(rng.integers(8, 97, size=9))]
+    plan = G.Plan([m.shape[0] for m in mats])
+    A = plan.pack(mats, device="cuda")
+    w = torch.empty(plan.w_elems, dtype=torch.float64, device="cuda")
+    V = torch.empty(plan.a_elems, dtype=torch.float64, device="cuda")
+    info = torch.zeros(len(mats), dtype=torch.int32, device="cuda")
+    plan.execute(A, w, V, info)
+    wbar = torch.tensor(rng.standard_normal(plan.w_elems), device="cuda")
+    Vbar = torch.tensor(rng.standard_normal(plan.a_elems), device="cuda")
+    Abar = torch.empty_like(V)
+    plan.adjoint(w, V, wbar, Vbar, Abar)
+    torch.cuda.synchronize()
+    Ah = np.empty(plan.a_elems)
+    plan.adjoint_host(w.cpu().numpy(), V.cpu().numpy(), wbar.cpu().numpy(), Vbar.cpu().numpy(), Ah)
+    assert np.array_equal(Ah, Abar.cpu().numpy())
+
+
+def test_adjoint_host_rejects_large_plan(G):
+    plan = G.Plan([300])
+    z = np.zeros(plan.a_elems)
+    with pytest.raises(G.GLAError):
+        plan.adjoint_host(np.zeros(plan.w_elems), z, np.zeros(plan.w_elems), z, np.empty(plan.a_elems))
+
+
+def wilkinson_plus(n):
+    m = (n - 1) / 2.0
+    return np.abs(np.arange(n) - m), np.ones(n - 1)
+
+
+@pytest.mark.parametrize("case", ["random", "wilkinson", "graded", "split"])
+def test_large_symtridiagonal_dc(G, case):
+    # orders above the batched bound go through gla_dstev's divide and conquer
+    rng = np.random.default_rng(17)
+    if case == "random":
+        n = 300
+        d, e = rng.standard_normal(n), rng.standard_normal(n - 1)
+    elif case == "wilkinson":  # W+_n: pairs of eigenvalues agreeing to many digits
+        n = 401
+        d, e = wilkinson_plus(n)
+    elif case == "graded":
+        n = 520
+        d = 10.0 ** np.linspace(0, -12, n)
+        e = 0.5 * np.sqrt(d[:-1] * d[1:])
+    else:  # exact zeros on the off-diagonal split the matrix into blocks
+        n = 700
+        d, e = rng.standard_normal(n), rng.standard_normal(n - 1)
+        e[rng.choice(n - 1, 25, replace=False)] = 0.0
+    T = tridiag_dense(d, e)
+    nT = np.linalg.norm(T, 2)
+    # the oracle's QL-with-vectors values: its root-free PWK variant (jobz 'N',
+    # src/eigenSelfAdjoint.jl:163-219) loses ~4e-9 on W+_401's near-integer pairs
+    wo, _, _ = O.stev(d, e, "V")
+    r = G.eigen(G.SymTridiagonal(d, e))
+    assert np.all(np.diff(r.values) >= 0)
+    assert np.abs(r.values - wo).max() <= 8 * n * EPS64 * nT
+    assert residual(T, r.vectors, r.values) <= 1e-13
+    assert orth(r.vectors) <= 1e-13
+    w = G.eigvals(G.SymTridiagonal(d, e))
+    assert np.abs(w - wo).max() <= 8 * n * EPS64 * nT
+    r2 = G.eigen2(G.SymTridiagonal(d, e))
+    assert np.array_equal(r2.vectors, r.vectors[[0, n - 1]])
+
+
+def test_large_symtridiagonal_device_inputs(G):
+    import torch
+    n = 1000
+    rng = np.random.default_rng(23)
+    d, e = rng.standard_normal(n), rng.standard_normal(n - 1)
+    r = G.eigen(G.SymTridiagonal(torch.tensor(d, device="cuda"), torch.tensor(e, device="cuda")))
+    assert r.values.is_cuda and r.vectors.shape == (n, n)
+    T = tridiag_dense(d, e)
+    wo, _, _ = O.stev(d, e, "V")
+    assert np.abs(r.values.cpu().numpy() - wo).max() <= 8 * n * EPS64 * np.linalg.norm(T, 2)
+    assert residual(T, r.vectors.cpu().numpy(), r.values.cpu().numpy()) <= 1e-13
