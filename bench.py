@@ -320,6 +320,8 @@ def run_ours(args):
     peak = measured_dgemm_tflops(torch) if rank == 0 else None
     large = run_large(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
     c4 = run_c4(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
+    c1 = run_c1(torch, glagpu, dev) if rank == 0 else None
+    c5 = run_c5(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
 
     if rank == 0:
         def meets(r):
@@ -380,6 +382,8 @@ def run_ours(args):
             "speedup_f32refined_vs_f64": graph_res["f32_refined"]["eigh_per_s"] / graph_res["f64"]["eigh_per_s"],
             "large": large,
             "c4_forward_adjoint": c4,
+            "c1_single_n64": c1,
+            "c5_mixed_forward_adjoint": c5,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -426,6 +430,130 @@ def run_c4(torch, glagpu, dev, reps=3):
         out[path] = {"matrices_per_s": len(ns) / (ms * 1e-3), "ms_per_step": ms,
                      "adjoint_ms": e0.elapsed_time(e1) / reps, "info_nonzero": int((info.cpu() != 0).sum())}
         plan.close()
+    return out
+
+
+def run_c1(torch, glagpu, dev, reps=200):
+    """Single matrix: eigen!(Hermitian(A)) FP64, n = 64 GOE (seed 1), through
+    gla_dsyev (device pointers; it synchronizes to return info). Latency per
+    solve on the GPU beside one host core running the oracle port."""
+    import ctypes
+    import glagpu._lib as L
+    from helpers import goe, orth, residual
+    from oracle import oracle as O
+    lib = L.load()
+    n = 64
+    A0 = goe(n, 1)
+    Ad = torch.tensor(A0.ravel(order="F"), device=dev)
+    A = torch.empty_like(Ad)
+    w = torch.empty(n, dtype=torch.float64, device=dev)
+    info = ctypes.c_int(0)
+    call = lambda: L.check(lib.gla_dsyev(b"V", b"L", n, ctypes.c_void_p(A.data_ptr()), n, ctypes.c_void_p(w.data_ptr()),
+                                         ctypes.byref(info), None), "gla_dsyev")
+    for _ in range(5):
+        A.copy_(Ad)
+        call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        A.copy_(Ad)
+        call()
+    torch.cuda.synchronize()
+    gpu_us = (time.perf_counter() - t0) / reps * 1e6
+    V = A.cpu().numpy().reshape(n, n).T
+    wh = w.cpu().numpy()
+    wo, _, _ = O.syev(A0)
+    t0 = time.perf_counter()
+    k = 0
+    while time.perf_counter() - t0 < 1.0:
+        O.syev(A0)
+        k += 1
+    cpu_us = (time.perf_counter() - t0) / k * 1e6
+    return {"n": n, "gpu_us_per_solve": gpu_us, "cpu_oracle_us_per_solve_1core": cpu_us,
+            "timing": "host wall clock per gla_dsyev call (copy-in of A, solve, info read), mean of %d" % reps,
+            "accuracy": {"residual": residual(A0, V, wh), "orthogonality": orth(V),
+                         "eig_err_vs_oracle": float(np.abs(wh - wo).max())}, "info": int(info.value)}
+
+
+def c5_workload():
+    """Mixed workload: 256 symmetric matrices, n log-uniform in [16, 1024]
+    (seed 5); even indices GOE, odd indices Q diag(lam) Q' with Q Haar and
+    lam = +-logspace(-8, 0, n) with random signs (cond 1e8)."""
+    from helpers import goe, prescribed
+    rng = np.random.default_rng(5)
+    ns = np.exp(rng.uniform(np.log(16), np.log(1024), size=256)).round().astype(np.int64)
+    mats, lams = [], []
+    for i, n in enumerate(ns):
+        n = int(n)
+        if i % 2 == 0:
+            mats.append(goe(n, 5000 + i))
+            lams.append(None)
+        else:
+            lam = np.logspace(-8, 0, n) * rng.choice([-1.0, 1.0], n)
+            mats.append(prescribed(lam, 5000 + i))
+            lams.append(np.sort(lam))
+    return ns, mats, lams
+
+
+def run_c5(torch, glagpu, dev, reps=2):
+    """Mixed workload (c5_workload): one step = forward eigen-decomposition of
+    all 256 matrices (one plan: orders <= 128 batched, larger ones by the
+    blocked path) + adjoint with cotangents ~ N(0, 1). Matrices per second for
+    FP64 and FP32 + refinement, accuracy over every matrix, and the HBM
+    footprint of the step (device memory taken by the arenas and the plan's
+    workspace, from cudaMemGetInfo). The step is not graph-captured: the
+    blocked path reads convergence and cluster decisions on the host."""
+    from helpers import orth, residual
+    ns, mats, lams = c5_workload()
+    out = {"workload": "256 symmetric matrices, n log-uniform [16, 1024] (seed 5), half GOE, half prescribed "
+                       "spectrum +-logspace(-8, 0) (cond 1e8); forward + adjoint",
+           "sum_n3": float((ns.astype(np.float64) ** 3).sum()), "orders_above_128": int((ns > 128).sum())}
+    for path in ("f64", "f32_refined"):
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        free0 = torch.cuda.mem_get_info()[0]
+        plan = glagpu.Plan(ns, precision=path)
+        A = plan.pack(mats, device=dev)
+        w = torch.empty(plan.w_elems, dtype=torch.float64, device=dev)
+        V = torch.empty(plan.a_elems, dtype=torch.float64, device=dev)
+        info = torch.zeros(len(ns), dtype=torch.int32, device=dev)
+        g = torch.Generator(device="cpu").manual_seed(55)
+        wbar = torch.randn(plan.w_elems, generator=g, dtype=torch.float64).to(dev)
+        Vbar = torch.randn(plan.a_elems, generator=g, dtype=torch.float64).to(dev)
+        Abar = torch.empty_like(V)
+        plan.execute(A, w, V, info)
+        plan.adjoint(w, V, wbar, Vbar, Abar)
+        torch.cuda.synchronize()
+        footprint = free0 - torch.cuda.mem_get_info()[0]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            plan.execute(A, w, V, info)
+            plan.adjoint(w, V, wbar, Vbar, Abar)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        e0.record()
+        plan.adjoint(w, V, wbar, Vbar, Abar)
+        e1.record()
+        e1.synchronize()
+        adj_ms = e0.elapsed_time(e1)
+        ws_, Vs_ = plan.unpack(w.cpu().numpy(), V.cpu().numpy())
+        res = ort = eig = 0.0
+        for Am, wg, Vg, lam in zip(mats, ws_, Vs_, lams):
+            nA = max(np.linalg.norm(Am, 2), 1e-300)
+            res = max(res, residual(Am, Vg, wg))
+            ort = max(ort, orth(Vg))
+            if lam is not None:
+                eig = max(eig, float(np.abs(wg - lam).max()) / nA)
+        out[path] = {"matrices_per_s": len(ns) / (ms * 1e-3), "ms_per_step": ms, "adjoint_ms": adj_ms,
+                     "hbm_footprint_bytes": int(footprint), "info_nonzero": int((info.cpu() != 0).sum()),
+                     "accuracy": {"max_residual": res, "max_orthogonality": ort,
+                                  "max_eig_err_vs_prescribed": eig}}
+        plan.close()
+        del A, w, V, info, wbar, Vbar, Abar
+    out["speedup_f32refined_vs_f64"] = out["f64"]["ms_per_step"] / out["f32_refined"]["ms_per_step"]
     return out
 
 

@@ -118,6 +118,7 @@ struct gla_plan_s {
   int* pin_pending = nullptr;
   df64* d_adj = nullptr;  // adjoint workspace (allocated by the first gla_plan_adjoint)
   double* h_adj = nullptr;  // device staging of gla_plan_adjoint_host
+  double* d_adj_large = nullptr;  // adjoint workspace of the orders above GLA_MAX_SMALL_N
   // orders above GLA_MAX_SMALL_N: solved one at a time by the large path
   std::vector<int> large_idx;           // batch indices, in batch order
   std::map<int, LargeCtx*> large_ctx;   // one context per distinct order
@@ -369,6 +370,7 @@ int gla_plan_destroy(gla_plan_t p) {
   cudaFreeHost(p->pin_pending);
   cudaFree(p->d_adj);
   cudaFree(p->h_adj);
+  cudaFree(p->d_adj_large);
   for (auto& kv : p->large_ctx) large_destroy(kv.second);
   for (auto& kv : p->large_ref) refine_large_destroy(kv.second);
   cudaFreeHost(p->h_large_info);
@@ -659,12 +661,28 @@ int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const doubl
   if (!Vbar && p->a_elems) return -5;
   if (!Abar && p->a_elems) return -6;
   if (!(gap_rel == gap_rel)) return -7;
-  if (!p->large_idx.empty()) return GLA_ERR_UNSUPPORTED;  // one-CTA adjoint: orders <= GLA_MAX_SMALL_N
-  if (p->nwork == 0) return 0;
-  if (!p->d_adj) GLA_CUDA(cudaMalloc((void**)&p->d_adj, adjoint_workspace_bytes(p->a_elems)));
+  const double gr = gap_rel > 0 ? gap_rel : 1e-10;
   cudaStream_t st = (cudaStream_t)stream;
-  GLA_CUDA(launch_adjoint(p->nwork, st, p->d_desc, p->d_perm_bucket, w, V, wbar, Vbar, Abar, p->d_adj, p->a_elems,
-                          gap_rel > 0 ? gap_rel : 1e-10));
+  if (p->nwork > 0) {  // orders <= GLA_MAX_SMALL_N: one CTA per matrix
+    if (!p->d_adj) GLA_CUDA(cudaMalloc((void**)&p->d_adj, adjoint_workspace_bytes(p->a_elems)));
+    GLA_CUDA(launch_adjoint(p->nwork, st, p->d_desc, p->d_perm_bucket, w, V, wbar, Vbar, Abar, p->d_adj, p->a_elems,
+                            gr));
+  }
+  if (!p->large_idx.empty()) {  // larger orders: three FP64 GEMMs each, one shared workspace
+    int nl = 0;
+    for (int b : p->large_idx) nl = std::max(nl, (int)p->n[b]);
+    if (!p->d_adj_large) GLA_CUDA(cudaMalloc((void**)&p->d_adj_large, sizeof(double) * large_adjoint_workspace_elems(nl)));
+    for (int b : p->large_idx) {
+      const int nb = (int)p->n[b];
+      int64_t aoff = 0, woff = 0;
+      for (int q = 0; q < b; q++) {
+        aoff += p->n[q] * p->n[q];
+        woff += p->n[q];
+      }
+      GLA_CUDA(large_adjoint(nb, w + woff, V + aoff, nb, wbar + woff, Vbar + aoff, nb, Abar + aoff, nb, gr,
+                             p->d_adj_large, st));
+    }
+  }
   return 0;
 }
 
@@ -678,8 +696,7 @@ int gla_plan_adjoint_host(gla_plan_t p, const double* w, const double* V, const 
   if (!Vbar && p->a_elems) return -5;
   if (!Abar && p->a_elems) return -6;
   if (!(gap_rel == gap_rel)) return -7;
-  if (!p->large_idx.empty()) return GLA_ERR_UNSUPPORTED;
-  if (p->nwork == 0) return 0;
+  if (p->a_elems == 0) return 0;
   cudaStream_t st = (cudaStream_t)stream;
   const size_t ab = sizeof(double) * p->a_elems, wb = sizeof(double) * p->w_elems;
   if (!p->h_adj) GLA_CUDA(cudaMalloc((void**)&p->h_adj, 3 * ab + 2 * wb));

@@ -64,6 +64,14 @@ cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long
                           cudaStream_t st);
 bool oz_fits(const OzWork* w, int m, int n, int K);
 
+// ---- adjoint of one large eigen-decomposition (large_adjoint.cu):
+// Abar = V (diag(wbar) + sym(F o (V' Vbar))) V', FP64; ws holds
+// large_adjoint_workspace_elems(n) doubles.
+size_t large_adjoint_workspace_elems(int n);
+cudaError_t large_adjoint(int n, const double* w, const double* V, long long ldv, const double* wbar,
+                          const double* Vbar, long long ldvb, double* Abar, long long lda, double gap_rel,
+                          double* ws, cudaStream_t st);
+
 // ---- stage plans (one order, one working precision)
 struct SytrdPlan;
 cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64);

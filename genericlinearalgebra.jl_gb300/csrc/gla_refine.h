@@ -30,6 +30,6 @@ void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t w_elems, 
 cudaError_t refine_kernels_init();
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
-                          const int* info, const int* scale_exp, unsigned long long* stats);
+                          int* info, const int* scale_exp, unsigned long long* stats);
 
 }  // namespace gla

@@ -65,7 +65,8 @@ struct RefineLarge {
   double* gdiag = nullptr;
   int* couple = nullptr;   // per consecutive pair: joined into one cluster
   int* cid = nullptr;      // per column: cluster id (or -1)
-  float* scal = nullptr;   // [0] max |E| outside clusters, [2] max column norm of Rres (float bits)
+  float* scal = nullptr;   // [0] max |E| outside clusters, [1] orthogonality defect entering the
+                           // polish, [2] max column norm of Rres (float bits)
   float* offmax = nullptr; // per cluster: max |off-diagonal| of C_J
   float* rn = nullptr;     // per column: residual norm
   unsigned long long* amax = nullptr;
@@ -79,6 +80,7 @@ struct RefineLarge {
   int iters = 0;
   int rotated = 0;  // cluster rotations of the last run
   int reorders = 0;
+  int ortho_steps = 0;  // extra orthogonalisation steps after the polish
 };
 
 namespace {
@@ -224,15 +226,17 @@ __device__ __forceinline__ void atomic_max_pos(float* a, float v) {
 // E + E' = R holds whatever the rounding of T.
 __global__ void k_ref_e(const float* __restrict__ T, const float* __restrict__ Ghi, const float* __restrict__ Glo,
                         const double* __restrict__ lam, const double* __restrict__ gdiag,
-                        const int* __restrict__ cid, int n, int polish, float* __restrict__ E, float* scal) {
+                        const int* __restrict__ cid, int n, int polish, double tfloor, float* __restrict__ E,
+                        float* scal) {
   const int j = blockIdx.y;
-  float em = 0.f;
+  float em = 0.f, od = 0.f;
   const double lj = lam[j];
   const int cj = cid[j];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const long long idx = i + (long long)j * n;
     const long long g = i > j ? idx : j + (long long)i * n;  // lower triangle of the Gram matrix
     float e;
+    if (polish) od = fmaxf(od, i == j ? (float)fabs(1.0 - gdiag[j]) : fabsf(Ghi[g]));
     if (i == j) {
       e = (float)(0.5 * (1.0 - gdiag[j]));
     } else if (cj >= 0 && cid[i] == cj) {
@@ -240,18 +244,47 @@ __global__ void k_ref_e(const float* __restrict__ T, const float* __restrict__ G
     } else {
       const double gap = lj - lam[i];
       float sep;
-      if (polish)
-        sep = (float)(0.5 * ((double)T[idx] + (double)T[j + (long long)i * n]) / gap);
-      else
+      if (polish) {
+        // polishing iteration: a pair at a tight gap whose coupling is at
+        // the rounding floor of T is not rotated: the rotation would be
+        // noise of size u ||A|| / gap (its square shows in the
+        // orthogonality) and leaving it changes the residual by less than
+        // tfloor; rotations below 1e-8 cost nothing in orthogonality and are
+        // kept (they carry the residual's last bits)
+        const double t = 0.5 * ((double)T[idx] + (double)T[j + (long long)i * n]);
+        const double rot = t / gap;
+        sep = (fabs(t) <= tfloor && fabs(rot) > 1e-8) ? 0.f : (float)rot;
+      } else {
         sep = (float)((double)T[idx] / gap);
+      }
       em = fmaxf(em, fabsf(sep));
       e = polish ? sep - 0.5f * (Ghi[g] + Glo[g]) : sep;
     }
     E[idx] = e;
   }
 #pragma unroll
-  for (int s = 16; s > 0; s >>= 1) em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, s));
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(scal, em);
+  for (int s = 16; s > 0; s >>= 1) {
+    em = fmaxf(em, __shfl_xor_sync(0xffffffffu, em, s));
+    od = fmaxf(od, __shfl_xor_sync(0xffffffffu, od, s));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_pos(scal, em);
+    if (polish) atomic_max_pos(scal + 1, od);
+  }
+}
+
+// Symmetric orthogonalisation step X <- X (I + R/2), R = I - X'X (one
+// Newton-Schulz step towards the orthonormal polar factor): E from the
+// lower triangle of the Gram matrix.
+__global__ void k_ref_ortho_e(const float* __restrict__ Ghi, const float* __restrict__ Glo, int n,
+                              float* __restrict__ E) {
+  const int j = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const long long idx = i + (long long)j * n;
+    const long long g = i >= j ? idx : j + (long long)i * n;
+    const double gv = (double)Ghi[g] + (double)Glo[g];
+    E[idx] = (float)(i == j ? 0.5 * (1.0 - gv) : -0.5 * gv);
+  }
 }
 
 // X <- X + XE in double-float.
@@ -260,6 +293,17 @@ __global__ void k_ref_update(float* __restrict__ Xhi, float* __restrict__ Xlo, c
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
        i += (long long)gridDim.x * blockDim.x) {
     const df64 x = df_add(df_make(Xhi[i], Xlo[i]), df_make(XE[i], 0.f));
+    Xhi[i] = x.hi;
+    Xlo[i] = x.lo;
+  }
+}
+
+// X <- X + (XE as a float pair) in double-float.
+__global__ void k_ref_update_df(float* __restrict__ Xhi, float* __restrict__ Xlo, const float* __restrict__ Phi,
+                                const float* __restrict__ Plo, long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const df64 x = df_add(df_make(Xhi[i], Xlo[i]), df_make(Phi[i], Plo[i]));
     Xhi[i] = x.hi;
     Xlo[i] = x.lo;
   }
@@ -470,6 +514,7 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
   r->iters = 0;
   r->rotated = 0;
   r->reorders = 0;
+  r->ortho_steps = 0;
   if (hflags[0] == 0) {
     bool polish = false;
     double emax_prev = 1e300;
@@ -533,23 +578,35 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
         RF_CUDA(cudaMemsetAsync(oz_error_word(r->ozx), 0, sizeof(int), st));
         RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Ghi, r->Glo, n, true, st));
       }
-      k_ref_e<<<g2, 256, 0, st>>>(r->T, r->Ghi, r->Glo, r->lam, r->gdiag, r->cid, n, polish ? 1 : 0, r->E, r->scal);
+      k_ref_e<<<g2, 256, 0, st>>>(r->T, r->Ghi, r->Glo, r->lam, r->gdiag, r->cid, n, polish ? 1 : 0, 1e-14 * lmax,
+                                  r->E, r->scal);
       RF_CUDA(cudaGetLastError());
-      // X <- X + X E
-      GemmDesc u{};
-      u.m = n;
-      u.n = n;
-      u.k = n;
-      u.A = r->Xhi;
-      u.lda = n;
-      u.B = r->E;
-      u.ldb = n;
-      u.C = r->XE;
-      u.ldc = n;
-      u.alpha = 1.0;
-      u.beta = 0.0;
-      RF_CUDA(gemm_launch(false, false, false, false, u, 1, st));
-      k_ref_update<<<2048, 256, 0, st>>>(r->Xhi, r->Xlo, r->XE, nn);
+      // X <- X + X E: FP32 product of X_hi and E while E is a correction
+      // that the next iteration refines (its rounding, 2^-24 |X E|, is a
+      // perturbation removed quadratically); the polishing iteration, the
+      // last, forms X E in double-float on the tensor cores (A operand: the
+      // rows of X; B operand: E, in the slot of X's slices, unused from here)
+      if (polish) {
+        RF_CUDA(oz_slice_rows(r->ozx, r->Xhi, r->Xlo, n, n, n, 7, st));
+        RF_CUDA(oz_slice(r->oz, false, r->E, nullptr, n, n, n, 7, st));
+        RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Phi, r->Plo, n, false, st));
+        k_ref_update_df<<<2048, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, nn);
+      } else {
+        GemmDesc u{};
+        u.m = n;
+        u.n = n;
+        u.k = n;
+        u.A = r->Xhi;
+        u.lda = n;
+        u.B = r->E;
+        u.ldb = n;
+        u.C = r->XE;
+        u.ldc = n;
+        u.alpha = 1.0;
+        u.beta = 0.0;
+        RF_CUDA(gemm_launch(false, false, false, false, u, 1, st));
+        k_ref_update<<<2048, 256, 0, st>>>(r->Xhi, r->Xlo, r->XE, nn);
+      }
       RF_CUDA(cudaGetLastError());
       // Rayleigh-Ritz inside the clusters whose projected matrix is still
       // coupled (a resolved cluster only gets the Gram correction above: an
@@ -611,7 +668,33 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
         }
       }
       r->rotated += (int)rs.size();
-      if (polish) break;
+      if (polish) {
+        // the polish corrects the orthogonality defect d it started from to
+        // first order, leaving ~3/4 d^2: above d = 3e-8 (tight clusters
+        // rotated by FP32 Rayleigh-Ritz solutions shortly before) one more
+        // symmetric step X <- X (I + R/2) squares it again; both products on
+        // the tensor cores in double-float. The residual moves by
+        // (lam_j - lam_i) r_ij / 2, negligible where the defect sits (pairs
+        // at tight gaps).
+        if (hs[1] > 3e-8f) {
+          RF_CUDA(oz_slice(r->ozx, true, r->Xhi, r->Xlo, n, n, n, 7, st));
+          RF_CUDA(oz_slice(r->oz, false, r->Xhi, r->Xlo, n, n, n, 7, st));
+          RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Ghi, r->Glo, n, true, st));
+          k_ref_ortho_e<<<g2, 256, 0, st>>>(r->Ghi, r->Glo, n, r->E);
+          RF_CUDA(cudaGetLastError());
+          RF_CUDA(oz_slice_rows(r->ozx, r->Xhi, r->Xlo, n, n, n, 7, st));
+          RF_CUDA(oz_slice(r->oz, false, r->E, nullptr, n, n, n, 7, st));
+          RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Phi, r->Plo, n, false, st));
+          k_ref_update_df<<<2048, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, nn);
+          RF_CUDA(cudaGetLastError());
+          int ozx_err = 0;
+          RF_CUDA(cudaMemcpyAsync(&ozx_err, oz_error_word(r->ozx), sizeof(int), cudaMemcpyDeviceToHost, st));
+          RF_CUDA(cudaStreamSynchronize(st));
+          if (ozx_err) return -1000 - (int)cudaErrorLaunchTimeout;
+          r->ortho_steps++;
+        }
+        break;
+      }
       // the eigenvectors have (nearly) converged: nothing rotated, and the
       // corrections are below 1e-7 (the polishing iteration, quadratically
       // convergent, leaves ~emax^2 ||A|| in the residual) or have stopped

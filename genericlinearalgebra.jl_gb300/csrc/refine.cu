@@ -125,7 +125,7 @@ GLA_DEV void jacobi_warp(int k, float* C, float* Z) {
 __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                 const double* __restrict__ A, int lower,
                                                 const float* __restrict__ X32, double* __restrict__ Vout,
-                                                double* __restrict__ wout, const int* __restrict__ info,
+                                                double* __restrict__ wout, int* __restrict__ info,
                                                 const int* __restrict__ scale_exp, RefineWork rw,
                                                 unsigned long long* __restrict__ stats) {
   __shared__ df64 As[16 * kTP];
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   __shared__ df64 lamdf[kSmallMaxN];
   __shared__ float red[kRT / 32];
   __shared__ unsigned long long keys[kSmallMaxN];
-  __shared__ int rank[kSmallMaxN], ord[kSmallMaxN], cstart[kSmallMaxN + 1];
+  __shared__ int rank[kSmallMaxN], ord[kSmallMaxN], cstart[kSmallMaxN + 1], cid[kSmallMaxN];
   __shared__ int ncl_s, flag_s, big_s;
   __shared__ double gmin_s, lmax_s;
   float* Bsf = reinterpret_cast<float*>(Bs2);
@@ -176,6 +176,8 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   auto zinit = [&](int, int) { return zero; };
   df64* cS = S0;
   df64* cR = R0;
+  bool converged = false;
+  float emax_prev = 1e30f;
   for (int it = 0; it < kMaxRefineIters; it++) {
     if (it == 0) {
       // ---- first iteration on the FP32 eigenvectors X0 (exact floats)
@@ -245,21 +247,6 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     const float sdn = sqrtf(block_sum_f(sd2, red));
     const float rn = sqrtf(block_sum_f(r2, red));
     const float delta = 2.f * (sdn + anorm * rn);
-    float emax = 0.f;
-    for (int idx = tid; idx < n * n; idx += kRT) {
-      const int i = idx % n, j = idx / n;
-      const float gap = (float)(lam[j] - lam[i]);
-      float e;
-      if (i != j && fabsf(gap) > delta) {
-        const df64 num = df_mac(cS[idx], lamdf[j], cR[idx]);
-        e = (num.hi + num.lo) / gap;
-      } else {
-        e = 0.5f * (cR[idx].hi + cR[idx].lo);
-      }
-      E[idx] = e;
-      emax = fmaxf(emax, fabsf(e));
-    }
-    emax = block_max_f(emax, red);
     for (int i = tid; i < n; i += kRT) {
       const unsigned long long ki = keys[i];
       int rk = 0;
@@ -280,13 +267,42 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
         }
       }
       cstart[++nc] = n;
-      for (int c = 0; c < nc; c++) big |= (cstart[c + 1] - cstart[c]) >= 2;
+      for (int c = 0; c < nc; c++) {
+        big |= (cstart[c + 1] - cstart[c]) >= 2;
+        for (int r = cstart[c]; r < cstart[c + 1]; r++) cid[ord[r]] = c;
+      }
       ncl_s = nc;
       flag_s = 0;
       gmin_s = gmin;
       big_s = big;
     }
     __syncthreads();
+    // E: the Newton-type correction between clusters; inside a cluster (its
+    // end-to-end gaps may exceed delta) only the orthogonality part r/2, the
+    // Rayleigh-Ritz rotation below takes care of the rest. A pair at a tight
+    // gap whose coupling is at the rounding floor of the double-float
+    // products (|s_ij| <= 1e-14 ||A||; s is symmetric, so the pair (j, i)
+    // decides alike) is not rotated either: the rotation
+    // would be noise of size 2^-47 ||A|| / gap, whose square shows in the
+    // orthogonality, and leaving it changes the residual by less than the
+    // floor; rotations below 1e-8 cost nothing and are kept
+    const float tfloor = (float)(1e-14 * lmax_s);
+    float emax = 0.f;
+    for (int idx = tid; idx < n * n; idx += kRT) {
+      const int i = idx % n, j = idx / n;
+      const float rhalf = 0.5f * (cR[idx].hi + cR[idx].lo);
+      float e = rhalf;
+      if (cid[i] != cid[j]) {
+        const float gap = (float)(lam[j] - lam[i]);
+        const df64 num = df_mac(cS[idx], lamdf[j], cR[idx]);
+        const float rot = (num.hi + num.lo) / gap;
+        const float sij = cS[idx].hi + cS[idx].lo;
+        if (!(fabsf(sij) <= tfloor && fabsf(sij / gap) > 1e-8f)) e = rot;
+      }
+      E[idx] = e;
+      emax = fmaxf(emax, fabsf(e));
+    }
+    emax = block_max_f(emax, red);
     // ---- X <- X + X E (FP32 product, see above), then Rayleigh-Ritz inside clusters
     tile_gemm_f32(
         n, [&](int i, int k) { return it == 0 ? X0[(size_t)k * n + i] : X[(size_t)k * n + i].hi; },
@@ -352,10 +368,23 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     Y = t;
     if (tid == 0) atomicAdd(&stats[3], (unsigned long long)n * n * n);
     __syncthreads();
-    // the next correction would be about emax^2 ||A||_2 / gap (quadratic
-    // convergence): stop when that is below 1e-14 and no cluster is unresolved
-    if (flag_s == 0 && (double)emax * emax * lmax_s < 1e-14 * gmin_s) break;
+    // stop when no cluster is unresolved and either the next correction
+    // would be below 1e-14 (about emax^2 ||A||_2 / gap, quadratic
+    // convergence), or the iterate this step started from was already
+    // accurate (delta bounds its residual and orthogonality defects), or the
+    // corrections have stopped falling quadratically below 1e-6: E then
+    // holds only the rounding floor of the double-float products, about
+    // 2^-47 ||A|| / gap at the tightest gaps, and the iterate is at the
+    // accuracy floor of the scheme
+    const bool quad = (double)emax * emax * lmax_s < 1e-14 * gmin_s;
+    const bool stalled = it > 0 && emax < 1e-6f && emax > 0.25f * emax_prev;
+    emax_prev = emax;
+    if (flag_s == 0 && (quad || stalled || delta <= 1e-13f * anorm)) {
+      converged = true;
+      break;
+    }
   }
+  if (!converged && tid == 0) info[mid] = n + 1;  // not converged within kMaxRefineIters
   // sorteig!: ascending eigenvalues, columns permuted to match
   __syncthreads();
   for (int i = tid; i < n; i += kRT) {
@@ -377,7 +406,7 @@ cudaError_t refine_kernels_init() { return cudaSuccess; }
 
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
-                          const int* info, const int* scale_exp, unsigned long long* stats) {
+                          int* info, const int* scale_exp, unsigned long long* stats) {
   if (nblocks <= 0) return cudaSuccess;
   (void)nmax;
   k_refine<<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw,

@@ -18,6 +18,9 @@
  *           >0  number of off-diagonal entries still above the deflation
  *               threshold after the sweep cap (30*n chases per matrix;
  *               the reference has no cap and never returns on such input)
+ *          n+1  (GLA_PREC_F32_REFINED) the refinement did not reach its
+ *               accuracy target within its iteration cap (outputs are the
+ *               last iterate)
  *           -1  the referenced triangle held NaN or Inf (outputs are NaN)
  *           -2  (GLA_FLAG_GRAPH plans only) the chase needed more passes than
  *               the captured sequence holds (outputs are not valid)
@@ -72,7 +75,7 @@ extern "C" {
                                  GLA_MAX_SMALL_N run the blocked large-matrix path) */
 #define GLA_STATIC_MAX_N 128
 #define GLA_ERR_STATIC_TOO_LARGE (-2001)
-#define GLA_ERR_UNSUPPORTED (-2002) /* e.g. gla_plan_adjoint on a plan with orders > GLA_MAX_SMALL_N */
+#define GLA_ERR_UNSUPPORTED (-2002) /* operation not available for this plan */
 
 typedef struct gla_plan_s* gla_plan_t;
 
@@ -135,9 +138,12 @@ int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, voi
  * Output Abar (packed like A, full symmetric matrices):
  *     Abar = V (diag(wbar) + sym(F o (V' Vbar))) V',  sym(X) = (X + X')/2,
  *     F_ij = 1/(w_j - w_i) when |w_j - w_i| > gap_rel * max|w|, else 0.
- * gap_rel <= 0 selects 1e-10. Products in double-float arithmetic (~1e-14).
- * The first call allocates the adjoint workspace (32 bytes per arena
- * element); later calls allocate nothing. Asynchronous on `stream`.
+ * gap_rel <= 0 selects 1e-10. Orders <= GLA_MAX_SMALL_N: one CTA per
+ * matrix, products in double-float arithmetic (~1e-14). Larger orders: three
+ * FP64 GEMMs per matrix (V'Vbar, V S, (V S) V'). The first call allocates the
+ * adjoint workspace (32 bytes per arena element, plus 16 n^2 bytes for the
+ * largest order above GLA_MAX_SMALL_N); later calls allocate nothing.
+ * Asynchronous on `stream`.
  */
 int gla_plan_adjoint(gla_plan_t plan, const double* w, const double* V, const double* wbar, const double* Vbar,
                      double* Abar, double gap_rel, void* stream);

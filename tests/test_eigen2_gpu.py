@@ -89,11 +89,23 @@ def test_adjoint_host_matches_device(G):
     assert np.array_equal(Ah, Abar.cpu().numpy())
 
 
-def test_adjoint_host_rejects_large_plan(G):
+def test_adjoint_host_large_plan_matches_device(G):
+    import torch
+    rng = np.random.default_rng(8)
     plan = G.Plan([300])
-    z = np.zeros(plan.a_elems)
-    with pytest.raises(G.GLAError):
-        plan.adjoint_host(np.zeros(plan.w_elems), z, np.zeros(plan.w_elems), z, np.empty(plan.a_elems))
+    A = plan.pack([goe(300, 3)], device="cuda")
+    w = torch.empty(plan.w_elems, dtype=torch.float64, device="cuda")
+    V = torch.empty(plan.a_elems, dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    plan.execute(A, w, V, info)
+    wbar = torch.tensor(rng.standard_normal(plan.w_elems), device="cuda")
+    Vbar = torch.tensor(rng.standard_normal(plan.a_elems), device="cuda")
+    Abar = torch.empty_like(V)
+    plan.adjoint(w, V, wbar, Vbar, Abar)
+    torch.cuda.synchronize()
+    Ah = np.empty(plan.a_elems)
+    plan.adjoint_host(w.cpu().numpy(), V.cpu().numpy(), wbar.cpu().numpy(), Vbar.cpu().numpy(), Ah)
+    assert np.array_equal(Ah, Abar.cpu().numpy())
 
 
 def wilkinson_plus(n):

@@ -138,6 +138,31 @@ def test_f32_refined_prescribed_spectrum(G):
         assert residual(A, r.vectors, r.values) <= 1e-13
 
 
+def test_f32_refined_cond1e8_clusters(G):
+    # lam = +-logspace(-8, 0) (the mixed workload's prescribed half): a run of
+    # eigenvalues below the FP32 resolution forms one cluster whose end-to-end
+    # gap exceeds delta; the refinement must neither stall nor report success
+    # on an unconverged iterate
+    rng = np.random.default_rng(235)
+    mats, lams = [], []
+    for n in (16, 21, 33, 47, 80, 128):
+        for rep in range(3):
+            lam = np.logspace(-8, 0, n) * rng.choice([-1.0, 1.0], n)
+            mats.append(prescribed(lam, 1000 * n + rep))
+            lams.append(np.sort(lam))
+    plan = G.Plan([m.shape[0] for m in mats], precision="f32_refined")
+    w = np.empty(plan.w_elems)
+    V = np.empty(plan.a_elems)
+    info = np.zeros(len(mats), dtype=np.int32)
+    plan.execute_host(plan.pack(mats), w, V, info)
+    ws, Vs = plan.unpack(w, V)
+    assert (info == 0).all(), info
+    for A, lam, wg, Vg in zip(mats, lams, ws, Vs):
+        assert np.abs(wg - lam).max() <= 1e-13
+        assert residual(A, Vg, wg) <= 1e-13
+        assert orth(Vg) <= 1e-13
+
+
 def test_reference_known_answers(G):
     # 1x1 (:100-105), issue 52 (:108-117, exact), #139 (:164-170, exact)
     r = G.eigen(np.array([[1.0]]))

@@ -174,13 +174,30 @@ def test_large_deterministic(G, precision, n):
     assert np.array_equal(r1[0][0], r2[0][0]) and np.array_equal(r1[1][0], r2[1][0])
 
 
-def test_large_adjoint_unsupported(G):
+def test_large_adjoint_vs_analytic(G):
+    # orders above the one-CTA bound: three FP64 GEMMs; mixed with small orders
     import torch
-    plan = G.Plan([200])
-    z = torch.zeros(plan.a_elems, dtype=torch.float64, device="cuda")
-    zw = torch.zeros(plan.w_elems, dtype=torch.float64, device="cuda")
-    with pytest.raises(G.GLAError):
-        plan.adjoint(zw, z, zw, z, z)
+    from helpers import analytic_adjoint
+    rng = np.random.default_rng(41)
+    ns = [150, 40, 300]
+    mats = [goe(n, 4100 + n) for n in ns]
+    plan = G.Plan(ns)
+    A = plan.pack(mats, device="cuda")
+    w = torch.empty(plan.w_elems, dtype=torch.float64, device="cuda")
+    V = torch.empty(plan.a_elems, dtype=torch.float64, device="cuda")
+    info = torch.zeros(len(ns), dtype=torch.int32, device="cuda")
+    plan.execute(A, w, V, info)
+    wbar = torch.tensor(rng.standard_normal(plan.w_elems), device="cuda")
+    Vbar = torch.tensor(rng.standard_normal(plan.a_elems), device="cuda")
+    Abar = torch.empty_like(V)
+    plan.adjoint(w, V, wbar, Vbar, Abar)
+    ws, Vs = plan.unpack(w.cpu().numpy(), V.cpu().numpy())
+    wbs, Vbs = plan.unpack(wbar.cpu().numpy(), Vbar.cpu().numpy())
+    _, Abs = plan.unpack(w.cpu().numpy(), Abar.cpu().numpy())
+    for wg, Vg, wb, Vb, Ab in zip(ws, Vs, wbs, Vbs, Abs):
+        ref = analytic_adjoint(Vg, wg, wb, Vb)
+        assert np.linalg.norm(Ab - ref) <= 1e-12 * np.linalg.norm(ref)
+        assert np.abs(Ab - Ab.T).max() <= 1e-13 * np.abs(Ab).max()
 
 
 # ---------------------------------------------------------------- FP32 solve + refinement
@@ -207,6 +224,20 @@ def test_refined_prescribed_cond1e6_clusters(G):
     rng = np.random.default_rng(3)
     lam = np.logspace(-6, 0, n) * rng.choice([-1.0, 1.0], n)
     A = prescribed(lam, 7)
+    ws, Vs, info = solve_refined(G, [A])
+    assert info[0] == 0
+    assert np.max(np.abs(ws[0] - np.sort(lam))) <= 1e-13
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+@pytest.mark.parametrize("n", [300, 800])
+def test_refined_prescribed_cond1e8(G, n):
+    # lam = +-logspace(-8, 0): gaps down to ~1e-10 ||A||; orthogonality must
+    # survive the polishing iteration
+    rng = np.random.default_rng(n)
+    lam = np.logspace(-8, 0, n) * rng.choice([-1.0, 1.0], n)
+    A = prescribed(lam, 17 + n)
     ws, Vs, info = solve_refined(G, [A])
     assert info[0] == 0
     assert np.max(np.abs(ws[0] - np.sort(lam))) <= 1e-13
