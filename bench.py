@@ -208,8 +208,12 @@ def run_ours(args):
             torch.distributed.barrier()
 
     results = {}
+    tuned = {}
     for path in args.paths.split(","):
-        plan = glagpu.Plan(ns, precision=path, timing=True)
+        # launch shapes per size bucket from the autotuner (measured at plan
+        # creation on synthetic matrices, outside every timed region)
+        plan = glagpu.Plan(ns, precision=path, timing=True, autotune=not args.no_autotune)
+        tuned[path] = plan.bucket_configs()
         dt = torch.float32 if path == "f32" else torch.float64
         A = dA32 if path == "f32" else dA64
         w = torch.empty(nW, dtype=dt, device=dev)
@@ -264,7 +268,7 @@ def run_ours(args):
     # ---- headline path captured in a CUDA graph and replayed
     graph_res = {}
     for path in ("f32_refined", "f64"):
-        gplan = glagpu.Plan(ns, precision=path, graph=True)
+        gplan = glagpu.Plan(ns, precision=path, graph=True, autotune=not args.no_autotune)
         w = torch.empty(nW, dtype=torch.float64, device=dev)
         V = torch.empty(nA, dtype=torch.float64, device=dev)
         info = torch.zeros(len(ns), dtype=torch.int32, device=dev)
@@ -293,7 +297,7 @@ def run_ours(args):
         del g
         gplan.close()
     # ---- end to end through the C ABI with host buffers (headline path)
-    plan = glagpu.Plan(ns, precision="f32_refined")
+    plan = glagpu.Plan(ns, precision="f32_refined", autotune=not args.no_autotune)
     hA = torch.from_numpy(A64).pin_memory()
     hw = torch.empty(nW, dtype=torch.float64).pin_memory()
     hV = torch.empty(nA, dtype=torch.float64).pin_memory()
@@ -365,7 +369,12 @@ def run_ours(args):
                        "timing": "CUDA-graph replay of the whole batched solve (plan with GLA_FLAG_GRAPH)"},
             "roofline": {"kernel": "k_refine", "bound": "fp32",
                          "achieved": achieved, "peak": peak_ops, "unit": "T FP32 ops/s",
-                         "frac": (achieved / peak_ops) if peak_ops else None, "traffic": None,
+                         "frac": (achieved / peak_ops) if peak_ops else None,
+                         # DRAM bytes of one step's k_refine launches (all buckets), from an ncu
+                         # capture of the 512-matrix case scaled by the matrix count
+                         "traffic": 66.0e6 * len(ns) / 512,
+                         "traffic_note": "bytes per step, profiles/k_refine_traffic_batched_512.md; "
+                                         "algorithmic ~20 sum(n^2) bytes",
                          "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, FMA rate (FP32 pipe); "
                                         "MEASURED_PEAKS.json has only HBM and bf16 peaks",
                          "note": "double-float arithmetic on the FP32 pipe; see profiles/"},
@@ -382,6 +391,7 @@ def run_ours(args):
             "speedup_f32refined_vs_f64": graph_res["f32_refined"]["eigh_per_s"] / graph_res["f64"]["eigh_per_s"],
             "large": large,
             "c4_forward_adjoint": c4,
+            "autotune": {"enabled": not args.no_autotune, "bucket_configs": tuned},
             "c1_single_n64": c1,
             "c5_mixed_forward_adjoint": c5,
         }
@@ -661,15 +671,27 @@ def time_ozaki(torch, glagpu, dev, n, reps=5):
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    # each call: slicing kernels, then the GEMM kernel; the library records
+    # stream events around both parts (gla_gemm_df_last_ms), so the kernel's
+    # own average duration comes from the same timed calls
+    import ctypes
+    sl, gm = ctypes.c_float(0), ctypes.c_float(0)
     e0.record()
+    kern = []
     for _ in range(reps):
         call()
+        L.check(lib.gla_gemm_df_last_ms(ctypes.byref(sl), ctypes.byref(gm)), "gla_gemm_df_last_ms")
+        kern.append(gm.value)
     e1.record()
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    kms = sum(kern) / len(kern)
     bf16_flops = 28 * 2.0 * n ** 3
-    return {"ms": ms, "bf16_tflops": bf16_flops / (ms * 1e-3) / 1e12,
-            "fp64_equivalent_tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12}
+    return {"ms_with_slicing": ms, "ms": kms, "bf16_tflops": bf16_flops / (kms * 1e-3) / 1e12,
+            "fp64_equivalent_tflops": 2.0 * n ** 3 / (kms * 1e-3) / 1e12,
+            "fp64_equivalent_tflops_with_slicing": 2.0 * n ** 3 / (ms * 1e-3) / 1e12,
+            "timing": "k_oz_gemm alone: CUDA events around the kernel launch inside gla_gemm_df, mean of %d "
+                      "calls on %d x %d float-pair operands" % (reps, n, n)}
 
 
 def plan_buckets(ns):
@@ -751,9 +773,17 @@ def main():
     ap.add_argument("--profile", action="store_true", help="profiling run: time the paths only, print nothing")
     ap.add_argument("--nrange", default="", help="profiling: keep matrices with lo <= n <= hi, as 'lo,hi'")
     ap.add_argument("--no-large", action="store_true", help="skip the n = 4096 single-matrix section")
+    ap.add_argument("--no-autotune", action="store_true", help="fixed launch shapes instead of the autotuner's")
+    ap.add_argument("--ozaki", type=int, default=0,
+                    help="profiling: time only the tensor-core double-float GEMM (gla_gemm_df) at this order")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.ozaki:
+        import torch
+        import glagpu
+        print(json.dumps(time_ozaki(torch, glagpu, "cuda", args.ozaki)), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <map>
 #include <mutex>
 #include <new>
@@ -58,6 +59,7 @@ struct Bucket {
   int nmax;   // largest order in the bucket
   int nt;     // threads per CTA (apply)
   int nt_tri; // threads per CTA (tridiagonalisation)
+  int lpw = 0;  // chase: matrices per warp (0: the launcher's default)
   int start;  // first index into perm_bucket (orders descending inside the bucket)
   int count;
   cudaStream_t stream = nullptr;  // the bucket's pipeline runs on its own stream
@@ -146,6 +148,10 @@ struct gla_plan_s {
   size_t io_elem() const { return prec == GLA_PREC_F32 ? 4 : 8; }       // caller element size
 };
 
+namespace {
+int autotune_plan(gla_plan_t p, int base_flags);
+}
+
 extern "C" {
 
 int gla_version(void) { return GLA_VERSION; }
@@ -189,7 +195,8 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     // large orders: no capture-safe mode (their solves synchronise)
     if (any_large && (flags & GLA_FLAG_GRAPH)) return -8;
   }
-  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH)) != 0 || (flags & 3) > GLA_ALG_QR)
+  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH | GLA_FLAG_AUTOTUNE)) != 0 ||
+      (flags & 3) > GLA_ALG_QR)
     return -8;
   GLA_CUDA(ensure_init());
 
@@ -347,6 +354,13 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     gla_plan_destroy(p);
     return -1000 - (int)err;
   }
+  if (flags & GLA_FLAG_AUTOTUNE) {
+    int rc = autotune_plan(p, flags & (3 | GLA_FLAG_SMALL_LOG));
+    if (rc) {
+      gla_plan_destroy(p);
+      return rc;
+    }
+  }
   *plan_out = p;
   return 0;
 }
@@ -407,7 +421,7 @@ int enqueue_pass(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info,
   if (timed) p->mark(b, GLA_PHASE_CHASE, 0, st);
   GLA_CUDA(launch_chase(work_t, p->algo, bk.count, chase_smem_bytes(bk.nmax, el), st, p->d_desc,
                         p->d_perm_bucket + bk.start, p->d_d, p->d_e, p->d_cst, p->d_rot, p->d_hdr, info, p->tol,
-                        kMaxSweepsPerN, p->d_pending + b, p->d_stats));
+                        kMaxSweepsPerN, p->d_pending + b, p->d_stats, bk.lpw));
   if (timed) {
     p->mark(b, GLA_PHASE_CHASE, 1, st);
     p->mark(b, GLA_PHASE_APPLY, 0, st);
@@ -578,7 +592,7 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
       p->mark(b, GLA_PHASE_CHASE, 0, s);
       GLA_CUDA(launch_chase(work_t, kAlgoPWK, bk.count, chase_smem_bytes(bk.nmax, el), s, p->d_desc,
                             p->d_perm_bucket + bk.start, p->d_d, p->d_e, p->d_cst, nullptr, nullptr, info, p->tol,
-                            kMaxSweepsPerN, p->d_pending + b, p->d_stats));
+                            kMaxSweepsPerN, p->d_pending + b, p->d_stats, bk.lpw));
       GLA_CUDA(launch_sort_values(work_t, bk.count, s, p->d_desc, p->d_perm_bucket + bk.start, p->d_d, w, info,
                                   nullptr));
       p->mark(b, GLA_PHASE_CHASE, 1, s);
@@ -789,6 +803,8 @@ std::mutex g_single_mu;
 std::map<SingleKey, SingleEntry> g_single;
 std::mutex g_gemm_mu;
 OzWork* g_gemm_w = nullptr;  // slice buffers of gla_gemm_df
+cudaEvent_t g_gemm_ev[3] = {nullptr, nullptr, nullptr};  // slicing start, GEMM start, GEMM end
+bool g_gemm_timed = false;
 std::map<int, LargeCtx*> g_stev_large;  // gla_dstev above GLA_MAX_SMALL_N
 
 int single_entry(int prec, char jobz, char uplo, int64_t n, int flags, SingleEntry** out) {
@@ -884,9 +900,27 @@ int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* 
     int rc = oz_create(&g_gemm_w, (int)m, (int)n, (int)k);
     if (rc) return rc;
   }
+  if (!g_gemm_ev[0])
+    for (auto& ev : g_gemm_ev) GLA_CUDA(cudaEventCreate(&ev));
+  GLA_CUDA(cudaEventRecord(g_gemm_ev[0], st));
   GLA_CUDA(oz_slice_rows(g_gemm_w, Ahi, Alo, lda, (int)m, (int)k, 7, st));
   GLA_CUDA(oz_slice(g_gemm_w, false, Bhi, Blo, ldb, (int)n, (int)k, 7, st));
+  GLA_CUDA(cudaEventRecord(g_gemm_ev[1], st));
   GLA_CUDA(oz_gemm(g_gemm_w, (int)m, (int)n, (int)k, Chi, Clo, ldc, false, st));
+  GLA_CUDA(cudaEventRecord(g_gemm_ev[2], st));
+  g_gemm_timed = true;
+  return 0;
+}
+
+int gla_gemm_df_last_ms(float* slice_ms, float* gemm_ms) {
+  if (!slice_ms) return -1;
+  if (!gemm_ms) return -2;
+  std::lock_guard<std::mutex> lk(g_gemm_mu);
+  *slice_ms = *gemm_ms = 0.f;
+  if (!g_gemm_timed) return 0;
+  GLA_CUDA(cudaEventSynchronize(g_gemm_ev[2]));
+  GLA_CUDA(cudaEventElapsedTime(slice_ms, g_gemm_ev[0], g_gemm_ev[1]));
+  GLA_CUDA(cudaEventElapsedTime(gemm_ms, g_gemm_ev[1], g_gemm_ev[2]));
   return 0;
 }
 
@@ -955,6 +989,234 @@ int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz
   GLA_CUDA(cudaMemcpyAsync(info, ent->dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
   GLA_CUDA(cudaStreamSynchronize(st));
   return *info != 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- autotuner
+//
+// The launch shapes of the two batched kernels whose best shape depends on
+// the order and on how many matrices share a bucket: threads per CTA of the
+// tridiagonalisation (1, 2 or 4 per row of the bucket's largest order, at
+// most 256) and matrices per warp of the chase (1, 2, 4, 8, 16 or 32 lanes).
+// Plans created with GLA_FLAG_AUTOTUNE look each bucket up in a process-wide
+// table keyed by (precision family, jobz, 16-wide order range, log2 of the
+// bucket's matrix count); a missing entry is measured on the spot: probe
+// plans of the range's largest order and the bucket's count run on
+// synthetic symmetric matrices (deterministic, generated on the device),
+// first one per tridiagonalisation shape, then one per chase shape with
+// the best of those, each timed by its phase events (best of two after a
+// warm-up). The table can be saved to and loaded from a text file.
+namespace {
+
+template <class T>
+__global__ void k_tune_fill(T* A, int n, long long total) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long nn = (long long)n * n;
+    const unsigned m = (unsigned)(t / nn);
+    const int r = (int)(t % nn), i = r % n, j = r / n;
+    const unsigned a = (unsigned)max(i, j), b = (unsigned)min(i, j);
+    unsigned h = (m * 0x9E3779B1u) ^ (a * 0x85EBCA77u) ^ (b * 0xC2B2AE3Du + 0x27D4EB2Fu);
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    A[t] = (T)((double)h * (2.0 / 4294967296.0) - 1.0);
+  }
+}
+
+struct TuneKey {
+  int fam;  // 0: FP64 kernels, 1: FP32 kernels
+  char jobz;
+  int range;   // orders 16 range + 1 .. 16 (range + 1)
+  int cclass;  // floor(log2(matrices in the bucket))
+  bool operator<(const TuneKey& o) const {
+    if (fam != o.fam) return fam < o.fam;
+    if (jobz != o.jobz) return jobz < o.jobz;
+    if (range != o.range) return range < o.range;
+    return cclass < o.cclass;
+  }
+};
+struct TuneVal {
+  int tri_mult;
+  int lpw;
+  float tri_ms, chase_ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune;
+
+constexpr int kTuneMaxCount = 2048;
+
+// One probe configuration: best-of-two phase times after a warm-up run.
+int tune_probe(int prec, char jobz, int n, int count, int base_flags, int tri_mult, int lpw, const void* A,
+               void* w, void* V, int* info, float* tri_ms, float* chase_ms) {
+  std::vector<int64_t> ns((size_t)count, n);
+  gla_plan_t q = nullptr;
+  int rc = gla_plan_create(&q, prec, jobz, 'L', count, ns.data(), 0.0, base_flags | GLA_FLAG_TIMING);
+  if (rc) return rc;
+  Bucket& bk = q->buckets[0];
+  bk.nt_tri = std::min(256, bk.nt * tri_mult);
+  bk.lpw = lpw;
+  float bt = 1e30f, bc = 1e30f;
+  for (int rep = 0; rep < 3 && rc >= 0; rep++) {
+    rc = gla_plan_execute(q, A, w, jobz == 'V' ? V : nullptr, info, nullptr);
+    if (rc < 0) break;
+    float ms[GLA_NUM_PHASES];
+    rc = gla_plan_phase_times(q, ms);
+    if (rep > 0) {
+      bt = std::min(bt, ms[GLA_PHASE_TRIDIAG]);
+      bc = std::min(bc, ms[GLA_PHASE_CHASE]);
+    }
+  }
+  gla_plan_destroy(q);
+  if (rc < 0) return rc;
+  *tri_ms = bt;
+  *chase_ms = bc;
+  return 0;
+}
+
+int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
+  const int n = 16 * (k.range + 1);
+  count = std::max(1, std::min(count, kTuneMaxCount));
+  const int prec = k.fam == 0 ? GLA_PREC_F64 : GLA_PREC_F32;
+  const size_t el = k.fam == 0 ? 8 : 4;
+  void *A = nullptr, *w = nullptr, *V = nullptr;
+  int* info = nullptr;
+  const long long total = (long long)count * n * n;
+  cudaError_t e = cudaMalloc(&A, el * total);
+  if (e == cudaSuccess) e = cudaMalloc(&V, el * total);
+  if (e == cudaSuccess) e = cudaMalloc(&w, el * (size_t)count * n);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&info, sizeof(int) * count);
+  if (e == cudaSuccess) {
+    if (k.fam == 0)
+      k_tune_fill<double><<<1024, 256>>>((double*)A, n, total);
+    else
+      k_tune_fill<float><<<1024, 256>>>((float*)A, n, total);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int rc = e == cudaSuccess ? 0 : -1000 - (int)e;
+  const int nt = std::max(32, (n + 31) / 32 * 32);
+  TuneVal best{1, k.fam == 0 ? 16 : 8, 1e30f, 1e30f};
+  for (int mult = 1; mult <= 4 && rc == 0; mult *= 2) {
+    if (mult > 1 && nt * mult / 2 >= 256) break;  // the shape would repeat the previous one
+    float t = 0, c = 0;
+    rc = tune_probe(prec, k.jobz, n, count, base_flags, mult, best.lpw, A, w, V, info, &t, &c);
+    if (rc == 0 && t < best.tri_ms) {
+      best.tri_ms = t;
+      best.tri_mult = mult;
+    }
+  }
+  for (int lpw : {1, 2, 4, 8, 16, 32}) {
+    if (rc) break;
+    float t = 0, c = 0;
+    rc = tune_probe(prec, k.jobz, n, count, base_flags, best.tri_mult, lpw, A, w, V, info, &t, &c);
+    if (rc == 0 && c < best.chase_ms) {
+      best.chase_ms = c;
+      best.lpw = lpw;
+    }
+  }
+  cudaFree(A);
+  cudaFree(V);
+  cudaFree(w);
+  cudaFree(info);
+  if (rc) return rc;
+  *out = best;
+  return 0;
+}
+
+int autotune_plan(gla_plan_t p, int base_flags) {
+  const int fam = p->prec == GLA_PREC_F64 ? 0 : 1;
+  const char jz = p->prec == GLA_PREC_F32_REFINED ? 'V' : p->jobz;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (Bucket& bk : p->buckets) {
+    int cc = 0;
+    while ((2 << cc) <= bk.count && cc < 30) cc++;
+    const TuneKey key{fam, jz, (bk.nmax - 1) / 16, cc};
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) {
+      TuneVal v{};
+      int rc = tune_measure(key, bk.count, base_flags, &v);
+      if (rc) return rc;
+      it = g_tune.emplace(key, v).first;
+    }
+    bk.nt_tri = std::min(256, bk.nt * it->second.tri_mult);
+    bk.lpw = it->second.lpw;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gla_autotune_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  return 0;
+}
+
+int gla_autotune_save(const char* path) {
+  if (!path) return -1;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  FILE* f = std::fopen(path, "w");
+  if (!f) return -1;
+  std::fprintf(f, "# glagpu autotune v1: family jobz range count_class tri_mult lanes_per_warp tri_ms chase_ms\n");
+  for (const auto& kv : g_tune)
+    std::fprintf(f, "%d %c %d %d %d %d %.6g %.6g\n", kv.first.fam, kv.first.jobz, kv.first.range, kv.first.cclass,
+                 kv.second.tri_mult, kv.second.lpw, kv.second.tri_ms, kv.second.chase_ms);
+  return std::fclose(f) == 0 ? 0 : -1;
+}
+
+int gla_autotune_load(const char* path) {
+  if (!path) return -1;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return -1;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  char line[256];
+  int loaded = 0;
+  while (std::fgets(line, sizeof line, f)) {
+    if (line[0] == '#') continue;
+    TuneKey k{};
+    TuneVal v{};
+    char jz = 0;
+    if (std::sscanf(line, "%d %c %d %d %d %d %g %g", &k.fam, &jz, &k.range, &k.cclass, &v.tri_mult, &v.lpw,
+                    &v.tri_ms, &v.chase_ms) != 8)
+      continue;
+    k.jobz = jz;
+    const bool ok = (k.fam == 0 || k.fam == 1) && (jz == 'V' || jz == 'N') && k.range >= 0 &&
+                    k.range < kMaxBuckets && k.cclass >= 0 && (v.tri_mult == 1 || v.tri_mult == 2 ||
+                    v.tri_mult == 4) && v.lpw >= 1 && v.lpw <= 32;
+    if (!ok) continue;
+    g_tune[k] = v;
+    loaded++;
+  }
+  std::fclose(f);
+  return loaded;
+}
+
+int gla_plan_buckets(gla_plan_t p, int* count) {
+  if (!p) return -1;
+  if (!count) return -2;
+  *count = (int)p->buckets.size();
+  return 0;
+}
+
+int gla_plan_bucket_config(gla_plan_t p, int b, int* nmax, int* matrices, int* nt_tri, int* lanes_per_warp) {
+  if (!p) return -1;
+  if (b < 0 || b >= (int)p->buckets.size()) return -2;
+  if (!nmax) return -3;
+  if (!matrices) return -4;
+  if (!nt_tri) return -5;
+  if (!lanes_per_warp) return -6;
+  const Bucket& bk = p->buckets[b];
+  *nmax = bk.nmax;
+  *matrices = bk.count;
+  *nt_tri = bk.nt_tri;
+  *lanes_per_warp = bk.lpw > 0 ? bk.lpw : (p->prec == GLA_PREC_F64 ? 16 : 8);
+  return 0;
 }
 
 }  // extern "C"

@@ -24,7 +24,8 @@ cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t sm
 
 cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,
-                         double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats);
+                         double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats,
+                         int lanes_per_warp = 0);
 
 cudaError_t launch_apply(int tcode, int nblocks, int nt, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* V, const void* d, void* w, ChaseState* cst, const void* rot,

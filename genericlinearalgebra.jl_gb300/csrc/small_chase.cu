@@ -570,12 +570,14 @@ cudaError_t chase_kernels_init() {
 
 cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,
-                         double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats) {
+                         double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats,
+                         int lanes_per_warp) {
   if (count <= 0) return cudaSuccess;
-  // FP32 chases are instruction-latency bound: 8 matrices per warp keeps the
-  // lanes of a warp in step; FP64 pays ~64 cycles per warp instruction, so
-  // the cost of divergence and of idle lanes balance at 16.
-  const int lpw = tcode == kF64 ? 16 : 8;
+  // Default: FP32 chases are instruction-latency bound, 8 matrices per warp
+  // keep the lanes of a warp in step; FP64 pays ~64 cycles per warp
+  // instruction, so the cost of divergence and of idle lanes balance at 16.
+  // A plan's autotuner may choose another count (1..32).
+  const int lpw = (lanes_per_warp >= 1 && lanes_per_warp <= 32) ? lanes_per_warp : (tcode == kF64 ? 16 : 8);
   const int nb = (count + lpw - 1) / lpw;
 #define GLA_CH(T, A)                                                                                             \
   k_chase<T, A><<<nb, 32, smem, st>>>(descs, perm, count, (T*)d, (T*)e, cst, (T*)rot, hdr, info, (T)tol,        \

@@ -100,7 +100,7 @@ class Plan:
     """
 
     def __init__(self, ns, precision="f64", jobz="V", uplo="L", tol=None, alg="QL", small_log=False,
-                 timing=False, graph=False):
+                 timing=False, graph=False, autotune=False):
         L = _lib.load()
         ns = np.ascontiguousarray(np.asarray(ns, dtype=np.int64))
         if (ns < 0).any() or (ns > GLA_MAX_N).any():
@@ -111,7 +111,8 @@ class Plan:
         self.uplo = uplo
         self.dtype = np.float32 if precision == "f32" else np.float64
         flags = (GLA_ALG_QR if alg == "QR" else GLA_ALG_QL) | (_lib.GLA_FLAG_SMALL_LOG if small_log else 0) | \
-            (_lib.GLA_FLAG_TIMING if timing else 0) | (_lib.GLA_FLAG_GRAPH if graph else 0)
+            (_lib.GLA_FLAG_TIMING if timing else 0) | (_lib.GLA_FLAG_GRAPH if graph else 0) | \
+            (_lib.GLA_FLAG_AUTOTUNE if autotune else 0)
         self.graph = graph
         h = C.c_void_p()
         _lib.check(L.gla_plan_create(C.byref(h), PRECISIONS[precision], jobz.encode(), uplo.encode(), len(ns),
@@ -139,6 +140,19 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+    def bucket_configs(self):
+        """Launch shapes of the size buckets: list of dicts (nmax, matrices,
+        threads per CTA of the tridiagonalisation, chase matrices per warp)."""
+        L = _lib.load()
+        nb = C.c_int()
+        _lib.check(L.gla_plan_buckets(self._h, C.byref(nb)), "gla_plan_buckets")
+        out = []
+        for b in range(nb.value):
+            v = [C.c_int() for _ in range(4)]
+            _lib.check(L.gla_plan_bucket_config(self._h, b, *[C.byref(x) for x in v]), "gla_plan_bucket_config")
+            out.append(dict(zip(("nmax", "matrices", "nt_tri", "lanes_per_warp"), [x.value for x in v])))
+        return out
 
     def workspace_bytes(self):
         b = C.c_size_t()
@@ -377,5 +391,24 @@ def eigen2(A, uplo="L", tol=None, precision="f64", alg="QL"):
     return Eigen(vals, vecs[rows].copy())
 
 
+def autotune_clear():
+    """Drop every entry of the process-wide autotune table."""
+    _lib.check(_lib.load().gla_autotune_clear(), "gla_autotune_clear")
+
+
+def autotune_save(path):
+    """Write the autotune table to a text file."""
+    _lib.check(_lib.load().gla_autotune_save(str(path).encode()), "gla_autotune_save")
+
+
+def autotune_load(path):
+    """Merge the entries of an autotune file; returns how many were loaded."""
+    rc = _lib.load().gla_autotune_load(str(path).encode())
+    if rc < 0:
+        raise OSError(f"cannot read autotune file {path}")
+    return rc
+
+
 __all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigen2", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
+           "autotune_clear", "autotune_save", "autotune_load",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

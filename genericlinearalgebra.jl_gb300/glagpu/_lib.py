@@ -23,6 +23,7 @@ GLA_ERR_UNSUPPORTED = -2002
 GLA_FLAG_SMALL_LOG = 4
 GLA_FLAG_TIMING = 8
 GLA_FLAG_GRAPH = 16
+GLA_FLAG_AUTOTUNE = 32
 PHASES = ("tridiag", "chase", "apply", "refine")
 COUNTERS = ("rotations", "sweeps", "row_rotations", "refine_n3", "passes")
 
@@ -35,6 +36,12 @@ _d = C.c_double
 SIGNATURES = {
     "gla_version": ([], _int),
     "gla_gemm_df": ([_i64, _i64, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp], _int),
+    "gla_gemm_df_last_ms": ([C.POINTER(C.c_float), C.POINTER(C.c_float)], _int),
+    "gla_autotune_clear": ([], _int),
+    "gla_autotune_save": ([C.c_char_p], _int),
+    "gla_autotune_load": ([C.c_char_p], _int),
+    "gla_plan_buckets": ([_vp, C.POINTER(_int)], _int),
+    "gla_plan_bucket_config": ([_vp, _int, C.POINTER(_int), C.POINTER(_int), C.POINTER(_int), C.POINTER(_int)], _int),
     "gla_status_string": ([_int], C.c_char_p),
     "gla_plan_create": ([C.POINTER(_vp), _int, _ch, _ch, _i64, C.POINTER(_i64), _d, _int], _int),
     "gla_plan_destroy": ([_vp], _int),

@@ -62,6 +62,12 @@ extern "C" {
  * rotations, twice what random spectra need) and a matrix that would need more
  * is reported with info = -2 instead of being finished by extra passes. */
 #define GLA_FLAG_GRAPH 16
+/* Flag bit: choose each size bucket's launch shapes (threads per CTA of the
+ * tridiagonalisation, 1-4 per row; matrices per warp of the chase, 1-32) from the process-wide
+ * autotune table; shapes missing from it are measured during plan creation
+ * on synthetic matrices of the bucket's order and count (synchronizes the
+ * device; a few seconds for a fresh table) and added. See gla_autotune_*. */
+#define GLA_FLAG_AUTOTUNE 32
 
 /* Phases reported by gla_plan_phase_times. */
 #define GLA_PHASE_TRIDIAG 0 /* symtri! + Array(Q)          */
@@ -220,6 +226,9 @@ int gla_dsyev_static(char jobz, char uplo, int64_t n, double* A, int64_t lda, do
  */
 int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* Alo, int64_t lda, const float* Bhi,
                 const float* Blo, int64_t ldb, float* Chi, float* Clo, int64_t ldc, void* stream);
+/* Stream-event durations of the most recent gla_gemm_df call (synchronizes
+ * with its end): the operand slicing and the tensor-core GEMM kernel. */
+int gla_gemm_df_last_ms(float* slice_ms, float* gemm_ms);
 
 /*
  * eigen!/eigvals! of SymTridiagonal(d, e) (src/eigenSelfAdjoint.jl:581,
@@ -231,6 +240,19 @@ int gla_gemm_df(int64_t m, int64_t n, int64_t k, const float* Ahi, const float* 
  */
 int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz, int flags, int* info,
               void* stream);
+
+/*
+ * Autotune table (GLA_FLAG_AUTOTUNE): drop every entry; write the entries to
+ * a text file; merge the entries of such a file (returns how many were
+ * loaded, <0 when the file cannot be read).
+ */
+int gla_autotune_clear(void);
+int gla_autotune_save(const char* path);
+int gla_autotune_load(const char* path);
+/* The plan's size buckets (orders <= GLA_MAX_SMALL_N) and the launch shapes
+ * each one runs with. */
+int gla_plan_buckets(gla_plan_t plan, int* count);
+int gla_plan_bucket_config(gla_plan_t plan, int bucket, int* nmax, int* matrices, int* nt_tri, int* lanes_per_warp);
 
 #ifdef __cplusplus
 }

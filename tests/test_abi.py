@@ -43,3 +43,25 @@ def test_host_only_calls(lib):
     lib.gla_status_string.argtypes = [ctypes.c_int]
     assert lib.gla_status_string(0) == b"success"
     assert b"argument 3" in lib.gla_status_string(-3)
+
+
+def test_autotune_table_file_roundtrip(lib, tmp_path):
+    # host-only: the table's text format, validation of loaded lines, save
+    lib.gla_autotune_load.argtypes = [ctypes.c_char_p]
+    lib.gla_autotune_save.argtypes = [ctypes.c_char_p]
+    assert lib.gla_autotune_clear() == 0
+    src = tmp_path / "tune.txt"
+    src.write_text("# comment\n"
+                   "0 V 7 9 2 16 1.5 3.25\n"
+                   "1 N 0 4 4 32 0.1 0.2\n"
+                   "1 V 3 2 3 8 0.1 0.2\n"      # tri_mult 3: rejected
+                   "0 V 2 1 1 64 0.1 0.2\n"     # 64 lanes: rejected
+                   "garbage line\n")
+    assert lib.gla_autotune_load(str(src).encode()) == 2
+    out = tmp_path / "out.txt"
+    assert lib.gla_autotune_save(str(out).encode()) == 0
+    rows = [l.split() for l in out.read_text().splitlines() if not l.startswith("#")]
+    assert sorted((r[0], r[1], r[2], r[3], r[4], r[5]) for r in rows) == \
+        [("0", "V", "7", "9", "2", "16"), ("1", "N", "0", "4", "4", "32")]
+    assert lib.gla_autotune_load(str(tmp_path / "missing.txt").encode()) < 0
+    assert lib.gla_autotune_clear() == 0
