@@ -44,12 +44,16 @@ cudaError_t dfgemm_launch(const DfGemmDesc& g, bool ta, cudaStream_t st);
 // accuracy on the bf16 tensor cores. Operands are sliced first: the A operand
 // from the columns of a float-pair matrix (its rows after transposition, or
 // the rows of a symmetric matrix), the B operand from its columns; S = 7
-// slices of 7 bits each (the only count accepted), relative to the largest
-// entry of the row or column: double-float accuracy whatever the spread of
-// the entries. oz_create with
+// slices of 7 bits each (oz_create; the slice count must match the work
+// object's), relative to the largest entry of the row or column:
+// double-float accuracy whatever the spread of the entries. oz_create with
 // m = 0 or n = 0 allocates only the other operand.
 struct OzWork;
 int oz_create(OzWork** out, int m, int n, int K);
+// FP32-accuracy configuration: S = 4 slices (28 bits relative to the row and
+// column maxima, pairs up to 2^-35), 128 x 128 tiles, C written in FP32 to
+// Chi (Clo unused).
+int oz_create_f32(OzWork** out, int m, int n, int K);
 void oz_destroy(OzWork* w);
 cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo, long long ld, int count, int len,
                      int S, cudaStream_t st);

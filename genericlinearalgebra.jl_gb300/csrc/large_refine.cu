@@ -7,13 +7,14 @@
 //   P    = A X                              tcgen05 Ozaki GEMM (ozaki.cuh)
 //   lam  = diag(X'P) / diag(X'X)            double-float column dots
 //   Rres = P - X diag(lam)                  double-float, rounded to FP32
-//   T    = X' Rres                          FP32 GEMM
+//   T    = X_hi' Rres                       FP32-accuracy tensor-core GEMM
 // With R = I - X'X and S = X'AX = (I - R) diag(lam) + T, the Ogita-Aishima
 // numerator s_ij + lam_j r_ij equals t_ij for i != j, so
 //   E_ij = t_ij / (lam_j - lam_i)          separated pairs
 //   E_ii = (1 - (X'X)_ii) / 2
 //   E_ij = -(X'X)_ij / 2                   pairs inside one cluster
-//   X   <- X + X E                          FP32 GEMM, added in double-float
+//   X   <- X + X_hi E                       FP32-accuracy tensor-core GEMM,
+//                                           added in double-float
 // (T. Ogita, K. Aishima, JJIAM 35 (2018) Alg. 1, rewritten on the residual;
 // t_ij - t_ji = r_ij (lam_j - lam_i) carries the orthogonality correction of
 // separated pairs, so X'X is only formed when clusters need it and in the
@@ -79,6 +80,7 @@ struct RefineLarge {
   std::map<int, LargeCtx*> big;  // FP32 solvers for clusters above the small limit
   OzWork* oz = nullptr;          // tcgen05 double-float GEMM: A slices (A operand), X slices (B operand)
   OzWork* ozx = nullptr;         // X slices as the A operand (the Gram matrix X'X)
+  OzWork* oz32 = nullptr;        // tcgen05 FP32-accuracy GEMM: T = X_hi' Rres and X_hi E
   std::vector<double> h_lam;
   std::vector<int> h_couple;
   int iters = 0;
@@ -392,6 +394,7 @@ int refine_large_create(RefineLarge** out, int n) {
   }
   int orc = oz_create(&r->oz, n, n, n);
   if (!orc) orc = oz_create(&r->ozx, n, 0, n);
+  if (!orc) orc = oz_create_f32(&r->oz32, n, n, n);
   if (orc) {
     refine_large_destroy(r);
     return orc;
@@ -421,6 +424,7 @@ void refine_large_destroy(RefineLarge* r) {
   for (auto& kv : r->big) large_destroy(kv.second);
   oz_destroy(r->oz);
   oz_destroy(r->ozx);
+  oz_destroy(r->oz32);
   delete r;
 }
 
@@ -534,20 +538,11 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       RF_CUDA(cudaMemsetAsync(r->scal, 0, sizeof(float) * 4, st));
       k_ref_rres<<<n, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, r->lam, n, r->Rres, r->rn, r->scal + 2);
       RF_CUDA(cudaGetLastError());
-      // T = X' Rres (FP32)
-      GemmDesc t{};
-      t.m = n;
-      t.n = n;
-      t.k = n;
-      t.A = r->Xhi;
-      t.lda = n;
-      t.B = r->Rres;
-      t.ldb = n;
-      t.C = r->T;
-      t.ldc = n;
-      t.alpha = 1.0;
-      t.beta = 0.0;
-      RF_CUDA(gemm_launch(false, true, false, false, t, 1, st));
+      // T = X_hi' Rres to FP32 accuracy on the tensor cores (A operand: the
+      // columns of X_hi; B operand: the columns of Rres)
+      RF_CUDA(oz_slice(r->oz32, true, r->Xhi, nullptr, n, n, n, 4, st));
+      RF_CUDA(oz_slice(r->oz32, false, r->Rres, nullptr, n, n, n, 4, st));
+      RF_CUDA(oz_gemm(r->oz32, n, n, n, r->T, nullptr, n, false, st));
       k_ref_couple<<<(n + 255) / 256, 256, 0, st>>>(r->T, r->lam, r->rn, n, r->couple);
       RF_CUDA(cudaGetLastError());
       RF_CUDA(cudaMemcpyAsync(r->h_lam.data(), r->lam, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
@@ -596,19 +591,9 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
         RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Phi, r->Plo, n, false, st));
         k_ref_update_df<<<2048, 256, 0, st>>>(r->Xhi, r->Xlo, r->Phi, r->Plo, nn);
       } else {
-        GemmDesc u{};
-        u.m = n;
-        u.n = n;
-        u.k = n;
-        u.A = r->Xhi;
-        u.lda = n;
-        u.B = r->E;
-        u.ldb = n;
-        u.C = r->XE;
-        u.ldc = n;
-        u.alpha = 1.0;
-        u.beta = 0.0;
-        RF_CUDA(gemm_launch(false, false, false, false, u, 1, st));
+        RF_CUDA(oz_slice_rows(r->oz32, r->Xhi, nullptr, n, n, n, 4, st));
+        RF_CUDA(oz_slice(r->oz32, false, r->E, nullptr, n, n, n, 4, st));
+        RF_CUDA(oz_gemm(r->oz32, n, n, n, r->XE, nullptr, n, false, st));
         k_ref_update<<<2048, 256, 0, st>>>(r->Xhi, r->Xlo, r->XE, nn);
       }
       RF_CUDA(cudaGetLastError());
@@ -630,11 +615,13 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       if (!cs.empty())
         RF_CUDA(cudaMemcpyAsync(hoff.data(), r->offmax, sizeof(float) * cs.size(), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaMemcpyAsync(hs, r->scal, sizeof(hs), cudaMemcpyDeviceToHost, st));
-      int oz_err[2] = {0, 0};
+      int oz_err[3] = {0, 0, 0};
       RF_CUDA(cudaMemcpyAsync(&oz_err[0], oz_error_word(r->oz), sizeof(int), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaMemcpyAsync(&oz_err[1], oz_error_word(r->ozx), sizeof(int), cudaMemcpyDeviceToHost, st));
+      RF_CUDA(cudaMemcpyAsync(&oz_err[2], oz_error_word(r->oz32), sizeof(int), cudaMemcpyDeviceToHost, st));
       RF_CUDA(cudaStreamSynchronize(st));
-      if (oz_err[0] || oz_err[1]) return -1000 - (int)cudaErrorLaunchTimeout;  // a bounded wait of the tensor-core GEMM ran out
+      if (oz_err[0] || oz_err[1] || oz_err[2])
+        return -1000 - (int)cudaErrorLaunchTimeout;  // a bounded wait of the tensor-core GEMM ran out
       std::vector<int> rs, rcnt;
       std::vector<long long> roff;
       std::vector<double> rmu;

@@ -41,23 +41,48 @@ namespace gla {
 namespace oz {
 
 constexpr int kBM = 128;        // C tile rows (MMA M)
-constexpr int kBN = 64;         // C tile columns (MMA N)
 constexpr int kKS = 32;         // k per pipeline stage (two K = 16 MMAs per slice pair)
-constexpr int kStages = 2;
 constexpr int kGroupK = 256;    // k per TMEM drain (exactness bound)
 constexpr int kMaxSlices = 7;
-constexpr int kMaxLevel = 8;    // pairs with s + t <= kMaxLevel
-constexpr int kLevels = kMaxLevel - 1;  // levels 2 .. 8
-constexpr int kDrainWarps = 8;  // two per TMEM lane quarter, 32 columns each
+constexpr int kDrainWarps = 8;  // two per TMEM lane quarter
 constexpr int kThreads = 64 + 32 * kDrainWarps;
-constexpr int kDrainCols = kBN / (kDrainWarps / 4);
 constexpr long long kWaitLimit = 1ll << 26;
 
 // Bytes of one tiled slab block: rows x kKS k, bf16.
 __host__ __device__ constexpr int block_bytes(int rows) { return rows * kKS * 2; }
 constexpr int kABlock = block_bytes(kBM);  // 8 KB
-constexpr int kBBlock = block_bytes(kBN);  // 4 KB
-__host__ __device__ constexpr size_t stage_bytes(int sa, int sb) { return (size_t)sa * kABlock + (size_t)sb * kBBlock; }
+
+// Kernel configurations. S slices per operand, pairs with s + t <= S + 1
+// (levels 2 .. S + 1, one TMEM accumulator of BN columns each), C tiles of
+// 128 x BN:
+//   double-float products: 7 slices (49 bits), 28 pairs, BN = 64, output as
+//     a float pair;
+//   FP32-accuracy products: 4 slices (28 bits, relative to the row and
+//     column maxima), 10 pairs, BN = 128 (four levels fill the 512 TMEM
+//     columns), output in FP32.
+// Exactness of a 256-k group for S = 4: the largest level (5) adds at most
+// 2 x 129 x 65 + 2 x 65^2 = 25,220 per k, 256 x 25,220 < 2^24.
+template <int S_, int BN_, bool DF_>
+struct OzCfg {
+  static constexpr int S = S_;
+  static constexpr int BN = BN_;
+  static constexpr bool DF = DF_;
+  static constexpr int kMaxLevel = S + 1;
+  static constexpr int kBBlock = block_bytes(BN);
+  static constexpr uint32_t kAAll = S * kABlock, kBAll = S * kBBlock;
+  static constexpr size_t kStageBytes = (size_t)kAAll + kBAll;
+  static constexpr int kStages = kStageBytes <= 65536 ? 3 : 2;
+  static constexpr size_t kSmem = kStages * kStageBytes;
+  static constexpr int kDrainCols = BN / (kDrainWarps / 4);
+  // kind::f16 instruction descriptor: F32 accumulate, bf16 A and B, both
+  // K-major, N = BN, M = kBM
+  static constexpr uint32_t kIdesc =
+      (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+  static_assert(S * BN <= 512, "level accumulators exceed the TMEM columns");
+  static_assert(kSmem + 1024 <= 232448, "stage ring exceeds shared memory");
+};
+using CfgDF = OzCfg<7, 64, true>;
+using CfgF32 = OzCfg<4, 128, false>;
 
 // Byte offset of element (r, kk) inside a tiled slab block (8-row x 8-k core
 // matrices of 128 contiguous bytes; K-neighbours 128 B apart = LBO, row
@@ -68,12 +93,13 @@ __host__ __device__ __forceinline__ int tile_off(int r, int kk) {
 }
 
 // Sliced operand: slice s, row block b (height H rows), k slab q at
-// base + ((b * nks + q) * kMaxSlices + s) * block_bytes(H): the slices of one
-// slab are adjacent, so one bulk copy moves all of them.
+// base + ((b * nks + q) * S + s) * block_bytes(H): the slices of one slab are
+// adjacent, so one bulk copy moves all of them.
 struct Sliced {
   __nv_bfloat16* base;
   int* exps;   // per row: scale exponent e (rows scaled by 2^-e)
-  int rows, nblk, nks, H, S;  // S: kMaxSlices once sliced, 0 before
+  unsigned* mbits;  // per row: bits of max |hi| (slicing scratch)
+  int rows, nblk, nks, H, S;  // S: slices per value once sliced, 0 before
 };
 
 GLA_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -87,10 +113,6 @@ GLA_DEV uint64_t make_desc(uint32_t saddr) {
   return d;                                      // base offset 0, no swizzle
 }
 
-// kind::f16 instruction descriptor: F32 accumulate, bf16 A and B, both
-// K-major, N = kBN, M = kBM.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
-                            ((uint32_t)(kBM >> 4) << 24);
 
 GLA_DEV void mbar_init(uint64_t* b, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
@@ -125,11 +147,11 @@ GLA_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
 }
-GLA_DEV void mma_f16(uint32_t tmem_d, uint64_t ad, uint64_t bd, uint32_t accumulate) {
+GLA_DEV void mma_f16(uint32_t tmem_d, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
           tmem_d),
-      "l"(ad), "l"(bd), "r"(kIdesc), "r"(accumulate));
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
 }
 GLA_DEV void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -144,113 +166,117 @@ GLA_DEV void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 struct GemmArgs {
-  Sliced A, B;           // A: rows = M (H = 128); B: rows = N (H = 64)
+  Sliced A, B;           // A: rows = M (H = 128); B: rows = N (H = BN)
   int M, N, K;
   int ntn;               // column tiles
-  float* Chi;
-  float* Clo;
+  float* Chi;            // FP32-accuracy configuration: the result
+  float* Clo;            // (double-float configuration only)
   long long ldc;
   int lower;             // only tiles touching the lower triangle, only i >= j stored
   int* err;
 };
 
 // ---------------------------------------------------------------- slicing
+//
+// A float-pair matrix becomes the tiled operand in two passes:
+//   1. the largest |hi| of every operand row (a column of the source for
+//      k_oz_rowmax_cols, a row for k_oz_rowmax_rows), as float bits;
+//   2. k_oz_tile: one CTA per (row block, 32-k slab) loads its H x 32 pairs
+//      coalesced, forms the seven slices of each, lays them out in shared
+//      memory in the MMA's canonical layout and writes the slab's seven
+//      contiguous blocks with 16-byte stores.
+// Slices of a value scaled to |v| < 1 by 2^-e, e = ilogb(max |hi|) + 1:
+// d_1 = rint(128 v), then repeatedly the remainder times 128 (the remainder
+// r = (hi, lo) 2^-e is kept exactly in double-float: scalings by powers of
+// two, TwoSum); |d_1| <= 128 (129 for an edge value reaching 1, still exact
+// in bf16 and inside the accumulation bound), |d_s| <= 65 after.
 
-// Column c of a float-pair matrix (len entries, leading dimension ld; for a
-// symmetric A its column c is its row c) -> S integer slices of the scaled
-// values, written as row c of a tiled operand. One CTA per column. The
-// slicing runs in double-float arithmetic on the FP32 pipe: the remainder
-// r = (hi, lo) 2^-e is kept exactly (scalings by powers of two, TwoSum), the
-// next slice is rint of its leading float (|d_1| <= 128, |d_s| <= 65 after).
-__global__ void __launch_bounds__(256) k_oz_slice(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                  long long ld, int len, int ncols, Sliced out) {
-  const int c = blockIdx.x;
-  __shared__ float red[8];
-  const float* h = hi + (long long)c * ld;
-  const float* l = lo ? lo + (long long)c * ld : nullptr;
+// Source columns c (len entries from hi + c ld): one warp per column.
+__global__ void __launch_bounds__(256) k_oz_rowmax_cols(const float* __restrict__ hi, long long ld, int len,
+                                                        int count, int rows_pad, unsigned* __restrict__ mbits) {
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= rows_pad) return;
   float m = 0.f;
-  if (c < ncols)
-    for (int k = threadIdx.x; k < len; k += 256) m = fmaxf(m, fabsf(h[k]));
+  if (c < count)
+    for (int k = lane; k < len; k += 32) m = fmaxf(m, fabsf(hi[(long long)c * ld + k]));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  m = 0.f;
-  for (int w = 0; w < 8; w++) m = fmaxf(m, red[w]);
-  // |hi + lo| < 2^(ilogb(m) + 1) up to the last ulp: |value| 2^-e < 1 (an
-  // edge value reaching 1 gives d_1 = 129, still exact in bf16 and inside
-  // the accumulation bound)
-  const int e = m > 0.f ? ilogbf(m) + 1 : 0;
-  if (threadIdx.x == 0) out.exps[c] = e;
-  const int b = c / out.H, r = c % out.H;
-  const size_t bb = (size_t)block_bytes(out.H);
-  char* base = reinterpret_cast<char*>(out.base);
-  const int kpad = out.nks * kKS;
-  for (int k = threadIdx.x; k < kpad; k += 256) {
-    float vh = 0.f, vl = 0.f;
-    if (c < ncols && k < len) {
-      vh = ldexpf(h[k], -e);
-      vl = l ? ldexpf(l[k], -e) : 0.f;
+  if (lane == 0) mbits[c] = __float_as_uint(m);
+}
+
+// Source rows c (element (c, k) at hi[c + k ld]): one thread per row and
+// k chunk, merged by an atomic max on the (non-negative) float bits; mbits
+// must be zero on entry.
+__global__ void __launch_bounds__(256) k_oz_rowmax_rows(const float* __restrict__ hi, long long ld, int len,
+                                                        int rows, int kchunk, unsigned* __restrict__ mbits) {
+  const int c = blockIdx.x * 256 + threadIdx.x;
+  if (c >= rows) return;
+  const int k0 = blockIdx.y * kchunk, k1 = min(len, k0 + kchunk);
+  float m = 0.f;
+  for (int k = k0; k < k1; k++) m = fmaxf(m, fabsf(hi[c + (long long)k * ld]));
+  if (m > 0.f) atomicMax(&mbits[c], __float_as_uint(m));
+}
+
+GLA_DEV int slice_exp(unsigned mb) {
+  const float m = __uint_as_float(mb);
+  return m > 0.f ? ilogbf(m) + 1 : 0;
+}
+
+// ROWS = false: operand row c is source column c (element (c, k) at
+// c ld + k); ROWS = true: operand row c is source row c (at c + k ld).
+// Dynamic shared memory: S x block_bytes(H).
+template <bool ROWS, int S>
+__global__ void __launch_bounds__(256) k_oz_tile(const float* __restrict__ hi, const float* __restrict__ lo,
+                                                 long long ld, int len, int count, Sliced out) {
+  extern __shared__ __align__(16) unsigned char tsm[];
+  const int b = blockIdx.x, q = blockIdx.y, H = out.H, tid = threadIdx.x;
+  const int bb = block_bytes(H);
+  const int per = H * kKS / 256;  // elements per thread
+  for (int t = 0; t < per; t++) {
+    int r, kk;
+    if (ROWS) {  // a warp covers 32 consecutive rows of one k
+      const int e = t * 256 + tid;
+      r = e % H;
+      kk = e / H;
+    } else {  // a warp covers the 32 k of one row
+      r = t * (256 / kKS) + tid / kKS;
+      kk = tid % kKS;
     }
-    const int q = k / kKS, kk = k % kKS;
-    char* blk = base + (((size_t)b * out.nks + q) * kMaxSlices * bb) + tile_off(r, kk);
-    for (int s = 0; s < kMaxSlices; s++) {
+    const int c = b * H + r, k = q * kKS + kk;
+    float vh = 0.f, vl = 0.f;
+    if (c < count && k < len) {
+      const long long idx = ROWS ? c + (long long)k * ld : (long long)c * ld + k;
+      const int ex = slice_exp(out.mbits[c]);
+      vh = ldexpf(hi[idx], -ex);
+      vl = lo ? ldexpf(lo[idx], -ex) : 0.f;
+    }
+    unsigned char* dst = tsm + tile_off(r, kk);
+#pragma unroll
+    for (int s = 0; s < S; s++) {
       const float th = vh * 128.f, tl = vl * 128.f;
       const float d = rintf(th);
       float sh, se;
       two_sum(th - d, tl, sh, se);  // th - d is exact (|th - d| <= 1/2, same binade scale)
       vh = sh;
       vl = se;
-      *reinterpret_cast<__nv_bfloat16*>(blk + s * bb) = __float2bfloat16_rn(d);
+      *reinterpret_cast<__nv_bfloat16*>(dst + s * bb) = __float2bfloat16_rn(d);
     }
   }
-}
-
-// Rows of a column-major float-pair matrix (element (c, k) at c + k ld) ->
-// tiled operand rows, same slicing as k_oz_slice. One CTA per block of
-// out.H rows; for each k the block's rows are read contiguously.
-__global__ void __launch_bounds__(256) k_oz_slice_rows(const float* __restrict__ hi, const float* __restrict__ lo,
-                                                       long long ld, int len, int nrows, Sliced out) {
-  const int b = blockIdx.x, H = out.H, tid = threadIdx.x;
-  const int per = 256 / H;            // threads per row (2 for H = 128, 4 for H = 64)
-  const int r = tid % H, part = tid / H;
-  const int c = b * H + r;
-  __shared__ float smax[256];
-  float m = 0.f;
-  if (c < nrows)
-    for (int k = part; k < len; k += per) m = fmaxf(m, fabsf(hi[c + (long long)k * ld]));
-  smax[tid] = m;
+  if (q == 0)
+    for (int r = tid; r < H; r += 256) out.exps[b * H + r] = slice_exp(out.mbits[b * H + r]);
   __syncthreads();
-  m = 0.f;
-  for (int q = 0; q < per; q++) m = fmaxf(m, smax[q * H + r]);
-  const int e = m > 0.f ? ilogbf(m) + 1 : 0;
-  if (part == 0) out.exps[c] = e;
-  const size_t bb = (size_t)block_bytes(H);
-  char* base = reinterpret_cast<char*>(out.base);
-  const int kpad = out.nks * kKS;
-  for (int k = part; k < kpad; k += per) {
-    float vh = 0.f, vl = 0.f;
-    if (c < nrows && k < len) {
-      vh = ldexpf(hi[c + (long long)k * ld], -e);
-      vl = lo ? ldexpf(lo[c + (long long)k * ld], -e) : 0.f;
-    }
-    const int q = k / kKS, kk = k % kKS;
-    char* blk = base + (((size_t)b * out.nks + q) * kMaxSlices * bb) + tile_off(r, kk);
-    for (int s = 0; s < kMaxSlices; s++) {
-      const float th = vh * 128.f, tl = vl * 128.f;
-      const float d = rintf(th);
-      float sh, se;
-      two_sum(th - d, tl, sh, se);
-      vh = sh;
-      vl = se;
-      *reinterpret_cast<__nv_bfloat16*>(blk + s * bb) = __float2bfloat16_rn(d);
-    }
-  }
+  uint4* g = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out.base) +
+                                      ((size_t)b * out.nks + q) * S * (size_t)bb);
+  const uint4* sv = reinterpret_cast<const uint4*>(tsm);
+  for (int v = tid; v < S * bb / 16; v += 256) g[v] = sv[v];
 }
 
 // ---------------------------------------------------------------- GEMM
 
+template <class Cfg>
 __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
+  constexpr int kStages = Cfg::kStages, kBN = Cfg::BN, kMaxLevel = Cfg::kMaxLevel, kDrainCols = Cfg::kDrainCols;
+  constexpr int kBBlock = Cfg::kBBlock;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], drain_full, drain_empty, fin_bar;
   __shared__ uint32_t tmem_base;
@@ -284,8 +310,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
-  constexpr size_t stB = stage_bytes(kMaxSlices, kMaxSlices);
-  constexpr uint32_t kAAll = kMaxSlices * kABlock, kBAll = kMaxSlices * kBBlock;
+  constexpr size_t stB = Cfg::kStageBytes;
+  constexpr uint32_t kAAll = Cfg::kAAll, kBAll = Cfg::kBAll;
 
   if (wid == 0) {
     // ---- producer: slabs of every slice into the stage ring
@@ -312,7 +338,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
         }
     }
   } else if (wid == 1) {
-    // ---- MMA issuer: per slab the 28 slice pairs, unrolled with constant
+    // ---- MMA issuer: per slab the slice pairs, unrolled with constant
     // descriptor offsets (the descriptor's address field is addr >> 4 and
     // shared-memory offsets stay below 2^18, so adding offset >> 4 is exact)
     if (lane == 0) {
@@ -336,16 +362,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
 #pragma unroll
           for (int ks = 0; ks < kKS / 16; ks++)  // K = 16 per instruction: 2 K-core matrices = 256 B
 #pragma unroll
-            for (int s = 1; s <= kMaxSlices; s++)
+            for (int s = 1; s <= Cfg::S; s++)
 #pragma unroll
-              for (int t = 1; t <= kMaxSlices; t++) {
+              for (int t = 1; t <= Cfg::S; t++) {
                 if (s + t > kMaxLevel) continue;
                 // in this order (s = 1 first) the group's first MMA into
                 // level s + t has s = 1 and starts the accumulator from zero
                 const uint32_t accumulate = (qq == 0 && ks == 0 && s == 1) ? 0u : 1u;
                 mma_f16(tmem + (uint32_t)((s + t - 2) * kBN),
                         a0 + (uint64_t)(((s - 1) * kABlock + ks * 256) >> 4),
-                        b0 + (uint64_t)(((t - 1) * kBBlock + ks * 256) >> 4), accumulate);
+                        b0 + (uint64_t)(((t - 1) * kBBlock + ks * 256) >> 4), Cfg::kIdesc, accumulate);
               }
           mma_commit(&empty_bar[st]);  // stage buffer reusable once these MMAs finish
         }
@@ -358,9 +384,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
     const int quarter = wid & 3;
     const int cbase = ((wid - 2) / 4) * kDrainCols;
     const int r = row0 + quarter * 32 + lane;
-    df64 acc[kDrainCols];
+    // double-float sums (DF) or FP32 sums of the groups
+    df64 acc[Cfg::DF ? kDrainCols : 1];
+    float accf[Cfg::DF ? 1 : kDrainCols];
 #pragma unroll
-    for (int c = 0; c < kDrainCols; c++) acc[c] = df_make(0.f, 0.f);
+    for (int c = 0; c < kDrainCols; c++) {
+      if (Cfg::DF)
+        acc[c] = df_make(0.f, 0.f);
+      else
+        accf[c] = 0.f;
+    }
     bool ok = true;
     for (int gi = 0; gi < ngroups && ok; gi++) {
       if (!mbar_wait(&drain_full, gi & 1, err)) {
@@ -382,14 +415,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
           const float sc = ldexpf(1.f, -7 * L);
 #pragma unroll
           for (int q = 0; q < 16; q++) {
-            float sh, se;
-            two_sum(part_hi[q], __uint_as_float(v[q]) * sc, sh, se);
-            part_hi[q] = sh;
-            part_lo[q] += se;
+            if (Cfg::DF) {
+              float sh, se;
+              two_sum(part_hi[q], __uint_as_float(v[q]) * sc, sh, se);
+              part_hi[q] = sh;
+              part_lo[q] += se;
+            } else {
+              part_hi[q] = fmaf(__uint_as_float(v[q]), sc, part_hi[q]);
+            }
           }
         }
 #pragma unroll
-        for (int q = 0; q < 16; q++) acc[c0 + q] = df_add(acc[c0 + q], df_make(part_hi[q], part_lo[q]));
+        for (int q = 0; q < 16; q++) {
+          if (Cfg::DF)
+            acc[c0 + q] = df_add(acc[c0 + q], df_make(part_hi[q], part_lo[q]));
+          else
+            accf[c0 + q] += part_hi[q];
+        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(&drain_empty);
@@ -402,8 +444,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
         if (r >= g.M || col >= g.N || (g.lower && r < col)) continue;
         const int e = ei + g.B.exps[col];
         const long long idx = (long long)r + (long long)col * g.ldc;
-        g.Chi[idx] = ldexpf(acc[c].hi, e);
-        g.Clo[idx] = ldexpf(acc[c].lo, e);
+        if (Cfg::DF) {
+          g.Chi[idx] = ldexpf(acc[c].hi, e);
+          g.Clo[idx] = ldexpf(acc[c].lo, e);
+        } else {
+          g.Chi[idx] = ldexpf(accf[c], e);
+        }
       }
     }
   }
