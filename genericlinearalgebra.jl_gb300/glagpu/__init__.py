@@ -368,11 +368,69 @@ def eigen(A, uplo="L", tol=None, precision="f64", alg="QL"):
     return eigen_batched([A], uplo=uplo, tol=tol, precision=precision, alg=alg)[0]
 
 
-def eigvals(A, uplo="L", tol=None, precision="f64"):
-    """eigvals(Hermitian(A, uplo)) / eigvals(SymTridiagonal): ascending values."""
+def eigvals(A, uplo="L", tol=None, precision="f64", irange=None, vl=None, vu=None, abstol=0.0):
+    """eigvals(Hermitian(A, uplo)) / eigvals(SymTridiagonal): ascending values.
+    For SymTridiagonal input, irange = (il, iu) (1-based, inclusive, as
+    Julia's eigvals(T, il:iu)) or vl < lambda <= vu (eigvals(T, vl, vu))
+    select a subset, computed by Sturm-count multisection (gla_dstebz)."""
     if isinstance(A, SymTridiagonal):
+        if irange is not None or vl is not None or vu is not None:
+            return _tridiag_subset(A, irange, vl, vu, abstol)
         return _tridiag(A, "N", "QL", tol)
+    if irange is not None or vl is not None or vu is not None:
+        raise ValueError("eigenvalue subsets are available for SymTridiagonal input")
     return eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
+
+
+def _tridiag_dev(T):
+    torch = _torch()
+    on_dev = _is_torch(T.dv)
+    dev = T.dv.device if on_dev else torch.device("cuda")
+    d = torch.as_tensor(T.dv, dtype=torch.float64, device=dev).contiguous()
+    e = torch.as_tensor(T.ev, dtype=torch.float64, device=dev).contiguous()
+    if e.numel() == 0:
+        e = torch.zeros(1, dtype=torch.float64, device=dev)
+    return d, e, on_dev, dev
+
+
+def numnegevals(T, sigma=0.0):
+    """numnegevals(T::SymTridiagonal, sigma) (src/tridiag.jl:20-36): the number
+    of negative eigenvalues of T - sigma I. sigma may be an array of shifts
+    (one count per shift, computed in parallel); counts equal the reference's
+    recurrence bit for bit."""
+    torch = _torch()
+    d, e, on_dev, dev = _tridiag_dev(T)
+    n = d.numel()
+    sig = torch.as_tensor(np.atleast_1d(np.asarray(sigma, dtype=np.float64)) if not _is_torch(sigma) else sigma,
+                          dtype=torch.float64, device=dev).reshape(-1).contiguous()
+    counts = torch.empty(sig.numel(), dtype=torch.int64, device=dev)
+    _lib.check(_lib.load().gla_numnegevals(n, C.c_void_p(d.data_ptr()), C.c_void_p(e.data_ptr()), sig.numel(),
+                                           C.c_void_p(sig.data_ptr()), C.c_void_p(counts.data_ptr()),
+                                           _stream_ptr()), "gla_numnegevals")
+    if not _is_torch(sigma) and np.ndim(sigma) == 0:
+        return int(counts[0].item())
+    return counts if on_dev else counts.cpu().numpy()
+
+
+def _tridiag_subset(T, irange, vl, vu, abstol):
+    torch = _torch()
+    d, e, on_dev, dev = _tridiag_dev(T)
+    n = d.numel()
+    if irange is not None:
+        il, iu = int(irange[0]), int(irange[1])
+    else:
+        lo = -np.inf if vl is None else float(vl)
+        hi = np.inf if vu is None else float(vu)
+        # vl < lambda <= vu through counts of eigenvalues below each end
+        il = 1 if lo == -np.inf else numnegevals(T, lo) + 1
+        iu = n if hi == np.inf else numnegevals(T, hi)
+    if iu < il:
+        w = torch.empty(0, dtype=torch.float64, device=dev)
+        return w if on_dev else w.cpu().numpy()
+    w = torch.empty(iu - il + 1, dtype=torch.float64, device=dev)
+    _lib.check(_lib.load().gla_dstebz(n, C.c_void_p(d.data_ptr()), C.c_void_p(e.data_ptr()), il, iu, float(abstol),
+                                      C.c_void_p(w.data_ptr()), _stream_ptr()), "gla_dstebz")
+    return w if on_dev else w.cpu().numpy()
 
 
 def eigen2(A, uplo="L", tol=None, precision="f64", alg="QL"):
@@ -410,5 +468,5 @@ def autotune_load(path):
 
 
 __all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigen2", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
-           "autotune_clear", "autotune_save", "autotune_load",
+           "autotune_clear", "autotune_save", "autotune_load", "numnegevals",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

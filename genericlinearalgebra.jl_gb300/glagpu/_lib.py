@@ -42,6 +42,10 @@ SIGNATURES = {
     "gla_autotune_load": ([C.c_char_p], _int),
     "gla_plan_buckets": ([_vp, C.POINTER(_int)], _int),
     "gla_plan_bucket_config": ([_vp, _int, C.POINTER(_int), C.POINTER(_int), C.POINTER(_int), C.POINTER(_int)], _int),
+    "gla_numnegevals": ([_i64, _vp, _vp, _i64, _vp, _vp, _vp], _int),
+    "gla_dstebz": ([_i64, _vp, _vp, _i64, _i64, _d, _vp, _vp], _int),
+    "gla_numnegevals_host": ([_i64, _vp, _vp, _i64, _vp, _vp], _int),
+    "gla_dstebz_host": ([_i64, _vp, _vp, _i64, _i64, _d, _vp], _int),
     "gla_status_string": ([_int], C.c_char_p),
     "gla_plan_create": ([C.POINTER(_vp), _int, _ch, _ch, _i64, C.POINTER(_i64), _d, _int], _int),
     "gla_plan_destroy": ([_vp], _int),

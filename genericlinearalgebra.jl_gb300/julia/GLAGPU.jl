@@ -187,4 +187,35 @@ function eigen_adjoint(E::LinearAlgebra.Eigen, wbar, Vbar; gap_rel = 0.0)
     return reshape(Abar[1:n*n], n, n)
 end
 
+# numnegevals (src/tridiag.jl:20-36): the number of negative eigenvalues of
+# T - sigma I, bit-identical to the reference's recurrence; many shifts at once.
+function numnegevals(T::SymTridiagonal{Float64}, sigma::Real = 0.0)
+    return numnegevals(T, Float64[sigma])[1]
+end
+function numnegevals(T::SymTridiagonal{Float64}, sigmas::AbstractVector{<:Real})
+    s = Vector{Float64}(sigmas)
+    counts = Vector{Int64}(undef, length(s))
+    check(ccall((:gla_numnegevals_host, libglagpu), Cint,
+                (Int64, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Int64}),
+                length(T.dv), Vector{Float64}(T.dv), Vector{Float64}(T.ev), length(s), s, counts))
+    return counts
+end
+
+# eigvals(T, il:iu) and eigvals(T, vl, vu) (LinearAlgebra's subset methods)
+# by Sturm-count multisection on the GPU.
+function eigvals(T::SymTridiagonal{Float64}, irange::UnitRange; abstol = 0.0)
+    n = length(T.dv)
+    il, iu = first(irange), last(irange)
+    w = Vector{Float64}(undef, max(iu - il + 1, 0))
+    check(ccall((:gla_dstebz_host, libglagpu), Cint,
+                (Int64, Ptr{Float64}, Ptr{Float64}, Int64, Int64, Cdouble, Ptr{Float64}),
+                n, Vector{Float64}(T.dv), Vector{Float64}(T.ev), il, iu, Float64(abstol), w))
+    return w
+end
+function eigvals(T::SymTridiagonal{Float64}, vl::Real, vu::Real; abstol = 0.0)
+    il = numnegevals(T, vl) + 1
+    iu = numnegevals(T, vu)
+    return iu < il ? Float64[] : eigvals(T, il:iu; abstol)
+end
+
 end # module

@@ -242,6 +242,24 @@ int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz
               void* stream);
 
 /*
+ * Spectrum slicing on SymTridiagonal(d, e) (d: n, e: n-1; device pointers;
+ * asynchronous on `stream`):
+ *   gla_numnegevals: counts[i] = the number of negative eigenvalues of
+ *     T - sigma[i] I, the reference's numnegevals (src/tridiag.jl:20-36) with
+ *     its exact operation order (bit-identical counts);
+ *   gla_dstebz: w[0 .. iu-il] = the eigenvalues il..iu (1-based, ascending)
+ *     by Sturm-count multisection, each to max(abstol, 2 eps |lambda|).
+ */
+int gla_numnegevals(int64_t n, const double* d, const double* e, int64_t m, const double* sigma, int64_t* counts,
+                    void* stream);
+int gla_dstebz(int64_t n, const double* d, const double* e, int64_t il, int64_t iu, double abstol, double* w,
+               void* stream);
+/* Same, from and to host buffers (synchronous). */
+int gla_numnegevals_host(int64_t n, const double* d, const double* e, int64_t m, const double* sigma,
+                         int64_t* counts);
+int gla_dstebz_host(int64_t n, const double* d, const double* e, int64_t il, int64_t iu, double abstol, double* w);
+
+/*
  * Autotune table (GLA_FLAG_AUTOTUNE): drop every entry; write the entries to
  * a text file; merge the entries of such a file (returns how many were
  * loaded, <0 when the file cannot be read).

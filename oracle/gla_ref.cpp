@@ -173,4 +173,10 @@ int gla_oracle_syev_batched_s(char jobz, char uplo, int64_t batch, const int64_t
 
 int gla_oracle_max_threads(void) { return omp_get_max_threads(); }
 
+// Sturm counts for m shifts (src/tridiag.jl:20-36).
+void gla_oracle_numnegevals_d(int64_t n, const double* a, const double* b, int64_t m, const double* sigma,
+                              int64_t* counts) {
+  for (int64_t i = 0; i < m; i++) counts[i] = numnegevals(a, b, n, sigma[i]);
+}
+
 }  // extern "C"

@@ -710,4 +710,24 @@ template <class T> int stev(Opts<T>& o, char jobz, int64_t n, T* d, T* e, T* V, 
   return info;
 }
 
+// numnegevals (src/tridiag.jl:20-36): the number of negative eigenvalues of
+// T - sigma I by the LDL' (Sturm) recurrence of Parlett, "The symmetric
+// eigenvalue problem", 3.3.1: delta_1 = a_1 - sigma,
+// delta_{k+1} = (a_{k+1} - sigma) - b_k (b_k / delta_k), counting the
+// negative deltas; a zero delta is replaced by eps (b_k + eps) as the
+// reference does. Evaluated in exactly this operation order (the oracle is
+// built without contraction).
+template <class T> int64_t numnegevals(const T* a, const T* b, int64_t n, T sigma) {
+  if (n <= 0) return 0;
+  const T eps = num<T>::eps();
+  T delta = a[0] - sigma;
+  int64_t nu = delta < T(0) ? 1 : 0;
+  for (int64_t k = 0; k + 1 < n; k++) {
+    if (delta == T(0)) delta = eps * (b[k] + eps);
+    delta = (a[k + 1] - sigma) - b[k] * (b[k] / delta);
+    nu += delta < T(0) ? 1 : 0;
+  }
+  return nu;
+}
+
 }  // namespace gla_oracle

@@ -58,6 +58,8 @@ def lib():
         L.gla_oracle_syev_batched_d.argtypes = [_ch, _ch, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _int]
         L.gla_oracle_syev_batched_s.argtypes = [_ch, _ch, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _f, _int]
         L.gla_oracle_max_threads.argtypes = []
+        L.gla_oracle_numnegevals_d.argtypes = [_i64, _vp, _vp, _i64, _vp, _vp]
+        L.gla_oracle_numnegevals_d.restype = None
         _lib = L
     return _lib
 
@@ -218,6 +220,17 @@ def batched_raw(jobz, uplo, ns, aoff, A, w, woff, V, info, dtype=np.float64, nth
     fn = lib().gla_oracle_syev_batched_d if dtype == np.float64 else lib().gla_oracle_syev_batched_s
     return fn(jobz.encode(), uplo.encode(), len(ns), _p(ns), _p(aoff), _p(A), _p(w), _p(woff),
               _p(V) if V is not None else None, _p(info), 0.0, nthreads)
+
+
+def numnegevals(d, e, sigma=0.0):
+    """numnegevals(SymTridiagonal(d, e), sigma) (src/tridiag.jl:20-36); sigma
+    may be a scalar or an array of shifts (one count per shift)."""
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    sig = np.atleast_1d(np.ascontiguousarray(sigma, dtype=np.float64))
+    out = np.zeros(len(sig), dtype=np.int64)
+    lib().gla_oracle_numnegevals_d(len(d), _p(d), _p(e), len(sig), _p(sig), _p(out))
+    return int(out[0]) if np.ndim(sigma) == 0 else out
 
 
 def max_threads():

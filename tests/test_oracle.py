@@ -183,3 +183,23 @@ def test_batched_matches_single():
         w1, V1, _ = O.syev(A)
         assert np.array_equal(w, w1) and np.array_equal(V, V1)
     assert (info == 0).all()
+
+
+def test_numnegevals_reference_case():
+    # test/tridiag.jl:3-7: numnegevals(T) == count(x -> x < 0, eigvals(T)), n = 20
+    for seed in range(5):
+        rng = np.random.default_rng(seed)
+        d, e = rng.standard_normal(20), rng.standard_normal(19)
+        T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+        w = np.linalg.eigvalsh(T)
+        assert O.numnegevals(d, e) == int((w < 0).sum())
+        # shifted counts match the sorted spectrum away from the eigenvalues
+        mids = (w[:-1] + w[1:]) / 2
+        assert list(O.numnegevals(d, e, mids)) == list(range(1, 20))
+
+
+def test_numnegevals_zero_pivot_rule():
+    # a zero pivot is replaced by eps (b_k + eps) (src/tridiag.jl:29-32):
+    # T = [[0, 1], [1, 0]] at sigma = 0 has delta_1 = 0
+    d, e = np.array([0.0, 0.0]), np.array([1.0])
+    assert O.numnegevals(d, e, 0.0) == 1  # eigenvalues -1, 1
