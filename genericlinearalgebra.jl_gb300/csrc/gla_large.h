@@ -95,8 +95,9 @@ size_t dc_plan_bytes(const DcPlan* p);
 struct BacktrPlan;
 int backtr_plan_create(BacktrPlan** out, int n, bool f64);
 void backtr_plan_destroy(BacktrPlan* p);
+// Z := Q Z, or Q' Z when trans, for Z of ncol columns (-1: n).
 int backtr_enqueue(BacktrPlan* p, const void* A, long long lda, const void* tau, void* Z, long long ldz,
-                   cudaStream_t st);
+                   cudaStream_t st, int ncol = -1, bool trans = false);
 
 // ---- large-path context: workspace for one order n and one working precision
 struct LargeCtx;
@@ -111,12 +112,15 @@ void large_stage_ms(const LargeCtx* c, float* ms3);
 // dimension lda, working precision), in place: d, e, tau and the reflectors
 // below the subdiagonal (symtri! layout, unit element implicit).
 int large_sytrd(LargeCtx* c, void* A, long long lda, void* d, void* e, void* tau, cudaStream_t st);
+// The context's n x n working matrix (leading dimension n).
+void* large_work_matrix(LargeCtx* c);
 // Eigenpairs of the symmetric tridiagonal (d, e): d becomes the ascending
 // eigenvalues, Z (ldz) the eigenvectors. info: 0, or > 0 if a subproblem
 // did not converge.
 int large_stedc(LargeCtx* c, void* d, const void* e, void* Z, long long ldz, int* info, cudaStream_t st);
 // Z := Q Z with Q = H_0 H_1 ... H_{n-2} from large_sytrd.
-int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void* Z, long long ldz, cudaStream_t st);
+int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void* Z, long long ldz, cudaStream_t st,
+                int ncol = -1, bool trans = false);
 // Full eigen-decomposition of one matrix. tcode: kF64, kF32 or kF32FromF64
 // (double input solved in FP32; outputs float). Ain has leading dimension
 // lda and uplo 'L'/'U'; w gets the ascending eigenvalues, V (ldv) the

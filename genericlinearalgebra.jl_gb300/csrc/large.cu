@@ -177,6 +177,8 @@ void large_destroy(LargeCtx* c) {
   delete c;
 }
 
+void* large_work_matrix(LargeCtx* c) { return c->Aw; }
+
 void large_stage_ms(const LargeCtx* c, float* ms3) {
   for (int i = 0; i < 3; i++) ms3[i] = c->ms[i];
 }
@@ -196,8 +198,9 @@ int large_stedc(LargeCtx* c, void* d, const void* e, void* Z, long long ldz, int
   return dc_enqueue(c->dc, d, e, Z, info, st);
 }
 
-int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void* Z, long long ldz, cudaStream_t st) {
-  return backtr_enqueue(c->bt, A, lda, tau, Z, ldz, st);
+int large_ormtr(LargeCtx* c, const void* A, long long lda, const void* tau, void* Z, long long ldz, cudaStream_t st,
+                int ncol, bool trans) {
+  return backtr_enqueue(c->bt, A, lda, tau, Z, ldz, st, ncol, trans);
 }
 
 int large_syev(LargeCtx* c, int tcode, bool wantv, bool lower, const void* Ain, long long lda, void* w, void* V,

@@ -92,10 +92,12 @@ __global__ void __launch_bounds__(256) k_larft(const T* __restrict__ Y, const T*
   for (int idx = tid; idx < kBT * kBT; idx += 256) Tb[idx] = Ts[idx % kBT][idx / kBT];
 }
 
-// W2 = T * sum_s Wpart_s   (W is kb x ncol, partials of leading dimension kb)
+// W2 = op(T) * sum_s Wpart_s   (W is kb x ncol, partials of leading dimension
+// kb; op(T) = T, or T' when trans)
 template <class T>
 __global__ void __launch_bounds__(256) k_tw(const T* __restrict__ Wp, int splits, long long pstride,
-                                            const T* __restrict__ Tb, T* __restrict__ W2, int kb, int ncol) {
+                                            const T* __restrict__ Tb, T* __restrict__ W2, int kb, int ncol,
+                                            int trans) {
   constexpr int kC = 16;  // columns per CTA
   __shared__ T Ts[kBT][kBT + 1];
   __shared__ T ws[kBT][kC + 1];
@@ -113,7 +115,10 @@ __global__ void __launch_bounds__(256) k_tw(const T* __restrict__ Wp, int splits
     const int i = idx % kBT, c = idx / kBT;
     if (i >= kb || c0 + c >= ncol) continue;
     T s = T(0);
-    for (int q = i; q < kb; q++) s = fma(Ts[i][q], ws[q][c], s);
+    if (trans)
+      for (int q = 0; q <= i; q++) s = fma(Ts[q][i], ws[q][c], s);
+    else
+      for (int q = i; q < kb; q++) s = fma(Ts[i][q], ws[q][c], s);
     W2[i + (long long)(c0 + c) * kb] = s;
   }
 }
@@ -169,10 +174,15 @@ void backtr_plan_destroy(BacktrPlan* p) {
   delete p;
 }
 
+// Z := Q Z (trans: Q' Z) for Z with ncol columns, in chunks of at most n
+// columns (the W buffers' width). Q = B_0 B_1 ... with the blocks
+// B_b = I - Y_b T_b Y_b': Q Z applies the last block first, Q' Z applies
+// B_0' = I - Y_0 T_0' Y_0' first.
 template <class T>
-int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, long long ldz, cudaStream_t st) {
+int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Zall, long long ldz, int ncol, bool trans,
+               cudaStream_t st) {
   const int n = p.n;
-  if (n < 2) return 0;
+  if (n < 2 || ncol <= 0) return 0;
   T* Y = (T*)p.Y;
   k_form_y<T><<<dim3((n + 255) / 256, n), 256, 0, st>>>(A, lda, Y, n);
   cudaError_t err = cudaGetLastError();
@@ -181,7 +191,11 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, lon
   if ((err = cudaGetLastError()) != cudaSuccess) return -1000 - (int)err;
   const bool f64 = sizeof(T) == 8;
   const int bk = f64 ? GemmCfg<double>::BK : GemmCfg<float>::BK;
-  for (int b = p.nblk - 1; b >= 0; b--) {
+  for (int c0 = 0; c0 < ncol; c0 += n) {
+  const int nc = std::min(n, ncol - c0);
+  T* Z = Zall + (long long)c0 * ldz;
+  for (int bi = 0; bi < p.nblk; bi++) {
+    const int b = trans ? bi : p.nblk - 1 - bi;
     const int j0 = b * kBT, kb = std::min(kBT, n - 1 - j0);
     // rows from r0 (j0 + 1 rounded down to a 16-byte boundary: Y is zero
     // above its unit diagonal, so the extra rows add nothing) keep Z's
@@ -191,7 +205,7 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, lon
     // W = Y_b' Z[r0:, :]
     GemmDesc g{};
     g.m = kb;
-    g.n = n;
+    g.n = nc;
     g.k = mrows;
     g.A = Y + r0 + (long long)j0 * n;
     g.lda = n;
@@ -206,13 +220,14 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, lon
     if (splits > 1) splits = (mrows + g.ksplit - 1) / g.ksplit;
     g.split_stride = (long long)kb * n;
     if ((err = gemm_launch(f64, true, false, false, g, splits, st)) != cudaSuccess) return -1000 - (int)err;
-    k_tw<T><<<(n + 15) / 16, 256, 0, st>>>((const T*)p.Wp, splits, (long long)kb * n, (const T*)p.Tm + (long long)b * kBT * kBT,
-                                           (T*)p.W2, kb, n);
+    k_tw<T><<<(nc + 15) / 16, 256, 0, st>>>((const T*)p.Wp, splits, (long long)kb * n,
+                                            (const T*)p.Tm + (long long)b * kBT * kBT, (T*)p.W2, kb, nc,
+                                            trans ? 1 : 0);
     if ((err = cudaGetLastError()) != cudaSuccess) return -1000 - (int)err;
     // Z[r0:, :] -= Y_b W2
     GemmDesc h{};
     h.m = mrows;
-    h.n = n;
+    h.n = nc;
     h.k = kb;
     h.A = Y + r0 + (long long)j0 * n;
     h.lda = n;
@@ -224,13 +239,16 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Z, lon
     h.beta = 1.0;
     if ((err = gemm_launch(f64, false, false, false, h, 1, st)) != cudaSuccess) return -1000 - (int)err;
   }
+  }
   return 0;
 }
 
 int backtr_enqueue(BacktrPlan* p, const void* A, long long lda, const void* tau, void* Z, long long ldz,
-                   cudaStream_t st) {
-  if (p->f64) return backtr_run<double>(*p, (const double*)A, lda, (const double*)tau, (double*)Z, ldz, st);
-  return backtr_run<float>(*p, (const float*)A, lda, (const float*)tau, (float*)Z, ldz, st);
+                   cudaStream_t st, int ncol, bool trans) {
+  if (ncol < 0) ncol = p->n;
+  if (p->f64)
+    return backtr_run<double>(*p, (const double*)A, lda, (const double*)tau, (double*)Z, ldz, ncol, trans, st);
+  return backtr_run<float>(*p, (const float*)A, lda, (const float*)tau, (float*)Z, ldz, ncol, trans, st);
 }
 
 }  // namespace gla

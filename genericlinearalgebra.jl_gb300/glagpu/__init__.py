@@ -393,6 +393,69 @@ def _tridiag_dev(T):
     return d, e, on_dev, dev
 
 
+class EigenQ:
+    """The orthogonal factor of symtri (src/eigenSelfAdjoint.jl:6-21): Householder
+    reflectors stored in `factors` (the reference's symtriLower! layout; a torch
+    CUDA float64 tensor, n x n) with scalars `tau`. lmul(B) = Q B and
+    rmul(B) = B Q (lmul!/rmul!, :23-99), array() = Q (Array(::EigenQ), :101);
+    the trans forms apply Q'."""
+
+    def __init__(self, factors, tau):
+        self.factors = factors
+        self.tau = tau
+        self.n = factors.shape[0]
+
+    def _apply(self, side, trans, B):
+        torch = _torch()
+        on_dev = _is_torch(B)
+        X = (B.to(torch.float64) if on_dev else torch.as_tensor(np.asarray(B, dtype=np.float64), device="cuda"))
+        if X.dim() != 2:
+            raise DimensionMismatch("B must be a matrix")
+        m, k = X.shape
+        if (side == "L" and m != self.n) or (side == "R" and k != self.n):
+            raise DimensionMismatch(f"Q has order {self.n}, B is {m} x {k}")
+        Xc = X.t().contiguous().clone()  # column-major storage of X
+        F = self.factors.t().contiguous()
+        _lib.check(_lib.load().gla_dormtr(side.encode(), trans.encode(), m, k, C.c_void_p(F.data_ptr()), self.n,
+                                          C.c_void_p(self.tau.data_ptr()), C.c_void_p(Xc.data_ptr()), max(m, 1),
+                                          _stream_ptr()), "gla_dormtr")
+        out = Xc.t()
+        return out if on_dev else out.cpu().numpy()
+
+    def lmul(self, B, trans=False):
+        return self._apply("L", "T" if trans else "N", B)
+
+    def rmul(self, B, trans=False):
+        return self._apply("R", "T" if trans else "N", B)
+
+    def array(self):
+        torch = _torch()
+        return self.lmul(torch.eye(self.n, dtype=torch.float64, device="cuda"))
+
+
+SymmetricTridiagonalFactorization = namedtuple("SymmetricTridiagonalFactorization", ["reflectors", "diagonals"])
+
+
+def symtri(A, uplo="L"):
+    """symtri!(Hermitian(A, uplo)) (src/eigenSelfAdjoint.jl:446-504) on the GPU:
+    A = Q T Q'. Returns SymmetricTridiagonalFactorization(EigenQ, SymTridiagonal)
+    with device tensors; the factors follow symtriLower!'s layout (an upper
+    input is factored as its symmetric lower counterpart)."""
+    torch = _torch()
+    X = A.to(torch.float64) if _is_torch(A) else torch.as_tensor(np.asarray(A, dtype=np.float64), device="cuda")
+    n = X.shape[0]
+    if X.dim() != 2 or X.shape[1] != n:
+        raise DimensionMismatch("A must be square")
+    F = X.t().contiguous().clone()  # column-major working storage
+    d = torch.empty(max(n, 1), dtype=torch.float64, device=X.device)
+    e = torch.empty(max(n - 1, 1), dtype=torch.float64, device=X.device)
+    tau = torch.empty(max(n - 1, 1), dtype=torch.float64, device=X.device)
+    _lib.check(_lib.load().gla_dsytrd(uplo.encode(), n, C.c_void_p(F.data_ptr()), max(n, 1), C.c_void_p(d.data_ptr()),
+                                      C.c_void_p(e.data_ptr()), C.c_void_p(tau.data_ptr()), _stream_ptr()),
+               "gla_dsytrd")
+    return SymmetricTridiagonalFactorization(EigenQ(F.t(), tau), SymTridiagonal(d[:n], e[:max(n - 1, 0)]))
+
+
 def numnegevals(T, sigma=0.0):
     """numnegevals(T::SymTridiagonal, sigma) (src/tridiag.jl:20-36): the number
     of negative eigenvalues of T - sigma I. sigma may be an array of shifts
@@ -468,5 +531,6 @@ def autotune_load(path):
 
 
 __all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigen2", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
-           "autotune_clear", "autotune_save", "autotune_load", "numnegevals",
+           "autotune_clear", "autotune_save", "autotune_load", "numnegevals", "symtri", "EigenQ",
+           "SymmetricTridiagonalFactorization",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

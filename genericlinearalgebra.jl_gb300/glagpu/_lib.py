@@ -46,6 +46,10 @@ SIGNATURES = {
     "gla_dstebz": ([_i64, _vp, _vp, _i64, _i64, _d, _vp, _vp], _int),
     "gla_numnegevals_host": ([_i64, _vp, _vp, _i64, _vp, _vp], _int),
     "gla_dstebz_host": ([_i64, _vp, _vp, _i64, _i64, _d, _vp], _int),
+    "gla_dsytrd": ([_ch, _i64, _vp, _i64, _vp, _vp, _vp, _vp], _int),
+    "gla_dormtr": ([_ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp], _int),
+    "gla_dsytrd_host": ([_ch, _i64, _vp, _i64, _vp, _vp, _vp], _int),
+    "gla_dormtr_host": ([_ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64], _int),
     "gla_status_string": ([_int], C.c_char_p),
     "gla_plan_create": ([C.POINTER(_vp), _int, _ch, _ch, _i64, C.POINTER(_i64), _d, _int], _int),
     "gla_plan_destroy": ([_vp], _int),

@@ -187,6 +187,40 @@ function eigen_adjoint(E::LinearAlgebra.Eigen, wbar, Vbar; gap_rel = 0.0)
     return reshape(Abar[1:n*n], n, n)
 end
 
+# symtri! (src/eigenSelfAdjoint.jl:446-504) on the GPU: the factorisation in
+# symtriLower!'s layout, with an EigenQ whose lmul!/rmul! (:23-99) and Array
+# (:101) run on the device (gla_dsytrd_host / gla_dormtr_host).
+struct GPUEigenQ
+    factors::Matrix{Float64}
+    tau::Vector{Float64}
+end
+struct GPUSymmetricTridiagonalFactorization
+    reflectors::GPUEigenQ
+    diagonals::SymTridiagonal{Float64,Vector{Float64}}
+end
+
+function symtri!(A::Union{Hermitian{Float64,Matrix{Float64}},Symmetric{Float64,Matrix{Float64}}})
+    n = size(A, 1)
+    d = Vector{Float64}(undef, n)
+    e = Vector{Float64}(undef, max(n - 1, 0))
+    tau = Vector{Float64}(undef, max(n - 1, 0))
+    check(ccall((:gla_dsytrd_host, libglagpu), Cint,
+                (UInt8, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                UInt8(uplochar(A)), n, A.data, max(n, 1), d, e, tau))
+    return GPUSymmetricTridiagonalFactorization(GPUEigenQ(A.data, tau), SymTridiagonal(d, e))
+end
+
+function _ormtr!(side::Char, trans::Char, Q::GPUEigenQ, B::Matrix{Float64})
+    m, k = size(B)
+    check(ccall((:gla_dormtr_host, libglagpu), Cint,
+                (UInt8, UInt8, Int64, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Int64),
+                UInt8(side), UInt8(trans), m, k, Q.factors, max(size(Q.factors, 1), 1), Q.tau, B, max(m, 1)))
+    return B
+end
+lmul!(Q::GPUEigenQ, B::Matrix{Float64}) = _ormtr!('L', 'N', Q, B)
+rmul!(B::Matrix{Float64}, Q::GPUEigenQ) = _ormtr!('R', 'N', Q, B)
+Base.Array(Q::GPUEigenQ) = lmul!(Q, Matrix{Float64}(I, size(Q.factors)...))
+
 # numnegevals (src/tridiag.jl:20-36): the number of negative eigenvalues of
 # T - sigma I, bit-identical to the reference's recurrence; many shifts at once.
 function numnegevals(T::SymTridiagonal{Float64}, sigma::Real = 0.0)
