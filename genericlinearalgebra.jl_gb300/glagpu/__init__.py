@@ -360,11 +360,46 @@ def eigh_autograd(A, plan):
     return _eigh_fn.apply(A, plan)
 
 
+def _is_complex(A):
+    if _is_torch(A):
+        return A.is_complex()
+    return np.iscomplexobj(A)
+
+
+def _zheev(A, jobz, uplo):
+    """Complex Hermitian input through gla_zheev (FP64 only)."""
+    torch = _torch()
+    on_dev = _is_torch(A)
+    X = A.to(torch.complex128) if on_dev else torch.as_tensor(np.asarray(A, dtype=np.complex128), device="cuda")
+    n = X.shape[0]
+    if X.dim() != 2 or X.shape[1] != n:
+        raise DimensionMismatch("A must be square")
+    Xc = X.t().contiguous()  # column-major, interleaved (re, im)
+    w = torch.empty(max(n, 1), dtype=torch.float64, device=X.device)
+    V = torch.empty((max(n, 1), max(n, 1)), dtype=torch.complex128, device=X.device) if jobz == "V" else None
+    info = C.c_int()
+    rc = _lib.load().gla_zheev(jobz.encode(), uplo.encode(), n, C.c_void_p(Xc.data_ptr()), max(n, 1),
+                               C.c_void_p(w.data_ptr()), C.c_void_p(V.data_ptr()) if V is not None else None,
+                               max(n, 1), C.byref(info), _stream_ptr())
+    _lib.check(rc, "gla_zheev")
+    _raise_for_info([info.value])
+    w = w[:n]
+    if jobz == "V":
+        Vt = V[:n, :n].t()  # column-major buffer -> row-major view
+        return Eigen(w, Vt) if on_dev else Eigen(w.cpu().numpy(), Vt.cpu().numpy())
+    return w if on_dev else w.cpu().numpy()
+
+
 def eigen(A, uplo="L", tol=None, precision="f64", alg="QL"):
     """eigen(Hermitian(A, uplo)) / eigen(SymTridiagonal): ascending values and
-    the matching orthonormal eigenvectors (columns)."""
+    the matching orthonormal eigenvectors (columns). Complex input is a
+    complex Hermitian matrix (FP64, gla_zheev)."""
     if isinstance(A, SymTridiagonal):
         return _tridiag(A, "V", alg, tol)
+    if _is_complex(A):
+        if precision != "f64" or tol is not None:
+            raise ValueError("complex Hermitian input: FP64 with the default tolerance only")
+        return _zheev(A, "V", uplo)
     return eigen_batched([A], uplo=uplo, tol=tol, precision=precision, alg=alg)[0]
 
 
@@ -379,6 +414,10 @@ def eigvals(A, uplo="L", tol=None, precision="f64", irange=None, vl=None, vu=Non
         return _tridiag(A, "N", "QL", tol)
     if irange is not None or vl is not None or vu is not None:
         raise ValueError("eigenvalue subsets are available for SymTridiagonal input")
+    if _is_complex(A):
+        if precision != "f64" or tol is not None:
+            raise ValueError("complex Hermitian input: FP64 with the default tolerance only")
+        return _zheev(A, "N", uplo)
     return eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
 
 

@@ -187,6 +187,32 @@ function eigen_adjoint(E::LinearAlgebra.Eigen, wbar, Vbar; gap_rel = 0.0)
     return reshape(Abar[1:n*n], n, n)
 end
 
+# eigen!/eigvals! on Hermitian{ComplexF64} (the reference's complex
+# Hermitian support, loop bound :462), through gla_zheev_host (the real
+# symmetric embedding of order 2n on the GPU).
+function eigen!(A::Hermitian{ComplexF64,Matrix{ComplexF64}}; tol = eps(Float64), sortby = LinearAlgebra.eigsortby,
+                alg = nothing)
+    n = size(A, 1)
+    w = Vector{Float64}(undef, n)
+    V = Matrix{ComplexF64}(undef, n, n)
+    info = Ref{Cint}(0)
+    check(ccall((:gla_zheev_host, libglagpu), Cint,
+                (UInt8, UInt8, Int64, Ptr{ComplexF64}, Int64, Ptr{Float64}, Ptr{ComplexF64}, Int64, Ref{Cint}),
+                UInt8('V'), UInt8(uplochar(A)), n, A.data, max(n, 1), w, V, max(n, 1), info))
+    raise_info(Cint[info[]])
+    return LinearAlgebra.Eigen(w, V)
+end
+function eigvals!(A::Hermitian{ComplexF64,Matrix{ComplexF64}}; tol = eps(Float64), sortby = LinearAlgebra.eigsortby)
+    n = size(A, 1)
+    w = Vector{Float64}(undef, n)
+    info = Ref{Cint}(0)
+    check(ccall((:gla_zheev_host, libglagpu), Cint,
+                (UInt8, UInt8, Int64, Ptr{ComplexF64}, Int64, Ptr{Float64}, Ptr{ComplexF64}, Int64, Ref{Cint}),
+                UInt8('N'), UInt8(uplochar(A)), n, A.data, max(n, 1), w, C_NULL, max(n, 1), info))
+    raise_info(Cint[info[]])
+    return w
+end
+
 # symtri! (src/eigenSelfAdjoint.jl:446-504) on the GPU: the factorisation in
 # symtriLower!'s layout, with an EigenQ whose lmul!/rmul! (:23-99) and Array
 # (:101) run on the device (gla_dsytrd_host / gla_dormtr_host).

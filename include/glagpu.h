@@ -242,6 +242,22 @@ int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz
               void* stream);
 
 /*
+ * Complex Hermitian eigenproblem (the reference's eigen!/eigvals! on
+ * Hermitian{<:Complex}): A is n x n complex, interleaved (re, im) doubles,
+ * column-major with leading dimension lda (in complex elements); only the
+ * uplo triangle is read (a diagonal's imaginary part is ignored). w: n
+ * ascending eigenvalues; V (jobz 'V'): n x n complex orthonormal eigenvectors,
+ * interleaved, leading dimension ldv. Device pointers; synchronizes. Solved
+ * through the real symmetric embedding [[B, -C], [C, B]] of order 2n
+ * (2n <= GLA_MAX_N). Status and info as for gla_dsyev.
+ */
+int gla_zheev(char jobz, char uplo, int64_t n, const double* A, int64_t lda, double* w, double* V, int64_t ldv,
+              int* info, void* stream);
+/* Same, from and to host buffers. */
+int gla_zheev_host(char jobz, char uplo, int64_t n, const double* A, int64_t lda, double* w, double* V, int64_t ldv,
+                   int* info);
+
+/*
  * The Householder factorisation on its own (the reference's symtri! /
  * SymmetricTridiagonalFactorization and lmul!/rmul! with its EigenQ,
  * src/eigenSelfAdjoint.jl:6-118, 446-504; FP64, device pointers,
