@@ -56,6 +56,7 @@ namespace gla {
 
 constexpr int kRefMaxIters = 10;
 constexpr int kWin = 32;
+constexpr int kOzRotateMin = 64;  // cluster rotations of at least this many columns on the tensor cores
 constexpr float kTheta = 0.05f;
 constexpr double kResTheta = 0.1;
 
@@ -585,7 +586,10 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       // perturbation removed quadratically); the polishing iteration, the
       // last, forms X E in double-float on the tensor cores (A operand: the
       // rows of X; B operand: E, in the slot of X's slices, unused from here)
-      if (polish) {
+      // unless the corrections of the iteration before were below 1e-8: the
+      // polish's then are smaller still, and the FP32-accuracy product's
+      // rounding, ~6e-8 |E|, stays below 1e-15
+      if (polish && !(emax_prev < 1e-8)) {
         RF_CUDA(oz_slice_rows(r->ozx, r->Xhi, r->Xlo, n, n, n, 7, st));
         RF_CUDA(oz_slice(r->oz, false, r->E, nullptr, n, n, n, 7, st));
         RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Phi, r->Plo, n, false, st));
@@ -636,6 +640,16 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
         int rc = solve_clusters(r, rs, rcnt, roff, st);
         if (rc) return rc;
         for (size_t k = 0; k < rs.size(); k++) {
+          if (rcnt[k] >= kOzRotateMin) {
+            // X_J W on the tensor cores in double-float (A operand: the rows
+            // of X_J in the Gram's slot, B operand: W in X's slot; both are
+            // free once E is formed, and X is sliced anew next iteration)
+            RF_CUDA(oz_slice_rows(r->ozx, r->Xhi + (long long)rs[k] * n, r->Xlo + (long long)rs[k] * n, n, n,
+                                  rcnt[k], 7, st));
+            RF_CUDA(oz_slice(r->oz, false, r->Wbuf + roff[k], nullptr, rcnt[k], rcnt[k], rcnt[k], 7, st));
+            RF_CUDA(oz_gemm2(r->ozx, r->oz, n, rcnt[k], rcnt[k], r->Phi + (long long)rs[k] * n,
+                             r->Plo + (long long)rs[k] * n, n, false, st));
+          } else {
           DfGemmDesc gr{};
           gr.m = n;
           gr.n = rcnt[k];
@@ -650,6 +664,7 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
           gr.Clo = r->Plo + (long long)rs[k] * n;
           gr.ldc = n;
           RF_CUDA(dfgemm_launch(gr, false, st));
+          }
           RF_CUDA(cudaMemcpyAsync(r->Xhi + (long long)rs[k] * n, r->Phi + (long long)rs[k] * n,
                                   sizeof(float) * n * rcnt[k], cudaMemcpyDeviceToDevice, st));
           RF_CUDA(cudaMemcpyAsync(r->Xlo + (long long)rs[k] * n, r->Plo + (long long)rs[k] * n,

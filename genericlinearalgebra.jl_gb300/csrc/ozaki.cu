@@ -15,6 +15,7 @@ namespace gla {
 struct OzWork {
   oz::Sliced A{}, B{};
   size_t abytes = 0, bbytes = 0;
+  int a_nks_cap = 0, b_nks_cap = 0;  // k slabs the buffers hold (the slicing sets the current count)
   int S = oz::kMaxSlices;  // slices per value of this configuration
   int* err = nullptr;
 };
@@ -56,6 +57,8 @@ int create(OzWork** out, int m, int n, int K, int S, int bn) {
   w->S = S;
   init_sliced(w->A, std::max(m, 1), K, oz::kBM);
   init_sliced(w->B, std::max(n, 1), K, bn);
+  w->a_nks_cap = w->A.nks;
+  w->b_nks_cap = w->B.nks;
   w->abytes = m > 0 ? sliced_bytes(m, K, oz::kBM, S) : 16;
   w->bbytes = n > 0 ? sliced_bytes(n, K, bn, S) : 16;
   cudaError_t e = cudaMalloc((void**)&w->A.base, w->abytes);
@@ -108,8 +111,11 @@ void oz_destroy(OzWork* w) {
 cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo, long long ld, int count, int len,
                      int S, cudaStream_t st) {
   oz::Sliced& s = a_operand ? w->A : w->B;
-  if (S != w->S || count > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks) return cudaErrorInvalidValue;
+  const int nks = std::max(1, (len + oz::kKS - 1) / oz::kKS);
+  if (S != w->S || count > s.nblk * s.H || nks > (a_operand ? w->a_nks_cap : w->b_nks_cap))
+    return cudaErrorInvalidValue;
   s.S = S;
+  s.nks = nks;
   const int rows_pad = s.nblk * s.H;
   oz::k_oz_rowmax_cols<<<(rows_pad + 7) / 8, 256, 0, st>>>(hi, ld, len, count, rows_pad, s.mbits);
   launch_tile<false>(S, hi, lo, ld, len, count, s, st);
@@ -119,8 +125,10 @@ cudaError_t oz_slice(OzWork* w, bool a_operand, const float* hi, const float* lo
 cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long ld, int rows, int len, int S,
                           cudaStream_t st) {
   oz::Sliced& s = w->A;
-  if (S != w->S || rows > s.nblk * s.H || (len + oz::kKS - 1) / oz::kKS > s.nks) return cudaErrorInvalidValue;
+  const int nks = std::max(1, (len + oz::kKS - 1) / oz::kKS);
+  if (S != w->S || rows > s.nblk * s.H || nks > w->a_nks_cap) return cudaErrorInvalidValue;
   s.S = S;
+  s.nks = nks;
   const int rows_pad = s.nblk * s.H;
   cudaError_t e = cudaMemsetAsync(s.mbits, 0, sizeof(unsigned) * rows_pad, st);
   if (e != cudaSuccess) return e;
@@ -132,7 +140,8 @@ cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long
 }
 
 bool oz_fits(const OzWork* w, int m, int n, int K) {
-  return w->A.nblk * w->A.H >= m && w->B.nblk * w->B.H >= n && w->A.nks == (K + oz::kKS - 1) / oz::kKS;
+  const int nks = std::max(1, (K + oz::kKS - 1) / oz::kKS);
+  return w->A.nblk * w->A.H >= m && w->B.nblk * w->B.H >= n && w->a_nks_cap >= nks && w->b_nks_cap >= nks;
 }
 
 cudaError_t oz_gemm(OzWork* w, int M, int N, int K, float* Chi, float* Clo, long long ldc, bool lower,
