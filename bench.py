@@ -774,6 +774,8 @@ def main():
     ap.add_argument("--nrange", default="", help="profiling: keep matrices with lo <= n <= hi, as 'lo,hi'")
     ap.add_argument("--no-large", action="store_true", help="skip the n = 4096 single-matrix section")
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch shapes instead of the autotuner's")
+    ap.add_argument("--c3-solve", action="store_true",
+                    help="profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix only")
     ap.add_argument("--ozaki", type=int, default=0,
                     help="profiling: time only the tensor-core double-float GEMM (gla_gemm_df) at this order")
     args = ap.parse_args()
@@ -783,6 +785,21 @@ def main():
         import torch
         import glagpu
         print(json.dumps(time_ozaki(torch, glagpu, "cuda", args.ozaki)), flush=True)
+        return
+    if args.c3_solve:
+        # profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix
+        import torch
+        import glagpu
+        A, lam = large_case("c3", 4096)
+        plan = glagpu.Plan([4096], precision="f32_refined")
+        Ad = plan.pack([A], device="cuda")
+        w = torch.empty(4096, dtype=torch.float64, device="cuda")
+        V = torch.empty(4096 * 4096, dtype=torch.float64, device="cuda")
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for _ in range(2):
+            plan.execute(Ad, w, V, info)
+        torch.cuda.synchronize()
+        print(json.dumps({"info": int(info.item()), "eig_err": float(np.abs(w.cpu().numpy() - lam).max())}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -998,7 +998,7 @@ int gla_dstev(char jobz, int64_t n, double* d, double* e, double* Z, int64_t ldz
 // The launch shapes of the two batched kernels whose best shape depends on
 // the order and on how many matrices share a bucket: threads per CTA of the
 // tridiagonalisation (1, 2 or 4 per row of the bucket's largest order, at
-// most 256) and matrices per warp of the chase (1, 2, 4, 8, 16 or 32 lanes).
+// most 256) and matrices per warp of the chase (4, 8, 16 or 32 lanes).
 // Plans created with GLA_FLAG_AUTOTUNE look each bucket up in a process-wide
 // table keyed by (precision family, jobz, 16-wide order range, log2 of the
 // bucket's matrix count); a missing entry is measured on the spot: probe
@@ -1109,7 +1109,10 @@ int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
       best.tri_mult = mult;
     }
   }
-  for (int lpw : {1, 2, 4, 8, 16, 32}) {
+  // 1 or 2 matrices per warp win a bucket's probe run alone but lose in a
+  // plan, where all buckets share the SMs: a warp pays its FP64 (and most
+  // FP32) issue slots for 32 lanes whatever the number active
+  for (int lpw : {4, 8, 16, 32}) {
     if (rc) break;
     float t = 0, c = 0;
     rc = tune_probe(prec, k.jobz, n, count, base_flags, best.tri_mult, lpw, A, w, V, info, &t, &c);

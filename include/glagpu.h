@@ -63,7 +63,7 @@ extern "C" {
  * is reported with info = -2 instead of being finished by extra passes. */
 #define GLA_FLAG_GRAPH 16
 /* Flag bit: choose each size bucket's launch shapes (threads per CTA of the
- * tridiagonalisation, 1-4 per row; matrices per warp of the chase, 1-32) from the process-wide
+ * tridiagonalisation, 1-4 per row; matrices per warp of the chase, 4-32) from the process-wide
  * autotune table; shapes missing from it are measured during plan creation
  * on synthetic matrices of the bucket's order and count (synchronizes the
  * device; a few seconds for a fresh table) and added. See gla_autotune_*. */

@@ -48,7 +48,7 @@ def test_autotuned_plan_configs_and_accuracy(G, precision):
     for c in cfgs:
         nt = max(32, (c["nmax"] + 31) // 32 * 32)
         assert c["nt_tri"] in {nt, min(256, 2 * nt), min(256, 4 * nt)}
-        assert c["lanes_per_warp"] in (1, 2, 4, 8, 16, 32)
+        assert c["lanes_per_warp"] in (4, 8, 16, 32)
     ws, Vs = solve(G, plan, mats)
     for A, w, V in zip(mats, ws, Vs):
         n = A.shape[0]
