@@ -774,6 +774,8 @@ def main():
     ap.add_argument("--nrange", default="", help="profiling: keep matrices with lo <= n <= hi, as 'lo,hi'")
     ap.add_argument("--no-large", action="store_true", help="skip the n = 4096 single-matrix section")
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch shapes instead of the autotuner's")
+    ap.add_argument("--solve", type=int, default=0,
+                    help="profiling: two solves of one GOE matrix of this order on the first of --paths")
     ap.add_argument("--c3-solve", action="store_true",
                     help="profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix only")
     ap.add_argument("--ozaki", type=int, default=0,
@@ -785,6 +787,25 @@ def main():
         import torch
         import glagpu
         print(json.dumps(time_ozaki(torch, glagpu, "cuda", args.ozaki)), flush=True)
+        return
+    if args.solve:
+        # profiling: two solves of one GOE matrix (seed 1) of order args.solve
+        # on the first path of --paths
+        import torch
+        import glagpu
+        from helpers import goe
+        prec = args.paths.split(",")[0]
+        n = args.solve
+        plan = glagpu.Plan([n], precision=prec)
+        dt = torch.float32 if prec == "f32" else torch.float64
+        Ad = plan.pack([goe(n, 1)], device="cuda").to(dt)
+        w = torch.empty(n, dtype=dt, device="cuda")
+        V = torch.empty(n * n, dtype=dt, device="cuda")
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for _ in range(2):
+            plan.execute(Ad, w, V, info)
+        torch.cuda.synchronize()
+        print(json.dumps({"n": n, "path": prec, "info": int(info.item())}), flush=True)
         return
     if args.c3_solve:
         # profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix
