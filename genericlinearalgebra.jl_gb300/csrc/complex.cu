@@ -96,8 +96,12 @@ __device__ double2 block_sum2(double2 v, double2* red) {
 
 // One CTA per group of 2k real eigenvectors (columns g0 .. g0 + 2k - 1 of E):
 // k orthonormal complex vectors into V[:, out0 .. out0 + k - 1] by modified
-// Gram-Schmidt (two passes) over the candidates in order, keeping those
-// whose residual norm exceeds 1/2. Scratch: n complex per CTA in r.
+// Gram-Schmidt (two passes) over the candidates in order. A first sweep
+// keeps candidates whose residual norm exceeds 1/2. Were it to end short (it
+// cannot for k < 4), a second sweep keeps those above 1/(2 sqrt k): the 2k
+// candidates are an orthonormal basis of the group's space, so with j < k
+// vectors kept their residuals' squares sum to 2 (k - j) and some
+// candidate's residual is at least 1/sqrt k. Scratch: n complex per CTA in r.
 __global__ void __launch_bounds__(256) k_zgroup(const double* __restrict__ E, int n, const int* __restrict__ g0s,
                                                 const int* __restrict__ ks, const int* __restrict__ outs,
                                                 double* __restrict__ V, long long ldv, double* __restrict__ scratch) {
@@ -108,47 +112,50 @@ __global__ void __launch_bounds__(256) k_zgroup(const double* __restrict__ E, in
   const long long n2 = 2LL * n;
   if (threadIdx.x == 0) kept_s = 0;
   __syncthreads();
-  for (int cand = 0; cand < 2 * k; cand++) {
-    if (kept_s >= k) break;
-    const long long s = g0 + cand;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      r[2 * i] = E[i + s * n2];
-      r[2 * i + 1] = E[(i + n) + s * n2];
-    }
-    __syncthreads();
-    const int kept = kept_s;
-    for (int pass = 0; pass < 2; pass++)
-      for (int q = 0; q < kept; q++) {
-        const double* vq = V + 2 * (out0 + q) * ldv;
-        // h = vq^H r
-        double2 h = make_double2(0.0, 0.0);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-          const double ar = vq[2 * i], ai = vq[2 * i + 1], br = r[2 * i], bi = r[2 * i + 1];
-          h.x += ar * br + ai * bi;
-          h.y += ar * bi - ai * br;
-        }
-        h = block_sum2(h, red);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-          const double ar = vq[2 * i], ai = vq[2 * i + 1];
-          r[2 * i] -= h.x * ar - h.y * ai;
-          r[2 * i + 1] -= h.x * ai + h.y * ar;
-        }
-        __syncthreads();
-      }
-    double2 nn = make_double2(0.0, 0.0);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) nn.x += r[2 * i] * r[2 * i] + r[2 * i + 1] * r[2 * i + 1];
-    nn = block_sum2(nn, red);
-    const double nrm = sqrt(nn.x);
-    if (nrm > 0.5) {
-      double* vo = V + 2 * (out0 + kept) * ldv;
+  for (int sweep = 0; sweep < 2; sweep++) {
+    const double thr = sweep == 0 ? 0.5 : 0.5 / sqrt((double)k);
+    for (int cand = 0; cand < 2 * k; cand++) {
+      if (kept_s >= k) break;
+      const long long s = g0 + cand;
       for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        vo[2 * i] = r[2 * i] / nrm;
-        vo[2 * i + 1] = r[2 * i + 1] / nrm;
+        r[2 * i] = E[i + s * n2];
+        r[2 * i + 1] = E[(i + n) + s * n2];
       }
       __syncthreads();
-      if (threadIdx.x == 0) kept_s = kept + 1;
+      const int kept = kept_s;
+      for (int pass = 0; pass < 2; pass++)
+        for (int q = 0; q < kept; q++) {
+          const double* vq = V + 2 * (out0 + q) * ldv;
+          // h = vq^H r
+          double2 h = make_double2(0.0, 0.0);
+          for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double ar = vq[2 * i], ai = vq[2 * i + 1], br = r[2 * i], bi = r[2 * i + 1];
+            h.x += ar * br + ai * bi;
+            h.y += ar * bi - ai * br;
+          }
+          h = block_sum2(h, red);
+          for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double ar = vq[2 * i], ai = vq[2 * i + 1];
+            r[2 * i] -= h.x * ar - h.y * ai;
+            r[2 * i + 1] -= h.x * ai + h.y * ar;
+          }
+          __syncthreads();
+        }
+      double2 nn = make_double2(0.0, 0.0);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) nn.x += r[2 * i] * r[2 * i] + r[2 * i + 1] * r[2 * i + 1];
+      nn = block_sum2(nn, red);
+      const double nrm = sqrt(nn.x);
+      if (nrm > thr) {
+        double* vo = V + 2 * (out0 + kept) * ldv;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+          vo[2 * i] = r[2 * i] / nrm;
+          vo[2 * i + 1] = r[2 * i + 1] / nrm;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) kept_s = kept + 1;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 

@@ -390,12 +390,53 @@ def _zheev(A, jobz, uplo):
     return w if on_dev else w.cpu().numpy()
 
 
+class QuaternionMatrix:
+    """A quaternion matrix as an (n, n, 4) float64 array or tensor of
+    components (s, i, j, k), the field order of Julia's Quaternion{Float64}:
+    eigen(QuaternionMatrix(A)) is the reference's eigen(Hermitian(A)) on
+    quaternion input. Its eigenvectors come back in the same (n, n, 4) form
+    (right eigenvectors, A v = v lambda)."""
+
+    def __init__(self, data):
+        if tuple(data.shape[2:]) != (4,) or len(data.shape) != 3 or data.shape[0] != data.shape[1]:
+            raise DimensionMismatch(f"a quaternion matrix is (n, n, 4), got {tuple(data.shape)}")
+        self.data = data
+
+
+def _qheev(Q, jobz, uplo):
+    """Quaternion Hermitian input through gla_qheev (FP64 only)."""
+    torch = _torch()
+    A = Q.data
+    on_dev = _is_torch(A)
+    X = A.to(torch.float64) if on_dev else torch.as_tensor(np.asarray(A, dtype=np.float64), device="cuda")
+    n = X.shape[0]
+    Xc = X.permute(1, 0, 2).contiguous()  # column-major, 4 doubles per entry
+    w = torch.empty(max(n, 1), dtype=torch.float64, device=X.device)
+    V = torch.empty((max(n, 1), max(n, 1), 4), dtype=torch.float64, device=X.device) if jobz == "V" else None
+    info = C.c_int()
+    rc = _lib.load().gla_qheev(jobz.encode(), uplo.encode(), n, C.c_void_p(Xc.data_ptr()), max(n, 1),
+                               C.c_void_p(w.data_ptr()), C.c_void_p(V.data_ptr()) if V is not None else None,
+                               max(n, 1), C.byref(info), _stream_ptr())
+    _lib.check(rc, "gla_qheev")
+    _raise_for_info([info.value])
+    w = w[:n]
+    if jobz == "V":
+        Vt = V[:n, :n].permute(1, 0, 2)  # column-major buffer -> (row, column, component)
+        return Eigen(w, Vt) if on_dev else Eigen(w.cpu().numpy(), Vt.cpu().numpy())
+    return w if on_dev else w.cpu().numpy()
+
+
 def eigen(A, uplo="L", tol=None, precision="f64", alg="QL"):
     """eigen(Hermitian(A, uplo)) / eigen(SymTridiagonal): ascending values and
     the matching orthonormal eigenvectors (columns). Complex input is a
-    complex Hermitian matrix (FP64, gla_zheev)."""
+    complex Hermitian matrix (FP64, gla_zheev); a QuaternionMatrix a
+    quaternion Hermitian one (FP64, gla_qheev)."""
     if isinstance(A, SymTridiagonal):
         return _tridiag(A, "V", alg, tol)
+    if isinstance(A, QuaternionMatrix):
+        if precision != "f64" or tol is not None:
+            raise ValueError("quaternion Hermitian input: FP64 with the default tolerance only")
+        return _qheev(A, "V", uplo)
     if _is_complex(A):
         if precision != "f64" or tol is not None:
             raise ValueError("complex Hermitian input: FP64 with the default tolerance only")
@@ -414,6 +455,10 @@ def eigvals(A, uplo="L", tol=None, precision="f64", irange=None, vl=None, vu=Non
         return _tridiag(A, "N", "QL", tol)
     if irange is not None or vl is not None or vu is not None:
         raise ValueError("eigenvalue subsets are available for SymTridiagonal input")
+    if isinstance(A, QuaternionMatrix):
+        if precision != "f64" or tol is not None:
+            raise ValueError("quaternion Hermitian input: FP64 with the default tolerance only")
+        return _qheev(A, "N", uplo)
     if _is_complex(A):
         if precision != "f64" or tol is not None:
             raise ValueError("complex Hermitian input: FP64 with the default tolerance only")
@@ -571,5 +616,5 @@ def autotune_load(path):
 
 __all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigen2", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
            "autotune_clear", "autotune_save", "autotune_load", "numnegevals", "symtri", "EigenQ",
-           "SymmetricTridiagonalFactorization",
+           "SymmetricTridiagonalFactorization", "QuaternionMatrix",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

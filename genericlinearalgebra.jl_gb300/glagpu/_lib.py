@@ -52,6 +52,8 @@ SIGNATURES = {
     "gla_dormtr_host": ([_ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64], _int),
     "gla_zheev": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int), _vp], _int),
     "gla_zheev_host": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int)], _int),
+    "gla_qheev": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int), _vp], _int),
+    "gla_qheev_host": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int)], _int),
     "gla_status_string": ([_int], C.c_char_p),
     "gla_plan_create": ([C.POINTER(_vp), _int, _ch, _ch, _i64, C.POINTER(_i64), _d, _int], _int),
     "gla_plan_destroy": ([_vp], _int),

@@ -258,6 +258,24 @@ int gla_zheev_host(char jobz, char uplo, int64_t n, const double* A, int64_t lda
                    int* info);
 
 /*
+ * Quaternion Hermitian eigenproblem (the reference's eigen!/eigvals! on
+ * Hermitian{Quaternion{Float64}}, test/eigenselfadjoint.jl:54-84): A is
+ * n x n quaternions of 4 doubles (s, i, j, k; the field order of
+ * Quaternion{Float64}), column-major with leading dimension lda (in
+ * quaternions); only the uplo triangle is read (a diagonal's i, j, k parts
+ * are ignored). w: n ascending eigenvalues (real); V (jobz 'V'): n x n
+ * orthonormal right eigenvectors (A v = v lambda), same layout, leading
+ * dimension ldv. Device pointers; synchronizes. Solved through the real
+ * symmetric matrix of left multiplication, of order 4n (4n <= GLA_MAX_N).
+ * Status and info as for gla_dsyev.
+ */
+int gla_qheev(char jobz, char uplo, int64_t n, const double* A, int64_t lda, double* w, double* V, int64_t ldv,
+              int* info, void* stream);
+/* Same, from and to host buffers. */
+int gla_qheev_host(char jobz, char uplo, int64_t n, const double* A, int64_t lda, double* w, double* V, int64_t ldv,
+                   int* info);
+
+/*
  * The Householder factorisation on its own (the reference's symtri! /
  * SymmetricTridiagonalFactorization and lmul!/rmul! with its EigenQ,
  * src/eigenSelfAdjoint.jl:6-118, 446-504; FP64, device pointers,
