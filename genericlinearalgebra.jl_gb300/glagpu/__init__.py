@@ -479,12 +479,15 @@ def _tridiag_dev(T):
 
 class EigenQ:
     """The orthogonal factor of symtri (src/eigenSelfAdjoint.jl:6-21): Householder
-    reflectors stored in `factors` (the reference's symtriLower! layout; a torch
-    CUDA float64 tensor, n x n) with scalars `tau`. lmul(B) = Q B and
-    rmul(B) = B Q (lmul!/rmul!, :23-99), array() = Q (Array(::EigenQ), :101);
-    the trans forms apply Q'."""
+    reflectors stored in `factors` (a torch CUDA float64 tensor, n x n, in the
+    reference's symtriLower! layout for uplo 'L' and symtriUpper!'s for 'U')
+    with scalars `tau`. lmul(B) = Q B and rmul(B) = B Q (lmul!/rmul!, :23-99),
+    array() = Q (Array(::EigenQ), :101); the trans forms apply Q'."""
 
-    def __init__(self, factors, tau):
+    def __init__(self, factors, tau, uplo="L"):
+        if uplo not in ("L", "U"):
+            raise ValueError("uplo must be 'L' or 'U'")
+        self.uplo = uplo
         self.factors = factors
         self.tau = tau
         self.n = factors.shape[0]
@@ -500,9 +503,9 @@ class EigenQ:
             raise DimensionMismatch(f"Q has order {self.n}, B is {m} x {k}")
         Xc = X.t().contiguous().clone()  # column-major storage of X
         F = self.factors.t().contiguous()
-        _lib.check(_lib.load().gla_dormtr(side.encode(), trans.encode(), m, k, C.c_void_p(F.data_ptr()), self.n,
-                                          C.c_void_p(self.tau.data_ptr()), C.c_void_p(Xc.data_ptr()), max(m, 1),
-                                          _stream_ptr()), "gla_dormtr")
+        _lib.check(_lib.load().gla_dormtr(side.encode(), self.uplo.encode(), trans.encode(), m, k,
+                                          C.c_void_p(F.data_ptr()), self.n, C.c_void_p(self.tau.data_ptr()),
+                                          C.c_void_p(Xc.data_ptr()), max(m, 1), _stream_ptr()), "gla_dormtr")
         out = Xc.t()
         return out if on_dev else out.cpu().numpy()
 
@@ -521,10 +524,10 @@ SymmetricTridiagonalFactorization = namedtuple("SymmetricTridiagonalFactorizatio
 
 
 def symtri(A, uplo="L"):
-    """symtri!(Hermitian(A, uplo)) (src/eigenSelfAdjoint.jl:446-504) on the GPU:
+    """symtri!(Hermitian(A, uplo)) (src/eigenSelfAdjoint.jl:446-564) on the GPU:
     A = Q T Q'. Returns SymmetricTridiagonalFactorization(EigenQ, SymTridiagonal)
-    with device tensors; the factors follow symtriLower!'s layout (an upper
-    input is factored as its symmetric lower counterpart)."""
+    with device tensors; the factors follow symtriLower!'s layout for uplo 'L'
+    and symtriUpper!'s for 'U'."""
     torch = _torch()
     X = A.to(torch.float64) if _is_torch(A) else torch.as_tensor(np.asarray(A, dtype=np.float64), device="cuda")
     n = X.shape[0]
@@ -537,7 +540,7 @@ def symtri(A, uplo="L"):
     _lib.check(_lib.load().gla_dsytrd(uplo.encode(), n, C.c_void_p(F.data_ptr()), max(n, 1), C.c_void_p(d.data_ptr()),
                                       C.c_void_p(e.data_ptr()), C.c_void_p(tau.data_ptr()), _stream_ptr()),
                "gla_dsytrd")
-    return SymmetricTridiagonalFactorization(EigenQ(F.t(), tau), SymTridiagonal(d[:n], e[:max(n - 1, 0)]))
+    return SymmetricTridiagonalFactorization(EigenQ(F.t(), tau, uplo), SymTridiagonal(d[:n], e[:max(n - 1, 0)]))
 
 
 def numnegevals(T, sigma=0.0):

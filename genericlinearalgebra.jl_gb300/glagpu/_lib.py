@@ -47,9 +47,9 @@ SIGNATURES = {
     "gla_numnegevals_host": ([_i64, _vp, _vp, _i64, _vp, _vp], _int),
     "gla_dstebz_host": ([_i64, _vp, _vp, _i64, _i64, _d, _vp], _int),
     "gla_dsytrd": ([_ch, _i64, _vp, _i64, _vp, _vp, _vp, _vp], _int),
-    "gla_dormtr": ([_ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp], _int),
+    "gla_dormtr": ([_ch, _ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp], _int),
     "gla_dsytrd_host": ([_ch, _i64, _vp, _i64, _vp, _vp, _vp], _int),
-    "gla_dormtr_host": ([_ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64], _int),
+    "gla_dormtr_host": ([_ch, _ch, _ch, _i64, _i64, _vp, _i64, _vp, _vp, _i64], _int),
     "gla_zheev": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int), _vp], _int),
     "gla_zheev_host": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int)], _int),
     "gla_qheev": ([_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, C.POINTER(_int), _vp], _int),

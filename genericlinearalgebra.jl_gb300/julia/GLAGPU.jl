@@ -213,10 +213,12 @@ function eigvals!(A::Hermitian{ComplexF64,Matrix{ComplexF64}}; tol = eps(Float64
     return w
 end
 
-# symtri! (src/eigenSelfAdjoint.jl:446-504) on the GPU: the factorisation in
-# symtriLower!'s layout, with an EigenQ whose lmul!/rmul! (:23-99) and Array
-# (:101) run on the device (gla_dsytrd_host / gla_dormtr_host).
+# symtri! (src/eigenSelfAdjoint.jl:446-564) on the GPU: the factorisation in
+# symtriLower!'s layout (uplo 'L') or symtriUpper!'s ('U'), with an EigenQ
+# whose lmul!/rmul! (:23-99) and Array (:101) run on the device
+# (gla_dsytrd_host / gla_dormtr_host).
 struct GPUEigenQ
+    uplo::Char
     factors::Matrix{Float64}
     tau::Vector{Float64}
 end
@@ -233,14 +235,15 @@ function symtri!(A::Union{Hermitian{Float64,Matrix{Float64}},Symmetric{Float64,M
     check(ccall((:gla_dsytrd_host, libglagpu), Cint,
                 (UInt8, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
                 UInt8(uplochar(A)), n, A.data, max(n, 1), d, e, tau))
-    return GPUSymmetricTridiagonalFactorization(GPUEigenQ(A.data, tau), SymTridiagonal(d, e))
+    return GPUSymmetricTridiagonalFactorization(GPUEigenQ(uplochar(A), A.data, tau), SymTridiagonal(d, e))
 end
 
 function _ormtr!(side::Char, trans::Char, Q::GPUEigenQ, B::Matrix{Float64})
     m, k = size(B)
     check(ccall((:gla_dormtr_host, libglagpu), Cint,
-                (UInt8, UInt8, Int64, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Int64),
-                UInt8(side), UInt8(trans), m, k, Q.factors, max(size(Q.factors, 1), 1), Q.tau, B, max(m, 1)))
+                (UInt8, UInt8, UInt8, Int64, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Int64),
+                UInt8(side), UInt8(Q.uplo), UInt8(trans), m, k, Q.factors, max(size(Q.factors, 1), 1), Q.tau, B,
+                max(m, 1)))
     return B
 end
 lmul!(Q::GPUEigenQ, B::Matrix{Float64}) = _ormtr!('L', 'N', Q, B)

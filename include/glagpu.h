@@ -278,25 +278,28 @@ int gla_qheev_host(char jobz, char uplo, int64_t n, const double* A, int64_t lda
 /*
  * The Householder factorisation on its own (the reference's symtri! /
  * SymmetricTridiagonalFactorization and lmul!/rmul! with its EigenQ,
- * src/eigenSelfAdjoint.jl:6-118, 446-504; FP64, device pointers,
+ * src/eigenSelfAdjoint.jl:6-118, 446-564; FP64, device pointers,
  * asynchronous):
- *   gla_dsytrd: A = Q T Q'. On return A's lower triangle holds the
- *     factorisation in the reference's symtriLower! layout: d on the
+ *   gla_dsytrd: A = Q T Q' from the uplo triangle, returned in that
+ *     triangle in the reference's layout. uplo 'L' (symtriLower!): d on the
  *     diagonal, e (the betas) on the first subdiagonal, reflector k in
- *     A[k+2:n, k] below its implicit unit at row k+1; d, e, tau (n-1) also
- *     returned. The upper triangle is not touched; uplo 'U' reads the upper
- *     triangle and factors its symmetric counterpart in the same lower layout.
+ *     A[k+2:n, k] below its implicit unit at row k+1. uplo 'U'
+ *     (symtriUpper!): e on the first superdiagonal, reflector k in
+ *     A[1:n-k-1, n-k+1] above its implicit unit at row n-k. d, e, tau (n-1)
+ *     are also returned. The other triangle is not touched.
  *   gla_dormtr: C := op(Q) C (side 'L', C is nq x n with nq = m) or
  *     C := C op(Q) (side 'R', C is m x nq with nq = n); trans 'N' or 'T';
- *     A and tau from gla_dsytrd of order nq.
+ *     A and tau from gla_dsytrd of order nq with the same uplo.
+ * Calls for one order share a cached workspace: issue them on one stream,
+ * or synchronize between streams.
  */
 int gla_dsytrd(char uplo, int64_t n, double* A, int64_t lda, double* d, double* e, double* tau, void* stream);
-int gla_dormtr(char side, char trans, int64_t m, int64_t n, const double* A, int64_t lda, const double* tau,
-               double* C, int64_t ldc, void* stream);
+int gla_dormtr(char side, char uplo, char trans, int64_t m, int64_t n, const double* A, int64_t lda,
+               const double* tau, double* C, int64_t ldc, void* stream);
 /* Same, from and to host buffers (synchronous). */
 int gla_dsytrd_host(char uplo, int64_t n, double* A, int64_t lda, double* d, double* e, double* tau);
-int gla_dormtr_host(char side, char trans, int64_t m, int64_t n, const double* A, int64_t lda, const double* tau,
-                    double* C, int64_t ldc);
+int gla_dormtr_host(char side, char uplo, char trans, int64_t m, int64_t n, const double* A, int64_t lda,
+                    const double* tau, double* C, int64_t ldc);
 
 /*
  * Spectrum slicing on SymTridiagonal(d, e) (d: n, e: n-1; device pointers;
