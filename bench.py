@@ -404,7 +404,8 @@ def run_c4(torch, glagpu, dev, reps=3):
     """Differentiation workload: 1024 symmetric matrices, n ~ U{32..96}
     (seed 4), Q diag(lam) Q' with lam sorted on [-1, 1] and gaps >= 1e-3;
     one step = forward eigen-decomposition + adjoint with cotangents
-    w, C ~ N(0, 1). Matrices per second, FP64 and FP32+refinement forward."""
+    w, C ~ N(0, 1). Matrices per second, FP64 and FP32+refinement forward,
+    run eagerly and as one captured CUDA graph (Plan.capture_step)."""
     from helpers import gapped_spectrum, prescribed
     rng = np.random.default_rng(4)
     ns = rng.integers(32, 97, size=1024)
@@ -440,6 +441,26 @@ def run_c4(torch, glagpu, dev, reps=3):
         out[path] = {"matrices_per_s": len(ns) / (ms * 1e-3), "ms_per_step": ms,
                      "adjoint_ms": e0.elapsed_time(e1) / reps, "info_nonzero": int((info.cpu() != 0).sum())}
         plan.close()
+        # the same step, forward plus adjoint, captured in one CUDA graph
+        gplan = glagpu.Plan(ns, precision=path, graph=True)
+        Ag = gplan.pack(mats, device=dev)
+        wg, Vg, Abg = torch.empty_like(w), torch.empty_like(V), torch.empty_like(Abar)
+        infog = torch.zeros_like(info)
+        g = gplan.capture_step(Ag, wg, Vg, infog, wbar, Vbar, Abg)
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            g.replay()
+        e1.record()
+        e1.synchronize()
+        gms = e0.elapsed_time(e1) / reps
+        out[path].update({"graph_matrices_per_s": len(ns) / (gms * 1e-3), "graph_ms_per_step": gms,
+                          "graph_info_nonzero": int((infog.cpu() != 0).sum()),
+                          "graph_equals_eager": bool(torch.equal(wg, w) and torch.equal(Vg, V)
+                                                     and torch.equal(Abg, Abar))})
+        gplan.close()
     return out
 
 
@@ -778,6 +799,8 @@ def main():
                     help="profiling: two solves of one GOE matrix of this order on the first of --paths")
     ap.add_argument("--c3-solve", action="store_true",
                     help="profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix only")
+    ap.add_argument("--c4", action="store_true",
+                    help="only the differentiation workload (forward + adjoint, eager and one CUDA graph)")
     ap.add_argument("--ozaki", type=int, default=0,
                     help="profiling: time only the tensor-core double-float GEMM (gla_gemm_df) at this order")
     args = ap.parse_args()
@@ -787,6 +810,11 @@ def main():
         import torch
         import glagpu
         print(json.dumps(time_ozaki(torch, glagpu, "cuda", args.ozaki)), flush=True)
+        return
+    if args.c4:
+        import torch
+        import glagpu
+        print(json.dumps(run_c4(torch, glagpu, "cuda")), flush=True)
         return
     if args.solve:
         # profiling: two solves of one GOE matrix (seed 1) of order args.solve

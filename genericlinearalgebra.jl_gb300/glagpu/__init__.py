@@ -180,6 +180,24 @@ class Plan:
             self.execute(A, w, V, info)
         return g
 
+    def capture_step(self, A, w, V, info, wbar, Vbar, Abar, gap_rel=0.0):
+        """Capture the forward solve and its adjoint, execute(A, w, V, info)
+        then adjoint(w, V, wbar, Vbar, Abar), into one torch.cuda.CUDAGraph
+        (plan made with graph=True). Replaying it re-solves whatever A holds
+        and back-propagates whatever wbar and Vbar hold."""
+        if not self.graph:
+            raise ValueError("plan was not created with graph=True")
+        torch = _torch()
+        # warm-up outside the capture: the first adjoint allocates its workspace
+        self.execute(A, w, V, info)
+        self.adjoint(w, V, wbar, Vbar, Abar, gap_rel)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.execute(A, w, V, info)
+            self.adjoint(w, V, wbar, Vbar, Abar, gap_rel)
+        return g
+
     def execute_host(self, A, w, V, info, stream=None):
         """Host-buffer run (numpy arenas); copies in/out and synchronizes.
         Returns the number of matrices with nonzero info."""

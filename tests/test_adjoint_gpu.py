@@ -121,3 +121,43 @@ def test_torch_autograd_wrapper(G):
     for wv, Vv, wb, Vb, g in zip(ws, Vs, wts, Cts, grads):
         ref = analytic_adjoint(Vv, wv, wb, Vb)
         assert np.linalg.norm(g - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32_refined"])
+def test_forward_and_adjoint_in_one_graph(G, precision):
+    # the solve plus its backward captured once (Plan.capture_step), replayed
+    # on two inputs and two cotangent pairs: bit-identical to eager execute
+    # followed by adjoint on the same data
+    import torch
+    mats1 = c4_batch(21, 40)
+    rng = np.random.default_rng(22)
+    mats2 = [prescribed(gapped_spectrum(m.shape[0], rng), 900 + i) for i, m in enumerate(mats1)]
+    sizes = [m.shape[0] for m in mats1]
+    ref = G.Plan(sizes, precision=precision)
+    gp = G.Plan(sizes, precision=precision, graph=True)
+    A = gp.pack(mats1, device="cuda")
+    w = torch.empty(gp.w_elems, dtype=torch.float64, device="cuda")
+    V = torch.empty(gp.a_elems, dtype=torch.float64, device="cuda")
+    info = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    wbar = torch.randn(gp.w_elems, dtype=torch.float64, device="cuda")
+    Vbar = torch.randn(gp.a_elems, dtype=torch.float64, device="cuda")
+    Abar = torch.empty_like(V)
+    g = gp.capture_step(A, w, V, info, wbar, Vbar, Abar)
+    for k, mats in enumerate((mats2, mats1)):
+        A.copy_(gp.pack(mats, device="cuda"))
+        wbar.copy_(torch.randn(gp.w_elems, dtype=torch.float64, device="cuda"))
+        Vbar.copy_(torch.randn(gp.a_elems, dtype=torch.float64, device="cuda"))
+        g.replay()
+        torch.cuda.synchronize()
+        A2 = ref.pack(mats, device="cuda")
+        w2, V2 = torch.empty_like(w), torch.empty_like(V)
+        info2 = torch.zeros_like(info)
+        Abar2 = torch.empty_like(Abar)
+        ref.execute(A2, w2, V2, info2)
+        ref.adjoint(w2, V2, wbar, Vbar, Abar2)
+        torch.cuda.synchronize()
+        assert (info.cpu().numpy() == 0).all()
+        assert torch.equal(w, w2) and torch.equal(V, V2)
+        assert torch.equal(Abar, Abar2)
+    gp.close()
+    ref.close()
