@@ -65,6 +65,21 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_seed(rank):
+    """Each rank solves its own seeded batch (replicas: no data exchange)."""
+    return SEED + 1000 * rank
+
+
+def max_over_ranks(torch, seconds, ws, dev):
+    """The slowest rank's elapsed time: with independent replicas the job
+    ends when the last one does (an all-reduce MAX when ws > 1)."""
+    if ws <= 1:
+        return seconds
+    t = torch.tensor([seconds], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def start_clock_sampler():
     path = tempfile.mktemp(suffix=".csv")
     try:
@@ -187,7 +202,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
-    ns, mats = workload(batch=args.batch, seed=SEED + 1000 * rank)
+    ns, mats = workload(batch=args.batch, seed=replica_seed(rank))
     if args.nrange:  # profiling: keep one size range of the workload
         lo, hi = (int(x) for x in args.nrange.split(","))
         keep = [i for i in range(len(ns)) if lo <= ns[i] <= hi]
@@ -239,10 +254,7 @@ def run_ours(args):
         barrier()
         el = ev0.elapsed_time(ev1) * 1e-3
         clocks = stop_clock_sampler(clk, local) if clk[0] is not None else None
-        if ws > 1:
-            t = torch.tensor([el], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(torch, el, ws, dev)
         counters = plan.stats()
         wh = w.cpu().numpy()
         Vh = V.cpu().numpy()
@@ -287,10 +299,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         barrier()
         el = ev0.elapsed_time(ev1) * 1e-3
-        if ws > 1:
-            t = torch.tensor([el], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(torch, el, ws, dev)
         acc = check_sample(ns, mats, w.cpu().numpy(), V.cpu().numpy(), woff, aoff, sample, np.float64)
         graph_res[path] = {"eigh_per_s": ws * len(ns) * args.steps / el, "ms_per_step": 1e3 * el / args.steps,
                            "accuracy": acc, "info_nonzero": int((info.cpu().numpy() != 0).sum())}
@@ -317,10 +326,7 @@ def run_ours(args):
     barrier()
     el_e2e = ev0.elapsed_time(ev1) * 1e-3
     plan.close()
-    if ws > 1:
-        t = torch.tensor([el_e2e], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el_e2e = float(t.item())
+    el_e2e = max_over_ranks(torch, el_e2e, ws, dev)
     peak = measured_dgemm_tflops(torch) if rank == 0 else None
     large = run_large(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
     c4 = run_c4(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
