@@ -116,6 +116,24 @@ void gla_oracle_symtri_d(char uplo, int64_t n, double* A, int64_t lda, double* t
   else symtri_upper(n, A, lda, tau, d, e);
 }
 
+// eigen!/eigvals! on Hermitian{ComplexF64}(A, uplo): A is n x n complex,
+// interleaved (re, im) doubles, column-major lda, overwritten by the
+// factorisation; w real ascending; V (jobz 'V') complex, interleaved.
+// tol <= 0 selects eps(Float64). Returns info.
+int gla_oracle_heev_z(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, double* V, int64_t ldv,
+                      double tol) {
+  Opts<double> o;
+  o.tol = tol > 0 ? tol : num<double>::eps();
+  return heev(o, jobz, uplo, n, reinterpret_cast<zc*>(A), lda, w, reinterpret_cast<zc*>(V), ldv);
+}
+
+// symtri! on Hermitian{ComplexF64}: factors (interleaved complex) in A, tau
+// (n-1 complex, interleaved), d and e real.
+void gla_oracle_symtri_z(char uplo, int64_t n, double* A, int64_t lda, double* tau, double* d, double* e) {
+  if (uplo == 'L') symtri_lower_c(n, reinterpret_cast<zc*>(A), lda, reinterpret_cast<zc*>(tau), d, e);
+  else symtri_upper_c(n, reinterpret_cast<zc*>(A), lda, reinterpret_cast<zc*>(tau), d, e);
+}
+
 // lmul!(Q::EigenQ, B) and rmul!(B, Q::EigenQ) with Q given by (uplo, F, tau).
 void gla_oracle_eigenq_lmul_d(char uplo, int64_t n, double* F, int64_t ldf, const double* tau, double* B, int64_t ldb,
                               int64_t ncols) {

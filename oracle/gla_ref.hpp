@@ -22,6 +22,7 @@
 #pragma once
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdint>
 #include <limits>
 #include <numeric>
@@ -235,12 +236,14 @@ template <class T> void givens(const Opts<T>& o, T f, T g, T& c, T& s, T& r) {
 }
 
 // _updateVectors! (src/eigenSelfAdjoint.jl:121-128): columns j, j+1 (0-based j).
-template <class T> void update_vectors(T c, T s, int64_t j, T* V, int64_t ldv, int64_t m) {
-  T* a = V + j * ldv;
-  T* b = V + (j + 1) * ldv;
+// The vectors' type VT is T, or std::complex<T> for complex Hermitian input
+// (real rotations on complex eigenvectors).
+template <class T, class VT> void update_vectors(T c, T s, int64_t j, VT* V, int64_t ldv, int64_t m) {
+  VT* a = V + j * ldv;
+  VT* b = V + (j + 1) * ldv;
   for (int64_t i = 0; i < m; i++) {
-    T v1 = b[i];
-    T v2 = a[i];
+    VT v1 = b[i];
+    VT v2 = a[i];
     b[i] = c * v1 + s * v2;
     a[i] = c * v2 - s * v1;
   }
@@ -255,7 +258,7 @@ template <class T> void eigvals2x2(T d1, T d2, T e, T& lp, T& lm) {
 }
 
 // eig2x2! (:136-161), j 0-based.
-template <class T> void eig2x2(T* d, T* e, int64_t j, T* V, int64_t ldv, int64_t m, T& c, T& s) {
+template <class T, class VT> void eig2x2(T* d, T* e, int64_t j, VT* V, int64_t ldv, int64_t m, T& c, T& s) {
   typedef num<T> N;
   T dj = d[j], dj1 = d[j + 1], ej = e[j];
   T r1 = (dj + dj1) / 2;
@@ -300,8 +303,8 @@ template <class T> void single_shift_ql_pwk(T* d, T* e, T shift, int64_t istart,
 }
 
 // singleShiftQL! (:377-409)
-template <class T>
-void single_shift_ql(Opts<T>& o, T* d, T* e, T shift, int64_t istart, int64_t iend, T* V, int64_t ldv, int64_t m) {
+template <class T, class VT>
+void single_shift_ql(Opts<T>& o, T* d, T* e, T shift, int64_t istart, int64_t iend, VT* V, int64_t ldv, int64_t m) {
   T gi = d[iend] - shift;
   T p = gi;
   T ci = 1, si = 0;
@@ -323,8 +326,8 @@ void single_shift_ql(Opts<T>& o, T* d, T* e, T shift, int64_t istart, int64_t ie
 }
 
 // singleShiftQR! (:412-444)
-template <class T>
-void single_shift_qr(Opts<T>& o, T* d, T* e, T shift, int64_t istart, int64_t iend, T* V, int64_t ldv, int64_t m) {
+template <class T, class VT>
+void single_shift_qr(Opts<T>& o, T* d, T* e, T shift, int64_t istart, int64_t iend, VT* V, int64_t ldv, int64_t m) {
   T gi = d[istart] - shift;
   T p = gi;
   T ci = 1, si = 0;
@@ -410,7 +413,7 @@ template <class T> int eigvals_pwk(Opts<T>& o, T* d, T* e, int64_t n) {
 }
 
 // eigQL! (:221-288); V is m x n (m <= n rows), column-major ldv.
-template <class T> int eig_ql(Opts<T>& o, T* d, T* e, int64_t n, T* V, int64_t ldv, int64_t m) {
+template <class T, class VT> int eig_ql(Opts<T>& o, T* d, T* e, int64_t n, VT* V, int64_t ldv, int64_t m) {
   typedef num<T> N;
   int64_t cap = o.max_sweeps >= 0 ? o.max_sweeps : 30 * n;
   int64_t bs = 0, be = n - 1;
@@ -438,7 +441,7 @@ template <class T> int eig_ql(Opts<T>& o, T* d, T* e, int64_t n, T* V, int64_t l
 }
 
 // eigQR! (:290-340)
-template <class T> int eig_qr(Opts<T>& o, T* d, T* e, int64_t n, T* V, int64_t ldv, int64_t m) {
+template <class T, class VT> int eig_qr(Opts<T>& o, T* d, T* e, int64_t n, VT* V, int64_t ldv, int64_t m) {
   typedef num<T> N;
   int64_t cap = o.max_sweeps >= 0 ? o.max_sweeps : 30 * n;
   int64_t bs = 0, be = n - 1;
@@ -640,7 +643,7 @@ template <class T> bool isless(T a, T b) {
 }
 
 // sorteig!: stable ascending sort of w with the columns of V (m x n) permuted to match.
-template <class T> void sorteig(T* w, int64_t n, T* V, int64_t ldv, int64_t m) {
+template <class T, class VT = T> void sorteig(T* w, int64_t n, VT* V, int64_t ldv, int64_t m) {
   std::vector<int64_t> p(n);
   std::iota(p.begin(), p.end(), 0);
   std::stable_sort(p.begin(), p.end(), [&](int64_t a, int64_t b) { return isless(w[a], w[b]); });
@@ -648,7 +651,7 @@ template <class T> void sorteig(T* w, int64_t n, T* V, int64_t ldv, int64_t m) {
   for (int64_t i = 0; i < n; i++) wt[i] = w[p[i]];
   for (int64_t i = 0; i < n; i++) w[i] = wt[i];
   if (V && m > 0) {
-    std::vector<T> Vt((size_t)m * n);
+    std::vector<VT> Vt((size_t)m * n);
     for (int64_t j = 0; j < n; j++)
       for (int64_t i = 0; i < m; i++) Vt[i + j * m] = V[i + p[j] * ldv];
     for (int64_t j = 0; j < n; j++)
@@ -683,7 +686,7 @@ int syev(Opts<T>& o, char jobz, char uplo, int64_t n, T* A, int64_t lda, T* w, T
   int info;
   if (jobz == 'N') {
     info = eigvals_pwk(o, w, e.data(), n);
-    sorteig<T>(w, n, nullptr, 0, 0);
+    sorteig<T, T>(w, n, nullptr, 0, 0);
   } else {
     for (int64_t j = 0; j < n; j++)
       for (int64_t i = 0; i < n; i++) V[i + j * ldv] = (i == j) ? 1 : 0;
@@ -700,12 +703,181 @@ template <class T> int stev(Opts<T>& o, char jobz, int64_t n, T* d, T* e, T* V, 
   int info;
   if (jobz == 'N') {
     info = eigvals_pwk(o, d, e, n);
-    sorteig<T>(d, n, nullptr, 0, 0);
+    sorteig<T, T>(d, n, nullptr, 0, 0);
   } else {
     for (int64_t j = 0; j < n; j++)
       for (int64_t i = 0; i < n; i++) V[i + j * ldv] = (i == j) ? 1 : 0;
     info = use_qr ? eig_qr(o, d, e, n, V, ldv, n) : eig_ql(o, d, e, n, V, ldv, n);
     sorteig(d, n, V, ldv, n);
+  }
+  return info;
+}
+
+// ---- Complex Hermitian input: the same algorithm with T <: Complex. ----
+// The reference runs symtriLower!/symtriUpper! on the complex matrix with one
+// more reflector than for real input (loop bound n-2+!(T<:Real), :462/:522),
+// which leaves a real tridiagonal; Array(Q) is complex and eigQL! applies its
+// real rotations to the complex vectors. Stdlib pieces restated: reflector!
+// for complex x (the LAPACK zlarfg reflector, H = I - tau v v' with
+// H' x = -nu e1, nu = copysign(norm(x), real(x1))), BLAS zhemv (netlib
+// reference loops) and zdotc.
+typedef std::complex<double> zc;
+
+inline double norm2c(const zc* x, int64_t n, int64_t inc) {
+  double maxabs = 0;
+  for (int64_t i = 0; i < n; i++) {
+    double a = std::abs(x[i * inc]);
+    if (!(a <= maxabs)) maxabs = a;
+  }
+  if (maxabs == 0 || !std::isfinite(maxabs)) return maxabs;
+  if (std::isfinite((double)n * maxabs * maxabs) && maxabs * maxabs != 0) {
+    double sum = 0;
+    for (int64_t i = 0; i < n; i++) sum += std::norm(x[i * inc]);
+    return std::sqrt(sum);
+  }
+  double sum = 0;
+  for (int64_t i = 0; i < n; i++) sum += std::norm(x[i * inc] / maxabs);
+  return maxabs * std::sqrt(sum);
+}
+
+inline zc reflector_c(zc* x, int64_t n, int64_t inc) {
+  if (n == 0) return 0;
+  zc xi1 = x[0];
+  double normu = norm2c(x, n, inc);
+  if (normu == 0) return 0;
+  double nu = std::copysign(normu, xi1.real());
+  xi1 += nu;
+  x[0] = -nu;
+  for (int64_t i = 1; i < n; i++) x[i * inc] /= xi1;
+  return xi1 / nu;
+}
+
+inline zc dotc(const zc* x, const zc* y, int64_t n) {
+  zc s = 0;
+  for (int64_t i = 0; i < n; i++) s += std::conj(x[i]) * y[i];
+  return s;
+}
+
+// netlib reference zhemv, y = alpha*A*x (beta = 0), lower / upper triangle.
+inline void hemv_lower(int64_t n, zc alpha, const zc* A, int64_t lda, const zc* x, zc* y) {
+  for (int64_t i = 0; i < n; i++) y[i] = 0;
+  for (int64_t j = 0; j < n; j++) {
+    zc temp1 = alpha * x[j], temp2 = 0;
+    y[j] += temp1 * A[j + j * lda].real();
+    for (int64_t i = j + 1; i < n; i++) {
+      y[i] += temp1 * A[i + j * lda];
+      temp2 += std::conj(A[i + j * lda]) * x[i];
+    }
+    y[j] += alpha * temp2;
+  }
+}
+inline void hemv_upper(int64_t n, zc alpha, const zc* A, int64_t lda, const zc* x, zc* y) {
+  for (int64_t i = 0; i < n; i++) y[i] = 0;
+  for (int64_t j = 0; j < n; j++) {
+    zc temp1 = alpha * x[j], temp2 = 0;
+    for (int64_t i = 0; i < j; i++) {
+      y[i] += temp1 * A[i + j * lda];
+      temp2 += std::conj(A[i + j * lda]) * x[i];
+    }
+    y[j] += temp1 * A[j + j * lda].real() + alpha * temp2;
+  }
+}
+
+// symtriLower! (:450-504) for complex AS: n-1 reflectors; d, e real.
+inline void symtri_lower_c(int64_t n, zc* AS, int64_t lda, zc* tau, double* d, double* e) {
+  std::vector<zc> u(std::max<int64_t>(n, 1));
+  for (int64_t i = 0; i < n; i++) at(AS, lda, i, i) = at(AS, lda, i, i).real();
+  for (int64_t k = 0; k + 1 < n; k++) {  // k = 1:(n-1) in 1-based terms
+    int64_t m = n - k - 1;
+    zc* x = &at(AS, lda, k + 1, k);
+    zc tk = reflector_c(x, m, 1);
+    tau[k] = tk;
+    zc tmp = x[0];
+    x[0] = 1;
+    zc* ut = u.data() + k + 1;
+    hemv_lower(m, tk, &at(AS, lda, k + 1, k + 1), lda, x, ut);
+    double xi = (std::conj(tk) * dotc(x, ut, m)).real();
+    for (int64_t j = 0; j < m; j++) {
+      zc xj = x[j], uj = ut[j], xixj = xi * xj;
+      for (int64_t i = j; i < m; i++)
+        at(AS, lda, k + 1 + i, k + 1 + j) += x[i] * std::conj(xixj) - x[i] * std::conj(uj) - ut[i] * std::conj(xj);
+    }
+    x[0] = tmp;
+  }
+  for (int64_t i = 0; i < n; i++) d[i] = at(AS, lda, i, i).real();
+  for (int64_t i = 0; i + 1 < n; i++) e[i] = at(AS, lda, i + 1, i).real();
+}
+
+// symtriUpper! (:507-564) for complex AS.
+inline void symtri_upper_c(int64_t n, zc* AS, int64_t lda, zc* tau, double* d, double* e) {
+  std::vector<zc> u(std::max<int64_t>(n, 1));
+  for (int64_t i = 0; i < n; i++) at(AS, lda, i, i) = at(AS, lda, i, i).real();
+  for (int64_t k = 0; k + 1 < n; k++) {
+    int64_t m = n - k - 1;
+    zc* x = &at(AS, lda, 0, n - k - 1);
+    zc tk = reflector_c(x + (m - 1), m, -1);  // the reversed view AS[(n-k):-1:1, n-k+1]
+    tau[k] = tk;
+    zc tmp = x[m - 1];
+    x[m - 1] = 1;
+    hemv_upper(m, tk, AS, lda, x, u.data());
+    double xi = (std::conj(tk) * dotc(x, u.data(), m)).real();
+    for (int64_t j = 0; j < m; j++) {
+      zc xj = x[j], uj = u[j], xixj = xi * xj;
+      for (int64_t i = 0; i <= j; i++)
+        at(AS, lda, i, j) += x[i] * std::conj(xixj) - x[i] * std::conj(uj) - u[i] * std::conj(xj);
+    }
+    x[m - 1] = tmp;
+  }
+  for (int64_t i = 0; i < n; i++) d[i] = at(AS, lda, i, i).real();
+  for (int64_t i = 0; i + 1 < n; i++) e[i] = at(AS, lda, i, i + 1).real();
+}
+
+// lmul!(Q::EigenQ, B) (:23-60) for complex factors: B (n x ncols) <- Q*B,
+// with h' * b = zdotc(h, b).
+inline void eigenq_lmul_c(char uplo, int64_t n, zc* F, int64_t ldf, const zc* tau, zc* B, int64_t ldb,
+                          int64_t ncols) {
+  for (int64_t k = n - 1; k >= 1; k--) {  // 1-based k over length(tau) = n-1
+    const int64_t len = n - k;
+    zc* h = uplo == 'L' ? &at(F, ldf, k, k - 1) : &at(F, ldf, 0, n - k);
+    const int64_t head = uplo == 'L' ? 0 : len - 1;
+    const zc t = tau[k - 1];
+    zc tmp = h[head];
+    h[head] = 1;
+    for (int64_t j = 0; j < ncols; j++) {
+      zc* Bj = uplo == 'L' ? &at(B, ldb, k, j) : &at(B, ldb, 0, j);
+      tmp = t * dotc(h, Bj, len);
+      for (int64_t i = 0; i < len; i++) Bj[i] -= h[i] * tmp;
+    }
+    h[head] = tmp;
+  }
+}
+
+// _eigen!/_eigvals!(Hermitian{<:Complex}): symtri!, then eigvalsPWK!
+// (values) or Array(Q) + eigQL! (vectors), then sorteig!. Returns info.
+inline int heev(Opts<double>& o, char jobz, char uplo, int64_t n, zc* A, int64_t lda, double* w, zc* V, int64_t ldv) {
+  if (n == 0) return 0;
+  for (int64_t j = 0; j < n; j++) {
+    int64_t i0 = uplo == 'L' ? j : 0, i1 = uplo == 'L' ? n : j + 1;
+    for (int64_t i = i0; i < i1; i++)
+      if (!std::isfinite(A[i + j * lda].real()) || !std::isfinite(A[i + j * lda].imag())) {
+        for (int64_t q = 0; q < n; q++) w[q] = std::numeric_limits<double>::quiet_NaN();
+        return -1;
+      }
+  }
+  std::vector<zc> tau(std::max<int64_t>(n - 1, 1));
+  std::vector<double> e(std::max<int64_t>(n - 1, 1));
+  if (uplo == 'L') symtri_lower_c(n, A, lda, tau.data(), w, e.data());
+  else symtri_upper_c(n, A, lda, tau.data(), w, e.data());
+  int info;
+  if (jobz == 'N') {
+    info = eigvals_pwk(o, w, e.data(), n);
+    sorteig<double, double>(w, n, nullptr, 0, 0);
+  } else {
+    for (int64_t j = 0; j < n; j++)
+      for (int64_t i = 0; i < n; i++) V[i + j * ldv] = (i == j) ? 1.0 : 0.0;
+    eigenq_lmul_c(uplo, n, A, lda, tau.data(), V, ldv, n);
+    info = eig_ql(o, w, e.data(), n, V, ldv, n);
+    sorteig(w, n, V, ldv, n);
   }
   return info;
 }

@@ -5,6 +5,7 @@ CPU-baseline leg of bench.py; the shipped GPU path never calls it.
 
 Functions mirror the reference entry points:
   syev(A, jobz, uplo)   -> _eigen!/_eigvals!(Hermitian(A, uplo))   :566-618
+  heev(A, jobz, uplo)   -> the same for complex Hermitian A (T <: Complex, :462)
   stev(d, e, jobz)      -> _eigen!/_eigvals!(SymTridiagonal(d, e)) :566,602-612
   eigql(d, e, V)        -> eigQL!/eigQR! on explicit vectors       :221-340
   symtri(A, uplo)       -> symtri!                                  :446-564
@@ -60,6 +61,9 @@ def lib():
         L.gla_oracle_max_threads.argtypes = []
         L.gla_oracle_numnegevals_d.argtypes = [_i64, _vp, _vp, _i64, _vp, _vp]
         L.gla_oracle_numnegevals_d.restype = None
+        L.gla_oracle_heev_z.argtypes = [_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, _d]
+        L.gla_oracle_symtri_z.argtypes = [_ch, _i64, _vp, _i64, _vp, _vp, _vp]
+        L.gla_oracle_symtri_z.restype = None
         _lib = L
     return _lib
 
@@ -92,6 +96,30 @@ def syev(A, jobz="V", uplo="L", tol=0.0, use_qr=False, generic_givens=False, max
     if return_stats:
         return out + ({"nrot": int(nrot[0]), "nsweeps": int(nsw[0])},)
     return out
+
+
+def heev(A, jobz="V", uplo="L", tol=0.0):
+    """_eigen!/_eigvals!(Hermitian(A, uplo)) for complex A (the T <: Complex
+    path: n-1 reflectors, complex Q, real QL rotations on complex vectors).
+    Returns (w, V, info); A is copied."""
+    A = np.array(A, dtype=np.complex128, order="F", copy=True)
+    n = A.shape[0]
+    assert A.shape == (n, n)
+    w = np.zeros(n)
+    V = np.zeros((n, n), dtype=np.complex128, order="F") if jobz == "V" else np.zeros((1, 1), np.complex128)
+    info = lib().gla_oracle_heev_z(jobz.encode(), uplo.encode(), n, _p(A), max(n, 1), _p(w), _p(V), max(n, 1), tol)
+    return w, (V if jobz == "V" else None), info
+
+
+def symtri_complex(A, uplo="L"):
+    """symtri!(Hermitian(A, uplo)) for complex A: returns (factors, tau, d, e)."""
+    F = np.array(A, dtype=np.complex128, order="F", copy=True)
+    n = F.shape[0]
+    tau = np.zeros(max(n - 1, 1), dtype=np.complex128)
+    d = np.zeros(n)
+    e = np.zeros(max(n - 1, 1))
+    lib().gla_oracle_symtri_z(uplo.encode(), n, _p(F), max(n, 1), _p(tau), _p(d), _p(e))
+    return F, tau[: n - 1], d, e[: n - 1]
 
 
 def syev_quad(A, jobz="V", uplo="L", use_qr=False, generic_givens=False):

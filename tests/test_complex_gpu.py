@@ -1,11 +1,15 @@
 """Complex Hermitian input (the reference's eigen/eigvals on
 Hermitian{<:Complex}; test/eigenselfadjoint.jl:86-91 and :171-176) through
-gla_zheev, against LAPACK (scipy eigh, zheevd).
+gla_zheev, against LAPACK (scipy eigh, zheevd) and against the oracle's
+restatement of the reference's own complex path (values, and eigenvectors
+up to their complex phase where the eigenvalue is separated).
 Tolerances: eigenvalues within 16 n eps ||A|| (the real embedding has order
 2n); residual ||AV - V diag(w)||/||A|| and ||V^H V - I|| <= 1e-13."""
 import numpy as np
 import pytest
 import scipy.linalg as sl
+
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -86,3 +90,24 @@ def test_complex_device_tensor(G):
     r = G.eigen(At)
     assert r.vectors.is_cuda and r.vectors.dtype == torch.complex128
     check(A, r.values.cpu().numpy(), r.vectors.cpu().numpy())
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("n", [4, 64, 200])
+def test_against_oracle_restatement(G, n, uplo):
+    A = herm(n, 500 + n)
+    r = G.eigen(A, uplo=uplo)
+    wo, Vo, info = O.heev(A, "V", uplo)
+    assert info == 0
+    nA = np.linalg.norm(A, 2)
+    assert np.abs(r.values - wo).max() <= 24 * n * EPS64 * nA
+    # eigenvectors agree up to a unit complex factor where the eigenvalue is separated
+    gaps = np.full(n, np.inf)
+    if n > 1:
+        dw = np.diff(wo)
+        gaps[:-1] = np.minimum(gaps[:-1], dw)
+        gaps[1:] = np.minimum(gaps[1:], dw)
+    sep = gaps > 1e-6 * nA
+    overlap = np.abs(np.sum(r.vectors.conj() * Vo, axis=0))
+    assert sep.sum() >= n // 2
+    assert np.all(overlap[sep] >= 1 - 1e-8)

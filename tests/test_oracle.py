@@ -203,3 +203,55 @@ def test_numnegevals_zero_pivot_rule():
     # T = [[0, 1], [1, 0]] at sigma = 0 has delta_1 = 0
     d, e = np.array([0.0, 0.0]), np.array([1.0])
     assert O.numnegevals(d, e, 0.0) == 1  # eigenvalues -1, 1
+
+
+def herm(n, seed):
+    rng = np.random.default_rng(seed)
+    B = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return (B + B.conj().T) / 2
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("n", [1, 2, 4, 17, 50])
+def test_complex_hermitian_against_lapack(n, uplo):
+    # the T <: Complex path (n-1 reflectors, :462/:522), pinned as the
+    # reference's own test pins it (test/eigenselfadjoint.jl:86-91, against
+    # stdlib LAPACK): values within 4 n eps ||A|| of zheevd, and the
+    # default testset's properties (residual, orthogonality)
+    A = herm(n, 300 + n)
+    junk = np.full((n, n), 5 - 5j)
+    S = np.where(np.tril(np.ones((n, n), bool)) if uplo == "L" else np.triu(np.ones((n, n), bool)), A, junk)
+    w, V, info = O.heev(S, "V", uplo)
+    assert info == 0 and np.all(np.diff(w) >= 0)
+    nA = max(np.linalg.norm(A, 2), 1e-300)
+    eps = 2.0 ** -52
+    assert np.abs(w - sl.eigh(A, eigvals_only=True)).max() <= 4 * n * eps * nA
+    assert np.linalg.norm(A @ V - V * w, 2) / nA <= 1e-13
+    assert np.linalg.norm(V.conj().T @ V - np.eye(n), 2) <= 1e-13
+    wn, _, info = O.heev(S, "N", uplo)
+    assert info == 0 and np.abs(wn - w).max() <= 4 * n * eps * nA
+
+
+def test_complex_reference_known_answers():
+    # test/eigenselfadjoint.jl:171-176: Hermitian(Tridiagonal(ones(ComplexF64, .)))
+    M = np.diag(np.ones(3, complex)) + np.diag(np.ones(2, complex), 1) + np.diag(np.ones(2, complex), -1)
+    w, V, info = O.heev(M)
+    assert info == 0
+    assert np.abs(w - np.array([1 - np.sqrt(2), 1.0, 1 + np.sqrt(2)])).max() <= 4e-16 * 4
+    # the complex factorisation leaves a real tridiagonal with Q' A Q = T
+    A = herm(30, 9)
+    F, tau, d, e = O.symtri_complex(A, "L")
+    assert len(tau) == 29  # one more reflector than for real input
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    assert np.abs(np.linalg.eigvalsh(T) - np.linalg.eigvalsh(A)).max() <= 1e-13 * np.linalg.norm(A, 2)
+
+
+def test_complex_path_on_real_input():
+    # a real symmetric matrix through the complex path: the values agree with
+    # the real path's to rounding (the real loop stops one reflector earlier)
+    A = goe(40, 4)
+    wr, _, _ = O.syev(A)
+    wz, Vz, info = O.heev(A.astype(complex))
+    assert info == 0
+    assert np.abs(wz - wr).max() <= 8 * 40 * 2.0 ** -52 * np.linalg.norm(A, 2)
+    assert np.linalg.norm(A @ Vz - Vz * wz, 2) / np.linalg.norm(A, 2) <= 1e-13
