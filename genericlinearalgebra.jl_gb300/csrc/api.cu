@@ -757,7 +757,7 @@ int gla_plan_phase_times(gla_plan_t p, float* ms) {
 }
 
 int gla_plan_stats(gla_plan_t p, int64_t* rotations, int64_t* sweeps, int* passes) {
-  int64_t c[GLA_NUM_COUNTERS];
+  int64_t c[GLA_NUM_COUNTERS] = {};
   int rc = gla_plan_counters(p, c);
   if (rc) return rc;
   if (rotations) *rotations = c[GLA_COUNTER_ROTATIONS];

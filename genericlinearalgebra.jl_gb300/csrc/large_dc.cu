@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(256) k_dc_vec(DcArrays<T> a) {
 template <class T>
 __global__ void __launch_bounds__(1024) k_dc_post(DcArrays<T> a, int mpow2) {
   MergeInfo* mp = a.info + blockIdx.x;
-  const int o = mp->o, m1 = mp->m1, m = m1 + mp->m2, k = mp->k, nf = mp->nf;
+  const int o = mp->o, m1 = mp->m1, m = m1 + mp->m2, k = mp->k;
   const int tid = threadIdx.x;
   extern __shared__ unsigned char smraw[];
   unsigned long long* key = reinterpret_cast<unsigned long long*>(smraw);

@@ -54,13 +54,25 @@ namespace {
 constexpr unsigned kSignMask = (0xEu << 0) | (0x4u << 4) | (0x8u << 8) | (0x2u << 12);
 __device__ __forceinline__ double lsign(int r, int c) { return (kSignMask >> (4 * r + c)) & 1u ? -1.0 : 1.0; }
 
-// One Hamilton product p q (4 doubles each).
-__device__ __forceinline__ double4 hmul(double4 p, double4 q) {
-  return make_double4(p.x * q.x - p.y * q.y - p.z * q.z - p.w * q.w, p.x * q.y + p.y * q.x + p.z * q.w - p.w * q.z,
-                      p.x * q.z - p.y * q.w + p.z * q.x + p.w * q.y, p.x * q.w + p.y * q.z - p.z * q.y + p.w * q.x);
+// A quaternion s + x i + y j + z k in registers.
+struct Quat {
+  double s, x, y, z;
+};
+__device__ __forceinline__ Quat quat(double s, double x, double y, double z) {
+  Quat q;
+  q.s = s;
+  q.x = x;
+  q.y = y;
+  q.z = z;
+  return q;
 }
-__device__ __forceinline__ double4 hconj(double4 p) { return make_double4(p.x, -p.y, -p.z, -p.w); }
-__device__ __forceinline__ double4 ld4(const double* p) { return make_double4(p[0], p[1], p[2], p[3]); }
+// One Hamilton product p q.
+__device__ __forceinline__ Quat hmul(Quat p, Quat q) {
+  return quat(p.s * q.s - p.x * q.x - p.y * q.y - p.z * q.z, p.s * q.x + p.x * q.s + p.y * q.z - p.z * q.y,
+              p.s * q.y - p.x * q.z + p.y * q.s + p.z * q.x, p.s * q.z + p.x * q.y - p.y * q.x + p.z * q.s);
+}
+__device__ __forceinline__ Quat hconj(Quat p) { return quat(p.s, -p.x, -p.y, -p.z); }
+__device__ __forceinline__ Quat ld4(const double* p) { return quat(p[0], p[1], p[2], p[3]); }
 
 // E = L(A) (4n x 4n, leading dimension 4n) from the referenced triangle of
 // the quaternion matrix A (leading dimension lda quaternions).
@@ -101,23 +113,23 @@ __global__ void k_qfour(const double* __restrict__ E, int n, const int* __restri
     for (int m = 0; m < 4; m++) V[4 * (i + d * ldv) + m] = E[(m * n + i) + s * n4];
 }
 
-__device__ double4 block_sum4(double4 v, double4* red) {
+__device__ Quat block_sum4(Quat v, Quat* red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
+    v.s += __shfl_xor_sync(0xffffffffu, v.s, o);
     v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
     v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
     v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
-    v.w += __shfl_xor_sync(0xffffffffu, v.w, o);
   }
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  double4 s = make_double4(0.0, 0.0, 0.0, 0.0);
+  Quat s = quat(0.0, 0.0, 0.0, 0.0);
   for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+    s.s += red[w].s;
     s.x += red[w].x;
     s.y += red[w].y;
     s.z += red[w].z;
-    s.w += red[w].w;
   }
   return s;
 }
@@ -134,7 +146,7 @@ __device__ double4 block_sum4(double4 v, double4* red) {
 __global__ void __launch_bounds__(256) k_qgroup(const double* __restrict__ E, int n, const int* __restrict__ g0s,
                                                 const int* __restrict__ ks, const int* __restrict__ outs,
                                                 double* __restrict__ V, long long ldv, double* __restrict__ scratch) {
-  __shared__ double4 red[8];
+  __shared__ Quat red[8];
   __shared__ int kept_s;
   const int g = blockIdx.x, g0 = g0s[g], k = ks[g], out0 = outs[g];
   double* r = scratch + 4LL * n * g;
@@ -154,30 +166,30 @@ __global__ void __launch_bounds__(256) k_qgroup(const double* __restrict__ E, in
       for (int pass = 0; pass < 2; pass++)
         for (int q = 0; q < kept; q++) {
           const double* vq = V + 4 * (out0 + q) * ldv;
-          double4 h = make_double4(0.0, 0.0, 0.0, 0.0);  // vq^H r
+          Quat h = quat(0.0, 0.0, 0.0, 0.0);  // vq^H r
           for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double4 t = hmul(hconj(ld4(vq + 4 * i)), ld4(r + 4 * i));
+            const Quat t = hmul(hconj(ld4(vq + 4 * i)), ld4(r + 4 * i));
+            h.s += t.s;
             h.x += t.x;
             h.y += t.y;
             h.z += t.z;
-            h.w += t.w;
           }
           h = block_sum4(h, red);
           for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double4 t = hmul(ld4(vq + 4 * i), h);
-            r[4 * i] -= t.x;
-            r[4 * i + 1] -= t.y;
-            r[4 * i + 2] -= t.z;
-            r[4 * i + 3] -= t.w;
+            const Quat t = hmul(ld4(vq + 4 * i), h);
+            r[4 * i] -= t.s;
+            r[4 * i + 1] -= t.x;
+            r[4 * i + 2] -= t.y;
+            r[4 * i + 3] -= t.z;
           }
           __syncthreads();
         }
-      double4 nn = make_double4(0.0, 0.0, 0.0, 0.0);
+      Quat nn = quat(0.0, 0.0, 0.0, 0.0);
       for (int i = threadIdx.x; i < n; i += blockDim.x)
 #pragma unroll
-        for (int m = 0; m < 4; m++) nn.x += r[4 * i + m] * r[4 * i + m];
+        for (int m = 0; m < 4; m++) nn.s += r[4 * i + m] * r[4 * i + m];
       nn = block_sum4(nn, red);
-      const double nrm = sqrt(nn.x);
+      const double nrm = sqrt(nn.s);
       if (nrm > thr) {
         double* vo = V + 4 * (out0 + kept) * ldv;
         for (int i = threadIdx.x; i < 4 * n; i += blockDim.x) vo[i] = r[i] / nrm;
