@@ -130,8 +130,28 @@ int gla_oracle_heev_z(char jobz, char uplo, int64_t n, double* A, int64_t lda, d
 // symtri! on Hermitian{ComplexF64}: factors (interleaved complex) in A, tau
 // (n-1 complex, interleaved), d and e real.
 void gla_oracle_symtri_z(char uplo, int64_t n, double* A, int64_t lda, double* tau, double* d, double* e) {
-  if (uplo == 'L') symtri_lower_c(n, reinterpret_cast<zc*>(A), lda, reinterpret_cast<zc*>(tau), d, e);
-  else symtri_upper_c(n, reinterpret_cast<zc*>(A), lda, reinterpret_cast<zc*>(tau), d, e);
+  if (uplo == 'L') symtri_lower_f(n, reinterpret_cast<zc*>(A), lda, reinterpret_cast<zc*>(tau), d, e);
+  else symtri_upper_f(n, reinterpret_cast<zc*>(A), lda, reinterpret_cast<zc*>(tau), d, e);
+}
+
+// The same for Hermitian{Quaternion{Float64}}: quaternions are 4 doubles
+// (s, i, j, k), matrices column-major with lda counted in quaternions.
+int gla_oracle_heev_q(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, double* V, int64_t ldv,
+                      double tol) {
+  static_assert(sizeof(Quat) == 4 * sizeof(double), "Quat is four packed doubles");
+  Opts<double> o;
+  o.tol = tol > 0 ? tol : num<double>::eps();
+  return heev(o, jobz, uplo, n, reinterpret_cast<Quat*>(A), lda, w, reinterpret_cast<Quat*>(V), ldv);
+}
+void gla_oracle_symtri_qt(char uplo, int64_t n, double* A, int64_t lda, double* tau, double* d, double* e) {
+  if (uplo == 'L') symtri_lower_f(n, reinterpret_cast<Quat*>(A), lda, reinterpret_cast<Quat*>(tau), d, e);
+  else symtri_upper_f(n, reinterpret_cast<Quat*>(A), lda, reinterpret_cast<Quat*>(tau), d, e);
+}
+// lmul!(Q::EigenQ, B) for quaternion factors (B: n x ncols quaternions).
+void gla_oracle_eigenq_lmul_qt(char uplo, int64_t n, double* F, int64_t ldf, const double* tau, double* B,
+                               int64_t ldb, int64_t ncols) {
+  eigenq_lmul_f(uplo, n, reinterpret_cast<Quat*>(F), ldf, reinterpret_cast<const Quat*>(tau),
+                reinterpret_cast<Quat*>(B), ldb, ncols);
 }
 
 // lmul!(Q::EigenQ, B) and rmul!(B, Q::EigenQ) with Q given by (uplo, F, tau).

@@ -713,138 +713,189 @@ template <class T> int stev(Opts<T>& o, char jobz, int64_t n, T* d, T* e, T* V, 
   return info;
 }
 
-// ---- Complex Hermitian input: the same algorithm with T <: Complex. ----
-// The reference runs symtriLower!/symtriUpper! on the complex matrix with one
-// more reflector than for real input (loop bound n-2+!(T<:Real), :462/:522),
-// which leaves a real tridiagonal; Array(Q) is complex and eigQL! applies its
-// real rotations to the complex vectors. Stdlib pieces restated: reflector!
-// for complex x (the LAPACK zlarfg reflector, H = I - tau v v' with
-// H' x = -nu e1, nu = copysign(norm(x), real(x1))), BLAS zhemv (netlib
-// reference loops) and zdotc.
+// ---- Complex and quaternion Hermitian input: the same algorithm with a
+// non-real element type F (std::complex<double>, or Quat below). ----
+// The reference runs symtriLower!/symtriUpper! on the non-real matrix with
+// one more reflector than for real input (loop bound n-2+!(T<:Real),
+// :462/:522), which leaves a real tridiagonal; Array(Q) has type F and
+// eigQL! applies its real rotations to those vectors. Stdlib pieces
+// restated: reflector! (x[i] /= xi1 with xi1 = x1 + nu, nu =
+// copysign(norm(x), real(x1)), tau = xi1/nu: the LAPACK zlarfg reflector
+// for complex x, H = I - tau v v', H' x = -nu e1), the Hermitian
+// matrix-vector product y = (A x) alpha (for complex, BLAS zhemv: the netlib
+// reference loops; the same loops serve quaternions, with the scalar applied
+// on the right as Julia's generic 5-argument mul! does) and dot(x, y) =
+// sum conj(x_i) y_i. Quaternion products do not commute, so every product is
+// written in the reference's order.
 typedef std::complex<double> zc;
 
-inline double norm2c(const zc* x, int64_t n, int64_t inc) {
+// A quaternion s + i x + j y + k z (Quaternions.jl's Quaternion{Float64}).
+struct Quat {
+  double s = 0, x = 0, y = 0, z = 0;
+  Quat() = default;
+  Quat(double a) : s(a) {}
+  Quat(double a, double b, double c, double d) : s(a), x(b), y(c), z(d) {}
+  Quat& operator+=(const Quat& q) {
+    s += q.s, x += q.x, y += q.y, z += q.z;
+    return *this;
+  }
+  Quat& operator-=(const Quat& q) {
+    s -= q.s, x -= q.x, y -= q.y, z -= q.z;
+    return *this;
+  }
+};
+inline Quat operator+(Quat a, const Quat& b) { return a += b; }
+inline Quat operator-(Quat a, const Quat& b) { return a -= b; }
+inline Quat operator-(const Quat& a) { return Quat(-a.s, -a.x, -a.y, -a.z); }
+inline Quat operator*(const Quat& p, const Quat& q) {  // Hamilton product
+  return Quat(p.s * q.s - p.x * q.x - p.y * q.y - p.z * q.z, p.s * q.x + p.x * q.s + p.y * q.z - p.z * q.y,
+              p.s * q.y - p.x * q.z + p.y * q.s + p.z * q.x, p.s * q.z + p.x * q.y - p.y * q.x + p.z * q.s);
+}
+inline Quat operator*(double a, const Quat& q) { return Quat(a * q.s, a * q.x, a * q.y, a * q.z); }
+inline Quat operator*(const Quat& q, double a) { return Quat(q.s * a, q.x * a, q.y * a, q.z * a); }
+inline Quat operator/(const Quat& q, double a) { return Quat(q.s / a, q.x / a, q.y / a, q.z / a); }
+
+inline zc conj_(const zc& a) { return std::conj(a); }
+inline Quat conj_(const Quat& a) { return Quat(a.s, -a.x, -a.y, -a.z); }
+inline double real_(const zc& a) { return a.real(); }
+inline double real_(const Quat& a) { return a.s; }
+inline double abs2_(const zc& a) { return std::norm(a); }
+inline double abs2_(const Quat& a) { return a.s * a.s + a.x * a.x + a.y * a.y + a.z * a.z; }
+inline double abs_(const zc& a) { return std::abs(a); }
+inline double abs_(const Quat& a) { return std::sqrt(abs2_(a)); }
+inline bool finite_(const zc& a) { return std::isfinite(a.real()) && std::isfinite(a.imag()); }
+inline bool finite_(const Quat& a) {
+  return std::isfinite(a.s) && std::isfinite(a.x) && std::isfinite(a.y) && std::isfinite(a.z);
+}
+// a / b = a inv(b) (Julia's right division)
+inline zc rdiv_(const zc& a, const zc& b) { return a / b; }
+inline Quat rdiv_(const Quat& a, const Quat& b) {
+  const double m = abs2_(b);
+  return a * Quat(b.s / m, -b.x / m, -b.y / m, -b.z / m);
+}
+
+template <class F> double norm2f(const F* x, int64_t n, int64_t inc) {
   double maxabs = 0;
   for (int64_t i = 0; i < n; i++) {
-    double a = std::abs(x[i * inc]);
+    double a = abs_(x[i * inc]);
     if (!(a <= maxabs)) maxabs = a;
   }
   if (maxabs == 0 || !std::isfinite(maxabs)) return maxabs;
   if (std::isfinite((double)n * maxabs * maxabs) && maxabs * maxabs != 0) {
     double sum = 0;
-    for (int64_t i = 0; i < n; i++) sum += std::norm(x[i * inc]);
+    for (int64_t i = 0; i < n; i++) sum += abs2_(x[i * inc]);
     return std::sqrt(sum);
   }
   double sum = 0;
-  for (int64_t i = 0; i < n; i++) sum += std::norm(x[i * inc] / maxabs);
+  for (int64_t i = 0; i < n; i++) sum += abs2_(x[i * inc] / maxabs);
   return maxabs * std::sqrt(sum);
 }
 
-inline zc reflector_c(zc* x, int64_t n, int64_t inc) {
-  if (n == 0) return 0;
-  zc xi1 = x[0];
-  double normu = norm2c(x, n, inc);
-  if (normu == 0) return 0;
-  double nu = std::copysign(normu, xi1.real());
-  xi1 += nu;
-  x[0] = -nu;
-  for (int64_t i = 1; i < n; i++) x[i * inc] /= xi1;
-  return xi1 / nu;
+template <class F> F reflector_f(F* x, int64_t n, int64_t inc) {
+  if (n == 0) return F(0);
+  F xi1 = x[0];
+  double normu = norm2f(x, n, inc);
+  if (normu == 0) return F(0);
+  double nu = std::copysign(normu, real_(xi1));
+  xi1 += F(nu);
+  x[0] = F(-nu);
+  for (int64_t i = 1; i < n; i++) x[i * inc] = rdiv_(x[i * inc], xi1);
+  return rdiv_(xi1, F(nu));
 }
 
-inline zc dotc(const zc* x, const zc* y, int64_t n) {
-  zc s = 0;
-  for (int64_t i = 0; i < n; i++) s += std::conj(x[i]) * y[i];
+template <class F> F dotc(const F* x, const F* y, int64_t n) {
+  F s(0);
+  for (int64_t i = 0; i < n; i++) s += conj_(x[i]) * y[i];
   return s;
 }
 
-// netlib reference zhemv, y = alpha*A*x (beta = 0), lower / upper triangle.
-inline void hemv_lower(int64_t n, zc alpha, const zc* A, int64_t lda, const zc* x, zc* y) {
-  for (int64_t i = 0; i < n; i++) y[i] = 0;
+// y = (A x) alpha (beta = 0), the Hermitian A given by its lower / upper
+// triangle; the netlib zhemv loops.
+template <class F> void hemv_lower(int64_t n, F alpha, const F* A, int64_t lda, const F* x, F* y) {
+  for (int64_t i = 0; i < n; i++) y[i] = F(0);
   for (int64_t j = 0; j < n; j++) {
-    zc temp1 = alpha * x[j], temp2 = 0;
-    y[j] += temp1 * A[j + j * lda].real();
+    F temp1 = x[j] * alpha, temp2(0);
+    y[j] += real_(A[j + j * lda]) * temp1;
     for (int64_t i = j + 1; i < n; i++) {
-      y[i] += temp1 * A[i + j * lda];
-      temp2 += std::conj(A[i + j * lda]) * x[i];
+      y[i] += A[i + j * lda] * temp1;
+      temp2 += conj_(A[i + j * lda]) * x[i];
     }
-    y[j] += alpha * temp2;
+    y[j] += temp2 * alpha;
   }
 }
-inline void hemv_upper(int64_t n, zc alpha, const zc* A, int64_t lda, const zc* x, zc* y) {
-  for (int64_t i = 0; i < n; i++) y[i] = 0;
+template <class F> void hemv_upper(int64_t n, F alpha, const F* A, int64_t lda, const F* x, F* y) {
+  for (int64_t i = 0; i < n; i++) y[i] = F(0);
   for (int64_t j = 0; j < n; j++) {
-    zc temp1 = alpha * x[j], temp2 = 0;
+    F temp1 = x[j] * alpha, temp2(0);
     for (int64_t i = 0; i < j; i++) {
-      y[i] += temp1 * A[i + j * lda];
-      temp2 += std::conj(A[i + j * lda]) * x[i];
+      y[i] += A[i + j * lda] * temp1;
+      temp2 += conj_(A[i + j * lda]) * x[i];
     }
-    y[j] += temp1 * A[j + j * lda].real() + alpha * temp2;
+    y[j] += real_(A[j + j * lda]) * temp1 + temp2 * alpha;
   }
 }
 
-// symtriLower! (:450-504) for complex AS: n-1 reflectors; d, e real.
-inline void symtri_lower_c(int64_t n, zc* AS, int64_t lda, zc* tau, double* d, double* e) {
-  std::vector<zc> u(std::max<int64_t>(n, 1));
-  for (int64_t i = 0; i < n; i++) at(AS, lda, i, i) = at(AS, lda, i, i).real();
+// symtriLower! (:450-504) for non-real AS: n-1 reflectors; d, e real.
+template <class F> void symtri_lower_f(int64_t n, F* AS, int64_t lda, F* tau, double* d, double* e) {
+  std::vector<F> u(std::max<int64_t>(n, 1));
+  for (int64_t i = 0; i < n; i++) at(AS, lda, i, i) = F(real_(at(AS, lda, i, i)));
   for (int64_t k = 0; k + 1 < n; k++) {  // k = 1:(n-1) in 1-based terms
     int64_t m = n - k - 1;
-    zc* x = &at(AS, lda, k + 1, k);
-    zc tk = reflector_c(x, m, 1);
+    F* x = &at(AS, lda, k + 1, k);
+    F tk = reflector_f(x, m, 1);
     tau[k] = tk;
-    zc tmp = x[0];
-    x[0] = 1;
-    zc* ut = u.data() + k + 1;
+    F tmp = x[0];
+    x[0] = F(1);
+    F* ut = u.data() + k + 1;
     hemv_lower(m, tk, &at(AS, lda, k + 1, k + 1), lda, x, ut);
-    double xi = (std::conj(tk) * dotc(x, ut, m)).real();
+    double xi = real_(conj_(tk) * dotc(x, ut, m));
     for (int64_t j = 0; j < m; j++) {
-      zc xj = x[j], uj = ut[j], xixj = xi * xj;
+      F xj = x[j], uj = ut[j], xixj = xi * xj;
       for (int64_t i = j; i < m; i++)
-        at(AS, lda, k + 1 + i, k + 1 + j) += x[i] * std::conj(xixj) - x[i] * std::conj(uj) - ut[i] * std::conj(xj);
+        at(AS, lda, k + 1 + i, k + 1 + j) += x[i] * conj_(xixj) - x[i] * conj_(uj) - ut[i] * conj_(xj);
     }
     x[0] = tmp;
   }
-  for (int64_t i = 0; i < n; i++) d[i] = at(AS, lda, i, i).real();
-  for (int64_t i = 0; i + 1 < n; i++) e[i] = at(AS, lda, i + 1, i).real();
+  for (int64_t i = 0; i < n; i++) d[i] = real_(at(AS, lda, i, i));
+  for (int64_t i = 0; i + 1 < n; i++) e[i] = real_(at(AS, lda, i + 1, i));
 }
 
-// symtriUpper! (:507-564) for complex AS.
-inline void symtri_upper_c(int64_t n, zc* AS, int64_t lda, zc* tau, double* d, double* e) {
-  std::vector<zc> u(std::max<int64_t>(n, 1));
-  for (int64_t i = 0; i < n; i++) at(AS, lda, i, i) = at(AS, lda, i, i).real();
+// symtriUpper! (:507-564) for non-real AS.
+template <class F> void symtri_upper_f(int64_t n, F* AS, int64_t lda, F* tau, double* d, double* e) {
+  std::vector<F> u(std::max<int64_t>(n, 1));
+  for (int64_t i = 0; i < n; i++) at(AS, lda, i, i) = F(real_(at(AS, lda, i, i)));
   for (int64_t k = 0; k + 1 < n; k++) {
     int64_t m = n - k - 1;
-    zc* x = &at(AS, lda, 0, n - k - 1);
-    zc tk = reflector_c(x + (m - 1), m, -1);  // the reversed view AS[(n-k):-1:1, n-k+1]
+    F* x = &at(AS, lda, 0, n - k - 1);
+    F tk = reflector_f(x + (m - 1), m, -1);  // the reversed view AS[(n-k):-1:1, n-k+1]
     tau[k] = tk;
-    zc tmp = x[m - 1];
-    x[m - 1] = 1;
+    F tmp = x[m - 1];
+    x[m - 1] = F(1);
     hemv_upper(m, tk, AS, lda, x, u.data());
-    double xi = (std::conj(tk) * dotc(x, u.data(), m)).real();
+    double xi = real_(conj_(tk) * dotc(x, u.data(), m));
     for (int64_t j = 0; j < m; j++) {
-      zc xj = x[j], uj = u[j], xixj = xi * xj;
-      for (int64_t i = 0; i <= j; i++)
-        at(AS, lda, i, j) += x[i] * std::conj(xixj) - x[i] * std::conj(uj) - u[i] * std::conj(xj);
+      F xj = x[j], uj = u[j], xixj = xi * xj;
+      for (int64_t i = 0; i <= j; i++) at(AS, lda, i, j) += x[i] * conj_(xixj) - x[i] * conj_(uj) - u[i] * conj_(xj);
     }
     x[m - 1] = tmp;
   }
-  for (int64_t i = 0; i < n; i++) d[i] = at(AS, lda, i, i).real();
-  for (int64_t i = 0; i + 1 < n; i++) e[i] = at(AS, lda, i, i + 1).real();
+  for (int64_t i = 0; i < n; i++) d[i] = real_(at(AS, lda, i, i));
+  for (int64_t i = 0; i + 1 < n; i++) e[i] = real_(at(AS, lda, i, i + 1));
 }
 
-// lmul!(Q::EigenQ, B) (:23-60) for complex factors: B (n x ncols) <- Q*B,
-// with h' * b = zdotc(h, b).
-inline void eigenq_lmul_c(char uplo, int64_t n, zc* F, int64_t ldf, const zc* tau, zc* B, int64_t ldb,
-                          int64_t ncols) {
+// lmul!(Q::EigenQ, B) (:23-60) for non-real factors: B (n x ncols) <- Q*B,
+// tmp = tau * (h' * b), b -= h * tmp.
+template <class F>
+void eigenq_lmul_f(char uplo, int64_t n, F* Fm, int64_t ldf, const F* tau, F* B, int64_t ldb, int64_t ncols) {
   for (int64_t k = n - 1; k >= 1; k--) {  // 1-based k over length(tau) = n-1
     const int64_t len = n - k;
-    zc* h = uplo == 'L' ? &at(F, ldf, k, k - 1) : &at(F, ldf, 0, n - k);
+    F* h = uplo == 'L' ? &at(Fm, ldf, k, k - 1) : &at(Fm, ldf, 0, n - k);
     const int64_t head = uplo == 'L' ? 0 : len - 1;
-    const zc t = tau[k - 1];
-    zc tmp = h[head];
-    h[head] = 1;
+    const F t = tau[k - 1];
+    F tmp = h[head];
+    h[head] = F(1);
     for (int64_t j = 0; j < ncols; j++) {
-      zc* Bj = uplo == 'L' ? &at(B, ldb, k, j) : &at(B, ldb, 0, j);
+      F* Bj = uplo == 'L' ? &at(B, ldb, k, j) : &at(B, ldb, 0, j);
       tmp = t * dotc(h, Bj, len);
       for (int64_t i = 0; i < len; i++) Bj[i] -= h[i] * tmp;
     }
@@ -852,30 +903,31 @@ inline void eigenq_lmul_c(char uplo, int64_t n, zc* F, int64_t ldf, const zc* ta
   }
 }
 
-// _eigen!/_eigvals!(Hermitian{<:Complex}): symtri!, then eigvalsPWK!
-// (values) or Array(Q) + eigQL! (vectors), then sorteig!. Returns info.
-inline int heev(Opts<double>& o, char jobz, char uplo, int64_t n, zc* A, int64_t lda, double* w, zc* V, int64_t ldv) {
+// _eigen!/_eigvals!(Hermitian{F}): symtri!, then eigvalsPWK! (values) or
+// Array(Q) + eigQL! (vectors), then sorteig!. Returns info.
+template <class F>
+int heev(Opts<double>& o, char jobz, char uplo, int64_t n, F* A, int64_t lda, double* w, F* V, int64_t ldv) {
   if (n == 0) return 0;
   for (int64_t j = 0; j < n; j++) {
     int64_t i0 = uplo == 'L' ? j : 0, i1 = uplo == 'L' ? n : j + 1;
     for (int64_t i = i0; i < i1; i++)
-      if (!std::isfinite(A[i + j * lda].real()) || !std::isfinite(A[i + j * lda].imag())) {
+      if (!finite_(A[i + j * lda])) {
         for (int64_t q = 0; q < n; q++) w[q] = std::numeric_limits<double>::quiet_NaN();
         return -1;
       }
   }
-  std::vector<zc> tau(std::max<int64_t>(n - 1, 1));
+  std::vector<F> tau(std::max<int64_t>(n - 1, 1));
   std::vector<double> e(std::max<int64_t>(n - 1, 1));
-  if (uplo == 'L') symtri_lower_c(n, A, lda, tau.data(), w, e.data());
-  else symtri_upper_c(n, A, lda, tau.data(), w, e.data());
+  if (uplo == 'L') symtri_lower_f(n, A, lda, tau.data(), w, e.data());
+  else symtri_upper_f(n, A, lda, tau.data(), w, e.data());
   int info;
   if (jobz == 'N') {
     info = eigvals_pwk(o, w, e.data(), n);
     sorteig<double, double>(w, n, nullptr, 0, 0);
   } else {
     for (int64_t j = 0; j < n; j++)
-      for (int64_t i = 0; i < n; i++) V[i + j * ldv] = (i == j) ? 1.0 : 0.0;
-    eigenq_lmul_c(uplo, n, A, lda, tau.data(), V, ldv, n);
+      for (int64_t i = 0; i < n; i++) V[i + j * ldv] = F(i == j ? 1.0 : 0.0);
+    eigenq_lmul_f(uplo, n, A, lda, tau.data(), V, ldv, n);
     info = eig_ql(o, w, e.data(), n, V, ldv, n);
     sorteig(w, n, V, ldv, n);
   }

@@ -6,6 +6,7 @@ CPU-baseline leg of bench.py; the shipped GPU path never calls it.
 Functions mirror the reference entry points:
   syev(A, jobz, uplo)   -> _eigen!/_eigvals!(Hermitian(A, uplo))   :566-618
   heev(A, jobz, uplo)   -> the same for complex Hermitian A (T <: Complex, :462)
+  heev_quaternion(...)  -> the same for quaternion Hermitian A ((n, n, 4) arrays)
   stev(d, e, jobz)      -> _eigen!/_eigvals!(SymTridiagonal(d, e)) :566,602-612
   eigql(d, e, V)        -> eigQL!/eigQR! on explicit vectors       :221-340
   symtri(A, uplo)       -> symtri!                                  :446-564
@@ -64,6 +65,11 @@ def lib():
         L.gla_oracle_heev_z.argtypes = [_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, _d]
         L.gla_oracle_symtri_z.argtypes = [_ch, _i64, _vp, _i64, _vp, _vp, _vp]
         L.gla_oracle_symtri_z.restype = None
+        L.gla_oracle_heev_q.argtypes = [_ch, _ch, _i64, _vp, _i64, _vp, _vp, _i64, _d]
+        L.gla_oracle_symtri_qt.argtypes = [_ch, _i64, _vp, _i64, _vp, _vp, _vp]
+        L.gla_oracle_symtri_qt.restype = None
+        L.gla_oracle_eigenq_lmul_qt.argtypes = [_ch, _i64, _vp, _i64, _vp, _vp, _i64, _i64]
+        L.gla_oracle_eigenq_lmul_qt.restype = None
         _lib = L
     return _lib
 
@@ -120,6 +126,47 @@ def symtri_complex(A, uplo="L"):
     e = np.zeros(max(n - 1, 1))
     lib().gla_oracle_symtri_z(uplo.encode(), n, _p(F), max(n, 1), _p(tau), _p(d), _p(e))
     return F, tau[: n - 1], d, e[: n - 1]
+
+
+def _qcols(A):
+    """(n, m, 4) quaternion array -> column-major storage, 4 doubles per entry."""
+    return np.ascontiguousarray(np.asarray(A, dtype=np.float64).transpose(1, 0, 2))
+
+
+def heev_quaternion(A, jobz="V", uplo="L", tol=0.0):
+    """_eigen!/_eigvals!(Hermitian(A, uplo)) for a quaternion matrix A given
+    as an (n, n, 4) array of (s, i, j, k) components. Returns (w, V, info),
+    V as (n, n, 4); A is copied."""
+    X = _qcols(A)
+    n = X.shape[0]
+    w = np.zeros(n)
+    V = np.zeros((max(n, 1), max(n, 1), 4))
+    info = lib().gla_oracle_heev_q(jobz.encode(), uplo.encode(), n, _p(X), max(n, 1), _p(w), _p(V), max(n, 1), tol)
+    return w, (V[:n, :n].transpose(1, 0, 2).copy() if jobz == "V" else None), info
+
+
+def symtri_quaternion(A, uplo="L"):
+    """symtri!(Hermitian(A, uplo)) for a quaternion (n, n, 4) array: returns
+    (factors (n, n, 4), tau (n-1, 4), d, e)."""
+    X = _qcols(A)
+    n = X.shape[0]
+    tau = np.zeros((max(n - 1, 1), 4))
+    d = np.zeros(n)
+    e = np.zeros(max(n - 1, 1))
+    lib().gla_oracle_symtri_qt(uplo.encode(), n, _p(X), max(n, 1), _p(tau), _p(d), _p(e))
+    return X.transpose(1, 0, 2).copy(), tau[: n - 1], d, e[: n - 1]
+
+
+def eigenq_lmul_quaternion(uplo, F, tau, B):
+    """lmul!(EigenQ(uplo, F, tau), B) for quaternion factors and B ((n, m, 4)
+    arrays); returns Q*B."""
+    Fc = _qcols(F)
+    Bc = _qcols(B)
+    n, m = Bc.shape[1], Bc.shape[0]
+    t = np.zeros((max(n - 1, 1), 4))
+    t[: n - 1] = tau
+    lib().gla_oracle_eigenq_lmul_qt(uplo.encode(), n, _p(Fc), max(n, 1), _p(t), _p(Bc), max(n, 1), m)
+    return Bc.transpose(1, 0, 2).copy()
 
 
 def syev_quad(A, jobz="V", uplo="L", use_qr=False, generic_givens=False):

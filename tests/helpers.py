@@ -95,3 +95,65 @@ def analytic_adjoint(V, w, wbar, Vbar, gap_rel=1e-10):
     np.fill_diagonal(F, 0.0)
     M = 0.5 * (F * G + (F * G).T) + np.diag(wbar)
     return V @ M @ V.T
+
+
+# ---- quaternion matrices as (m, n, 4) arrays of (s, i, j, k) components ----
+
+def qmul(A, B):
+    """Quaternion matrix product (m, k, 4) x (k, n, 4), Hamilton's rules."""
+    a0, a1, a2, a3 = (A[..., m] for m in range(4))
+    b0, b1, b2, b3 = (B[..., m] for m in range(4))
+    return np.stack([a0 @ b0 - a1 @ b1 - a2 @ b2 - a3 @ b3,
+                     a0 @ b1 + a1 @ b0 + a2 @ b3 - a3 @ b2,
+                     a0 @ b2 - a1 @ b3 + a2 @ b0 + a3 @ b1,
+                     a0 @ b3 + a1 @ b2 - a2 @ b1 + a3 @ b0], -1)
+
+
+def qH(A):
+    B = np.swapaxes(A, 0, 1).copy()
+    B[..., 1:] *= -1
+    return B
+
+
+def qeye(n):
+    Z = np.zeros((n, n, 4))
+    Z[..., 0] = np.eye(n)
+    return Z
+
+
+def chi(A):
+    Z1 = A[..., 0] + 1j * A[..., 1]
+    Z2 = A[..., 2] + 1j * A[..., 3]
+    return np.block([[Z1, Z2], [-Z2.conj(), Z1.conj()]])
+
+
+def qnorm(A):
+    return np.linalg.norm(chi(A), 2)
+
+
+def qunitary(n, rng):
+    """A random unitary quaternion matrix (Gram-Schmidt on Gaussian columns)."""
+    X = rng.standard_normal((n, n, 4))
+    Q = np.zeros_like(X)
+    for j in range(n):
+        r = X[:, j:j + 1]
+        for _ in range(2):
+            for q in range(j):
+                v = Q[:, q:q + 1]
+                r = r - qmul(v, qmul(qH(v), r))
+        Q[:, j:j + 1] = r / np.sqrt((r ** 2).sum())
+    return Q
+
+
+def qherm_spectrum(lam, rng):
+    n = len(lam)
+    U = qunitary(n, rng)
+    D = np.zeros((n, n, 4))
+    D[..., 0] = np.diag(lam)
+    A = qmul(qmul(U, D), qH(U))
+    return (A + qH(A)) / 2
+
+
+def qherm_random(n, rng):
+    B = rng.standard_normal((n, n, 4))
+    return (B + qH(B)) / 2

@@ -255,3 +255,40 @@ def test_complex_path_on_real_input():
     assert info == 0
     assert np.abs(wz - wr).max() <= 8 * 40 * 2.0 ** -52 * np.linalg.norm(A, 2)
     assert np.linalg.norm(A @ Vz - Vz * wz, 2) / np.linalg.norm(A, 2) <= 1e-13
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_quaternion_hermitian_reference_testset(uplo):
+    # test/eigenselfadjoint.jl:54-84, n = 50: Hermitian(V diag(lambda) V', uplo)
+    # with V a random unitary quaternion matrix and lambda = 10 .^ range(-8, 0, n)
+    from helpers import qeye, qH, qherm_spectrum, qmul, qnorm
+    n = 50
+    lam = 10.0 ** np.linspace(-8, 0, n)
+    A = qherm_spectrum(lam, np.random.default_rng(54))
+    vals, vecs, info = O.heev_quaternion(A, "V", uplo)
+    assert info == 0 and np.all(np.diff(vals) >= 0)
+    # symtri!: Q == lmul!(Q, I), Q'Q ~ QQ' ~ I, Q' A Q ~ T (:61-68)
+    F, tau, d, e = O.symtri_quaternion(A, uplo)
+    Q = O.eigenq_lmul_quaternion(uplo, F, tau, qeye(n))
+    assert qnorm(qmul(qH(Q), Q) - qeye(n)) <= 1e-13 and qnorm(qmul(Q, qH(Q)) - qeye(n)) <= 1e-13
+    T = np.zeros((n, n, 4))
+    T[..., 0] = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    assert qnorm(qmul(qmul(qH(Q), A), Q) - T) <= 1e-13
+    # default: A vecs ~ vecs diag(vals), eigvals(A) ~ vals, vals ~ lambda at rtol 1e-13 n, vecs'vecs ~ I
+    assert qnorm(qmul(A, vecs) - vecs * vals[None, :, None]) <= 1e-13
+    wn, _, info = O.heev_quaternion(A, "N", uplo)
+    assert info == 0 and np.linalg.norm(wn - vals) <= 1e-13 * np.linalg.norm(vals)
+    assert np.linalg.norm(vals - lam) <= 1e-13 * n * max(np.linalg.norm(vals), np.linalg.norm(lam))
+    assert qnorm(qmul(qH(vecs), vecs) - qeye(n)) <= 1e-13
+
+
+def test_quaternion_path_on_complex_input():
+    # a complex Hermitian matrix as a quaternion one (j, k parts zero): the
+    # quaternion path's values equal the complex path's to rounding
+    A = herm(30, 12)
+    Aq = np.zeros((30, 30, 4))
+    Aq[..., 0], Aq[..., 1] = A.real, A.imag
+    wq, Vq, info = O.heev_quaternion(Aq)
+    wz, _, _ = O.heev(A)
+    assert info == 0
+    assert np.abs(wq - wz).max() <= 8 * 30 * 2.0 ** -52 * np.linalg.norm(A, 2)

@@ -4,7 +4,9 @@ gla_qheev. The checker is independent of the device path's real embedding:
 quaternion products are written out from the Hamilton product, and the
 reference eigenvalues come from LAPACK (scipy eigh, zheevd) on the complex
 adjoint matrix chi(A) = [[Z1, Z2], [-conj Z2, conj Z1]] (A = Z1 + Z2 j), whose
-eigenvalues are those of A, each twice. Norms of quaternion matrices are the
+eigenvalues are those of A, each twice, and from the oracle's restatement of
+the reference's own quaternion path (values, and eigenvectors up to a unit
+quaternion factor where the eigenvalue is separated). Norms of quaternion matrices are the
 spectral norms of their chi.
 Tolerances: eigenvalues within 32 n eps ||A|| (the real embedding has order
 4n); residual ||AV - V diag(w)||/||A|| and ||V^H V - I|| <= 1e-13; the
@@ -12,6 +14,9 @@ reference's prescribed spectrum at its rtol 1e-13 n."""
 import numpy as np
 import pytest
 import scipy.linalg as sl
+
+from helpers import chi, qeye, qH, qherm_random, qherm_spectrum, qmul, qnorm
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -25,66 +30,6 @@ def G():
         pytest.skip("no CUDA device")
     import glagpu
     return glagpu
-
-
-def qmul(A, B):
-    """Quaternion matrix product (m, k, 4) x (k, n, 4), Hamilton's rules."""
-    a0, a1, a2, a3 = (A[..., m] for m in range(4))
-    b0, b1, b2, b3 = (B[..., m] for m in range(4))
-    return np.stack([a0 @ b0 - a1 @ b1 - a2 @ b2 - a3 @ b3,
-                     a0 @ b1 + a1 @ b0 + a2 @ b3 - a3 @ b2,
-                     a0 @ b2 - a1 @ b3 + a2 @ b0 + a3 @ b1,
-                     a0 @ b3 + a1 @ b2 - a2 @ b1 + a3 @ b0], -1)
-
-
-def qH(A):
-    B = np.swapaxes(A, 0, 1).copy()
-    B[..., 1:] *= -1
-    return B
-
-
-def qeye(n):
-    Z = np.zeros((n, n, 4))
-    Z[..., 0] = np.eye(n)
-    return Z
-
-
-def chi(A):
-    Z1 = A[..., 0] + 1j * A[..., 1]
-    Z2 = A[..., 2] + 1j * A[..., 3]
-    return np.block([[Z1, Z2], [-Z2.conj(), Z1.conj()]])
-
-
-def qnorm(A):
-    return np.linalg.norm(chi(A), 2)
-
-
-def qunitary(n, rng):
-    """A random unitary quaternion matrix (Gram-Schmidt on Gaussian columns)."""
-    X = rng.standard_normal((n, n, 4))
-    Q = np.zeros_like(X)
-    for j in range(n):
-        r = X[:, j:j + 1]
-        for _ in range(2):
-            for q in range(j):
-                v = Q[:, q:q + 1]
-                r = r - qmul(v, qmul(qH(v), r))
-        Q[:, j:j + 1] = r / np.sqrt((r ** 2).sum())
-    return Q
-
-
-def qherm_spectrum(lam, rng):
-    n = len(lam)
-    U = qunitary(n, rng)
-    D = np.zeros((n, n, 4))
-    D[..., 0] = np.diag(lam)
-    A = qmul(qmul(U, D), qH(U))
-    return (A + qH(A)) / 2
-
-
-def qherm_random(n, rng):
-    B = rng.standard_normal((n, n, 4))
-    return (B + qH(B)) / 2
 
 
 def ref_values(A):
@@ -176,3 +121,25 @@ def test_host_entry_and_arguments(G):
     assert L.gla_qheev_host(b"V", b"L", 4097, p(Ac), 4097, p(w), p(Vc), 4097, C.byref(info)) == -3
     with pytest.raises(Exception):
         G.QuaternionMatrix(np.zeros((3, 3, 3)))
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("n", [4, 50, 120])
+def test_against_oracle_restatement(G, n, uplo):
+    A = qherm_random(n, np.random.default_rng(600 + n))
+    vals, vecs = G.eigen(G.QuaternionMatrix(A), uplo=uplo)
+    wo, Vo, info = O.heev_quaternion(A, "V", uplo)
+    assert info == 0
+    nA = qnorm(A)
+    assert np.abs(vals - wo).max() <= 32 * n * EPS64 * nA
+    # v_gpu = v_oracle q with |q| = 1 where the eigenvalue is separated: |v_gpu^H v_oracle| = 1
+    gaps = np.full(n, np.inf)
+    if n > 1:
+        dw = np.diff(wo)
+        gaps[:-1] = np.minimum(gaps[:-1], dw)
+        gaps[1:] = np.minimum(gaps[1:], dw)
+    sep = gaps > 1e-6 * nA
+    inner = np.stack([qmul(qH(vecs[:, j:j + 1]), Vo[:, j:j + 1])[0, 0] for j in range(n)])
+    overlap = np.sqrt((inner ** 2).sum(axis=1))
+    assert sep.sum() >= n // 2
+    assert np.all(overlap[sep] >= 1 - 1e-8)
