@@ -356,6 +356,7 @@ def run_ours(args):
         achieved = ops / (refine_ms * 1e-3) / 1e12 if refine_ms > 0 else 0.0
         peak_ops = sg / 2.0
         cpu = cpu_baseline(ns, mats)
+        lapack = lapack_baseline(ns, mats)
         line = {
             "metric": METRIC,
             "value": G["eigh_per_s"],
@@ -387,6 +388,7 @@ def run_ours(args):
             "roofline_large": large_roofline(large, measured_peaks_file()),
             "fp64_dgemm_tflops_measured": peak,
             "cpu_baseline": cpu,
+            "cpu_lapack": lapack,
             "e2e": {"value": ws * len(ns) * args.steps / el_e2e, "unit": "eigh/s",
                     "h2d_bytes_per_step": int(A64.nbytes),
                     "d2h_bytes_per_step": int(8 * nA + 8 * nW + 4 * len(ns))},
@@ -744,6 +746,74 @@ def cpu_baseline(ns, mats, budget_s=15.0):
                       f"{nth} OpenMP threads (one matrix per thread)"}
 
 
+def lapack_child(m):
+    """Body of `bench.py --cpu-lapack M`, run in a fresh process whose
+    environment pins BLAS to one thread: scipy.linalg.eigh (LAPACK dsyevr,
+    the routine stdlib Julia's Float64 eigen(Hermitian) calls) over the first
+    M workload matrices, one forked worker per core (this process holds no
+    GPU context), wall time from a common start barrier to the last worker's
+    end. Every wait is bounded. Prints one JSON object."""
+    import multiprocessing as mp
+
+    import scipy
+    import scipy.linalg as sl
+    ns, mats = workload()
+    sample = mats[:m]
+    nth = os.cpu_count() or 1
+    ctx = mp.get_context("fork")
+    barrier = ctx.Barrier(nth)
+    q = ctx.Queue()
+
+    def work(i):
+        part = sample[i::nth]
+        if part:
+            sl.eigh(part[0], driver="evr", check_finite=False)  # load LAPACK before the clock starts
+        barrier.wait(timeout=120)
+        t0 = time.monotonic()
+        for M in part:
+            sl.eigh(M, driver="evr", check_finite=False)
+        q.put((t0, time.monotonic()))
+
+    procs = [ctx.Process(target=work, args=(i,), daemon=True) for i in range(nth)]
+    for p in procs:
+        p.start()
+    try:
+        spans = [q.get(timeout=240) for _ in procs]
+    finally:
+        for p in procs:
+            p.join(timeout=5)
+            if p.is_alive():
+                p.terminate()
+    wall = max(b for _, b in spans) - min(a for a, _ in spans)
+    print(json.dumps({"value": m / wall, "unit": "eigh/s", "cores": nth, "kind": "lapack",
+                      "sample": f"first {m} of the {len(ns)} workload matrices, scipy {scipy.__version__} "
+                                f"linalg.eigh (LAPACK dsyevr, eigenvalues and vectors), {nth} processes x "
+                                "1 BLAS thread"}), flush=True)
+
+
+def lapack_baseline(ns, mats, budget_s=5.0):
+    """LAPACK on the host cores (see lapack_child), in a subprocess with a
+    time limit; a sample sized for about budget_s seconds of work. Returns
+    the child's JSON object, or {"unavailable": reason}."""
+    import scipy.linalg as sl
+    nth = os.cpu_count() or 1
+    k = min(len(mats), 64)
+    t0 = time.perf_counter()
+    for M in mats[:k]:
+        sl.eigh(M, driver="evr", check_finite=False)
+    per = (time.perf_counter() - t0) / max(k, 1)
+    m = int(min(len(ns), max(k, budget_s * nth / max(per, 1e-9))))
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    try:
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-lapack", str(m)], env=env,
+                           capture_output=True, text=True, timeout=300)
+        if r.returncode != 0:
+            return {"unavailable": f"LAPACK baseline process exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    except (subprocess.TimeoutExpired, ValueError, IndexError) as e:
+        return {"unavailable": f"LAPACK baseline failed: {type(e).__name__}"}
+
+
 def time_oracle(ns, mats, nth):
     from oracle import oracle as O
     aoff = np.concatenate([[0], np.cumsum(ns * ns)[:-1]]).astype(np.int64)
@@ -807,6 +877,8 @@ def main():
                     help="profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix only")
     ap.add_argument("--c4", action="store_true",
                     help="only the differentiation workload (forward + adjoint, eager and one CUDA graph)")
+    ap.add_argument("--cpu-lapack", type=int, default=0,
+                    help="internal: the LAPACK CPU baseline over the first N workload matrices (one JSON object)")
     ap.add_argument("--ozaki", type=int, default=0,
                     help="profiling: time only the tensor-core double-float GEMM (gla_gemm_df) at this order")
     args = ap.parse_args()
@@ -816,6 +888,9 @@ def main():
         import torch
         import glagpu
         print(json.dumps(time_ozaki(torch, glagpu, "cuda", args.ozaki)), flush=True)
+        return
+    if args.cpu_lapack:
+        lapack_child(args.cpu_lapack)
         return
     if args.c4:
         import torch
