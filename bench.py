@@ -810,7 +810,7 @@ def lapack_baseline(ns, mats, budget_s=5.0):
         if r.returncode != 0:
             return {"unavailable": f"LAPACK baseline process exited {r.returncode}: {r.stderr.strip()[-200:]}"}
         return json.loads(r.stdout.strip().splitlines()[-1])
-    except (subprocess.TimeoutExpired, ValueError, IndexError) as e:
+    except Exception as e:  # a side baseline: report, never fail the benchmark
         return {"unavailable": f"LAPACK baseline failed: {type(e).__name__}"}
 
 
