@@ -795,16 +795,16 @@ def lapack_baseline(ns, mats, budget_s=5.0):
     """LAPACK on the host cores (see lapack_child), in a subprocess with a
     time limit; a sample sized for about budget_s seconds of work. Returns
     the child's JSON object, or {"unavailable": reason}."""
-    import scipy.linalg as sl
-    nth = os.cpu_count() or 1
-    k = min(len(mats), 64)
-    t0 = time.perf_counter()
-    for M in mats[:k]:
-        sl.eigh(M, driver="evr", check_finite=False)
-    per = (time.perf_counter() - t0) / max(k, 1)
-    m = int(min(len(ns), max(k, budget_s * nth / max(per, 1e-9))))
-    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
     try:
+        import scipy.linalg as sl
+        nth = os.cpu_count() or 1
+        k = min(len(mats), 64)
+        t0 = time.perf_counter()
+        for M in mats[:k]:
+            sl.eigh(M, driver="evr", check_finite=False)
+        per = (time.perf_counter() - t0) / max(k, 1)
+        m = int(min(len(ns), max(k, budget_s * nth / max(per, 1e-9))))
+        env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-lapack", str(m)], env=env,
                            capture_output=True, text=True, timeout=300)
         if r.returncode != 0:
