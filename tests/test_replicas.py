@@ -1,8 +1,10 @@
-"""The multi-GPU form of the benchmark is independent replicas: each rank
-solves its own seeded batch, the ranks meet only at barriers, and the job's
-time is the slowest rank's. This covers that host logic with two gloo ranks
-on the CPU (bench.replica_seed, bench.max_over_ranks) and the reference arm's
-rank-0-only output, without a GPU."""
+"""The benchmark's host logic, without a GPU. Its multi-GPU form is
+independent replicas: each rank solves its own seeded batch, the ranks meet
+only at barriers, and the job's time is the slowest rank's. Two gloo ranks on
+the CPU cover bench.replica_seed and bench.max_over_ranks; the reference arm
+(the CPU restatement on the host cores) is run end to end for its JSON line
+and its rank-0-only output, and the LAPACK side baseline's child for its
+JSON object."""
 import io
 import os
 import socket
@@ -79,3 +81,33 @@ def test_reference_arm_prints_on_rank_zero_only(monkeypatch):
     with redirect_stdout(buf):
         bench.run_reference(Args())
     assert buf.getvalue() == ""
+
+
+def test_reference_arm_json_line():
+    # the reference arm runs on the host cores only: its JSON line carries
+    # the contract's keys, with the CPU baseline describing this run
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+
+
+def test_lapack_side_baseline_child():
+    import json
+    import subprocess
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--cpu-lapack", "64"], capture_output=True,
+                       text=True, timeout=300, cwd=ROOT, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["kind"] == "lapack" and out["value"] > 0 and out["cores"] >= 1
