@@ -818,8 +818,13 @@ int single_entry(int prec, char jobz, char uplo, int64_t n, int flags, SingleEnt
   int rc = gla_plan_create(&e.plan, prec, jobz, uplo, 1, &n, 0.0, flags);
   if (rc) return rc;
   const size_t el = prec == GLA_PREC_F32 ? 4 : 8;
-  GLA_CUDA(cudaMalloc(&e.buf, el * (size_t)(n * n + 2 * n + 2)));
-  GLA_CUDA(cudaMalloc((void**)&e.dinfo, sizeof(int)));
+  cudaError_t ce = cudaMalloc(&e.buf, el * (size_t)(n * n + 2 * n + 2));
+  if (ce == cudaSuccess) ce = cudaMalloc((void**)&e.dinfo, sizeof(int));
+  if (ce != cudaSuccess) {  // nothing is cached on failure
+    cudaFree(e.buf);
+    gla_plan_destroy(e.plan);
+    return -1000 - (int)ce;
+  }
   auto r = g_single.emplace(k, e);
   *out = &r.first->second;
   return 0;
