@@ -55,6 +55,16 @@ constexpr int kMaxBuckets = 8;      // size buckets of width 16 over (0, 128]
     if (e_ != cudaSuccess) return -1000 - (int)e_;   \
   } while (0)
 
+// A lazily allocated cache buffer: *slot is set only on success, so a failed
+// allocation leaves it empty and a later call retries.
+template <class P>
+cudaError_t cache_alloc(P** slot, size_t bytes) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e == cudaSuccess) *slot = static_cast<P*>(q);
+  return e;
+}
+
 struct Bucket {
   int nmax;   // largest order in the bucket
   int nt;     // threads per CTA (apply)
@@ -647,11 +657,19 @@ int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* 
   cudaStream_t st = (cudaStream_t)stream;
   const size_t ioe = p->io_elem();
   const size_t abytes = ioe * std::max<int64_t>(p->a_elems, 1), wbytes = ioe * std::max<int64_t>(p->w_elems, 1);
-  if (!p->h_A) {
-    GLA_CUDA(cudaMalloc(&p->h_A, abytes));
-    GLA_CUDA(cudaMalloc(&p->h_w, wbytes));
-    GLA_CUDA(cudaMalloc(&p->h_V, p->jobz == 'V' ? abytes : 16));
-    GLA_CUDA(cudaMalloc((void**)&p->h_info, sizeof(int) * std::max<int64_t>(p->batch, 1)));
+  if (!p->h_info) {  // all four staging buffers, or none (a later call retries)
+    cudaError_t e = cudaMalloc(&p->h_A, abytes);
+    if (e == cudaSuccess) e = cudaMalloc(&p->h_w, wbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&p->h_V, p->jobz == 'V' ? abytes : 16);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&p->h_info, sizeof(int) * std::max<int64_t>(p->batch, 1));
+    if (e != cudaSuccess) {
+      cudaFree(p->h_A);
+      cudaFree(p->h_w);
+      cudaFree(p->h_V);
+      p->h_A = p->h_w = p->h_V = nullptr;
+      p->h_info = nullptr;
+      return -1000 - (int)e;
+    }
   }
   GLA_CUDA(cudaMemcpyAsync(p->h_A, A_host, ioe * p->a_elems, cudaMemcpyHostToDevice, st));
   int rc = plan_execute(p, p->h_A, p->h_w, p->h_V, p->h_info, st);
@@ -678,14 +696,14 @@ int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const doubl
   const double gr = gap_rel > 0 ? gap_rel : 1e-10;
   cudaStream_t st = (cudaStream_t)stream;
   if (p->nwork > 0) {  // orders <= GLA_MAX_SMALL_N: one CTA per matrix
-    if (!p->d_adj) GLA_CUDA(cudaMalloc((void**)&p->d_adj, adjoint_workspace_bytes(p->a_elems)));
+    if (!p->d_adj) GLA_CUDA(cache_alloc(&p->d_adj, adjoint_workspace_bytes(p->a_elems)));
     GLA_CUDA(launch_adjoint(p->nwork, st, p->d_desc, p->d_perm_bucket, w, V, wbar, Vbar, Abar, p->d_adj, p->a_elems,
                             gr));
   }
   if (!p->large_idx.empty()) {  // larger orders: three FP64 GEMMs each, one shared workspace
     int nl = 0;
     for (int b : p->large_idx) nl = std::max(nl, (int)p->n[b]);
-    if (!p->d_adj_large) GLA_CUDA(cudaMalloc((void**)&p->d_adj_large, sizeof(double) * large_adjoint_workspace_elems(nl)));
+    if (!p->d_adj_large) GLA_CUDA(cache_alloc(&p->d_adj_large, sizeof(double) * large_adjoint_workspace_elems(nl)));
     for (int b : p->large_idx) {
       const int nb = (int)p->n[b];
       int64_t aoff = 0, woff = 0;
@@ -713,7 +731,7 @@ int gla_plan_adjoint_host(gla_plan_t p, const double* w, const double* V, const 
   if (p->a_elems == 0) return 0;
   cudaStream_t st = (cudaStream_t)stream;
   const size_t ab = sizeof(double) * p->a_elems, wb = sizeof(double) * p->w_elems;
-  if (!p->h_adj) GLA_CUDA(cudaMalloc((void**)&p->h_adj, 3 * ab + 2 * wb));
+  if (!p->h_adj) GLA_CUDA(cache_alloc(&p->h_adj, 3 * ab + 2 * wb));
   double* dV = p->h_adj;
   double* dVbar = dV + p->a_elems;
   double* dAbar = dVbar + p->a_elems;

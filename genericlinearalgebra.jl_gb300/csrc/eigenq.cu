@@ -228,7 +228,11 @@ int gla_dormtr(char side, char uplo, char trans, int64_t m, int64_t n, const dou
   const double* F = A;
   long long ldf = lda;
   if (upper) {
-    if (!q->frev) Q_CUDA(cudaMalloc((void**)&q->frev, sizeof(double) * (size_t)nq * nq));
+    if (!q->frev) {  // set only on success, so a failed allocation is retried
+      void* f = nullptr;
+      Q_CUDA(cudaMalloc(&f, sizeof(double) * (size_t)nq * nq));
+      q->frev = static_cast<double*>(f);
+    }
     k_q_revfactors<<<dim3((nqi + 255) / 256, nqi), 256, 0, st>>>(A, lda, nqi, q->frev);
     Q_CUDA(cudaGetLastError());
     F = q->frev;
