@@ -65,6 +65,24 @@ def dist_env():
     return ws, rank, local
 
 
+def chase_roofline(counters, chase_ms, ops_peak, pipe):
+    """Roofline figures of k_chase, the kernel with the largest share of the
+    batched step's ncu launch list. Algorithmic work: 16 operations per
+    rotation of the shifted-QL recurrence (src/eigenSelfAdjoint.jl:389-405:
+    the Givens rotation's hypot, square root and two divisions, e, gamma, d
+    and the next pi), times the rotations the chase applied (the plan's
+    counter); achieved = that over the summed chase time of all size buckets;
+    peak = the pipe's measured FMA rate. One lane runs one matrix's serial
+    recurrence, so the kernel is latency-bound and frac is small by
+    construction: the buckets' streams overlap it with the other phases."""
+    ops = 16.0 * counters["rotations"]
+    achieved = ops / (chase_ms * 1e-3) / 1e12 if chase_ms > 0 else 0.0
+    return {"kernel": "k_chase", "bound": "latency", "achieved": achieved, "peak": ops_peak,
+            "unit": f"T {pipe} ops/s", "frac": (achieved / ops_peak) if ops_peak else None, "traffic": None,
+            "note": "serial recurrence, one lane per matrix; leads the launch list "
+                    "(profiles/launches_batched_4096_goe.md); k_refine, the throughput kernel, is roofline_refine"}
+
+
 def replica_seed(rank):
     """Each rank solves its own seeded batch (replicas: no data exchange)."""
     return SEED + 1000 * rank
@@ -343,9 +361,10 @@ def run_ours(args):
         ph = H["phase_ms_per_step"]
         c = H["counters"]
         ns3 = float((ns.astype(np.float64) ** 3).sum())
-        # Roofline of the top kernel of the batched step (k_refine: it leads the
-        # ncu launch list of this workload). Its double-float arithmetic runs on
-        # the FP32 pipe: achieved = FP32 operations per second, counted as
+        # Rooflines of the batched step's two largest kernels in its ncu launch
+        # list: k_chase (the larger share; latency-bound) and k_refine. The
+        # refinement's double-float arithmetic runs on the FP32 pipe: achieved
+        # = FP32 operations per second, counted as
         # 13 instructions per double-float multiply-add (TwoProduct 2, TwoSum 6,
         # 2 adds, QuickTwoSum 3) and ~3 n^3 multiply-adds per iteration (A X,
         # X'(AX), X'X as symmetric halves, X E); peak = the FP32 FMA rate of
@@ -374,7 +393,9 @@ def run_ours(args):
                        "path": hp, "batch": len(ns), "sum_n": int(ns.sum()), "sum_n3": ns3,
                        "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}",
                        "timing": "CUDA-graph replay of the whole batched solve (plan with GLA_FLAG_GRAPH)"},
-            "roofline": {"kernel": "k_refine", "bound": "fp32",
+            "roofline": chase_roofline(c, ph.get("chase", 0.0), peak_ops if hp == "f32_refined" else
+                                       (peak / 2.0 if peak else None), "FP32" if hp == "f32_refined" else "FP64"),
+            "roofline_refine": {"kernel": "k_refine", "bound": "fp32",
                          "achieved": achieved, "peak": peak_ops, "unit": "T FP32 ops/s",
                          "frac": (achieved / peak_ops) if peak_ops else None,
                          # DRAM bytes of one step's k_refine launches (all buckets), from an ncu

@@ -111,3 +111,14 @@ def test_lapack_side_baseline_child():
     assert r.returncode == 0, r.stderr[-2000:]
     out = json.loads(r.stdout.strip().splitlines()[-1])
     assert out["kind"] == "lapack" and out["value"] > 0 and out["cores"] >= 1
+
+
+def test_chase_roofline_figures():
+    # the launch list's top kernel of the batched step is reported with its
+    # algorithmic work (16 operations per applied rotation) over its time
+    import bench
+    r = bench.chase_roofline({"rotations": 1_000_000}, 2.0, 35.0, "FP32")
+    assert r["kernel"] == "k_chase" and r["bound"] == "latency" and r["unit"] == "T FP32 ops/s"
+    assert abs(r["achieved"] - 16e6 / 2e-3 / 1e12) < 1e-15
+    assert abs(r["frac"] - r["achieved"] / 35.0) < 1e-18 and r["traffic"] is None
+    assert bench.chase_roofline({"rotations": 5}, 0.0, None, "FP64")["frac"] is None
