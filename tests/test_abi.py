@@ -45,6 +45,32 @@ def test_host_only_calls(lib):
     assert b"argument 3" in lib.gla_status_string(-3)
 
 
+def test_header_is_plain_c_and_links(lib, tmp_path):
+    # the boundary is a C ABI: the header compiles as strict C99 and a C
+    # program that takes the address of every declared entry point links
+    # against the library and runs its host-only calls
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    syms = header_symbols()
+    src = tmp_path / "abi.c"
+    src.write_text('#include "glagpu.h"\n#include <stdio.h>\n'
+                   "typedef void (*fn)(void);\n"
+                   "static const fn table[] = {" + ", ".join(f"(fn){s}" for s in syms) + "};\n"
+                   "int main(void) {\n"
+                   "  printf(\"%d %d\\n\", gla_version(), (int)(sizeof(table) / sizeof(table[0])));\n"
+                   "  return 0;\n}\n")
+    exe = tmp_path / "abi"
+    libdir = os.path.dirname(lib._name)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-L", libdir, "-lglagpu", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.split() == ["100", str(len(syms))]
+
+
 def test_autotune_table_file_roundtrip(lib, tmp_path):
     # host-only: the table's text format, validation of loaded lines, save
     lib.gla_autotune_load.argtypes = [ctypes.c_char_p]
