@@ -122,3 +122,12 @@ def test_chase_roofline_figures():
     assert abs(r["achieved"] - 16e6 / 2e-3 / 1e12) < 1e-15
     assert abs(r["frac"] - r["achieved"] / 35.0) < 1e-18 and r["traffic"] is None
     assert bench.chase_roofline({"rotations": 5}, 0.0, None, "FP64")["frac"] is None
+
+
+def test_launch_counts():
+    # per size bucket: tridiagonalisation, (chase, replay) per pass, the
+    # refinement, and in a graph plan the unfinished-matrix mark
+    import bench
+    assert bench.launches_per_step(8, 2, True, False) == 8 * 6
+    assert bench.launches_per_step(8, bench.GRAPH_PASSES, True, True) == 8 * 11
+    assert bench.launches_per_step(8, bench.GRAPH_PASSES, False, True) == 8 * 10
