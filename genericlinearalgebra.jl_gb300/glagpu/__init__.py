@@ -511,14 +511,17 @@ class EigenQ:
         self.n = factors.shape[0]
 
     def _apply(self, side, trans, B):
+        # the operand's shape is checked before any device work (lmul!/rmul!
+        # raise DimensionMismatch, src/eigenSelfAdjoint.jl:25-27, :64-66)
+        shape = tuple(B.shape) if hasattr(B, "shape") else np.shape(B)
+        if len(shape) != 2:
+            raise DimensionMismatch("B must be a matrix")
+        m, k = shape
+        if (side == "L" and m != self.n) or (side == "R" and k != self.n):
+            raise DimensionMismatch(f"Q has order {self.n}, B is {m} x {k}")
         torch = _torch()
         on_dev = _is_torch(B)
         X = (B.to(torch.float64) if on_dev else torch.as_tensor(np.asarray(B, dtype=np.float64), device="cuda"))
-        if X.dim() != 2:
-            raise DimensionMismatch("B must be a matrix")
-        m, k = X.shape
-        if (side == "L" and m != self.n) or (side == "R" and k != self.n):
-            raise DimensionMismatch(f"Q has order {self.n}, B is {m} x {k}")
         Xc = X.t().contiguous().clone()  # column-major storage of X
         F = self.factors.t().contiguous()
         _lib.check(_lib.load().gla_dormtr(side.encode(), self.uplo.encode(), trans.encode(), m, k,

@@ -44,3 +44,14 @@ def test_precision_limits_of_non_real_input(G):
         G.eigen(np.eye(2, dtype=complex), precision="f32")
     with pytest.raises(ValueError):
         G.eigvals(G.QuaternionMatrix(np.zeros((2, 2, 4))), tol=1e-3)
+
+
+def test_eigenq_operand_shapes(G):
+    # lmul! needs size(Q, 1) rows, rmul! size(Q, 1) columns; checked before any device work
+    q = G.EigenQ(np.eye(4), np.zeros(3))
+    with pytest.raises(G.DimensionMismatch):
+        q.lmul(np.zeros((3, 2)))
+    with pytest.raises(G.DimensionMismatch):
+        q.rmul(np.zeros((2, 3)))
+    with pytest.raises(G.DimensionMismatch):
+        q.lmul(np.zeros(4))
