@@ -9,6 +9,11 @@ and the functions here that mirror it:
   eigen!(SymTridiagonal)        :623       -> eigen(SymTridiagonal(dv, ev))
   eigvals!(SymTridiagonal)      :581       -> eigvals(SymTridiagonal(dv, ev))
   eigQR!                        :290-340   -> alg="QR"
+  eigen2                        :633-668   -> eigen2(A)
+  symtri! / EigenQ              :6-118, :446-564 -> symtri(A, uplo) / EigenQ.lmul, rmul, array
+  eigen!(Hermitian{<:Complex})  :462       -> eigen(A) with complex A
+  eigen!(Hermitian{Quaternion}) (test/eigenselfadjoint.jl:54-84) -> eigen(QuaternionMatrix(A))
+  numnegevals                   src/tridiag.jl:20-36 -> numnegevals(T, sigma)
   keyword tol = eps(T)          :566-630   -> tol=None (eps of the precision)
   sortby = eigsortby (ascending)           -> always ascending (the default)
   LinearAlgebra.Eigen                      -> Eigen(values, vectors)
