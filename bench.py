@@ -9,7 +9,7 @@ larger than the 129 MB L2, so every step streams it from HBM.
 
 Paths timed: plain FP64 (the reference's arithmetic), plain FP32, and FP32 +
 FP64 Ogita-Aishima refinement (the headline `value`, eigh/s, when it meets
-residual and eigenvalue error <= 1e-13 ||A|| on the checked sample).
+residual and eigenvalue error <= 1e-13 ||A|| over every matrix of the batch).
 
 The single-matrix half of the metric ("large"): n = 4096, FP64 GPU path vs
 FP32 solve + refinement, on the prescribed-spectrum matrix Q diag(lam) Q'
@@ -91,8 +91,8 @@ def chase_roofline(counters, chase_ms, ops_peak, pipe):
     achieved = ops / (chase_ms * 1e-3) / 1e12 if chase_ms > 0 else 0.0
     return {"kernel": "k_chase", "bound": "latency", "achieved": achieved, "peak": ops_peak,
             "unit": f"T {pipe} ops/s", "frac": (achieved / ops_peak) if ops_peak else None, "traffic": None,
-            "note": "serial recurrence, one lane per matrix; leads the launch list "
-                    "(profiles/launches_batched_4096_goe.md); k_refine, the throughput kernel, is roofline_refine"}
+            "note": "serial recurrence, one lane per matrix; leads the batched step's ncu launch list; "
+                    "k_refine, the throughput kernel, is roofline_refine"}
 
 
 def replica_seed(rank):
@@ -203,22 +203,40 @@ def measured_peaks_file():
         return {}
 
 
-def check_sample(ns, mats, w, V, woff, aoff, idx, dtype):
-    """Max residual ||AV - VW||/||A||, orthogonality and eigenvalue error vs the
-    CPU oracle over the sampled matrices."""
+def oracle_values(ns, mats):
+    """Eigenvalues of every workload matrix from the CPU oracle (the
+    reference's eigvals! restated, FP64), all host threads; packed like w."""
     from oracle import oracle as O
+    aoff = np.concatenate([[0], np.cumsum(ns * ns)[:-1]]).astype(np.int64)
+    woff = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    A = pack_f(mats)
+    w = np.zeros(int(ns.sum()))
+    V = np.zeros(1)
+    info = np.zeros(len(ns), np.int32)
+    O.batched_raw("N", "L", np.ascontiguousarray(ns), aoff, A, w, woff, V, info, nthreads=os.cpu_count() or 1)
+    return w
+
+
+def check_all(ns, mats, w, V, woff, aoff, w_oracle):
+    """Max residual ||AV - VW||/||A||, orthogonality ||V'V - I|| and eigenvalue
+    error |w - w_oracle|/||A|| over EVERY matrix of the batch (2-norms,
+    matrices of one order stacked)."""
     res = orth = ev = 0.0
-    for b in idx:
-        n = int(ns[b])
-        A = mats[b]
-        wb = w[woff[b]: woff[b] + n].astype(np.float64)
-        Vb = V[aoff[b]: aoff[b] + n * n].reshape(n, n, order="F").astype(np.float64)
-        nA = np.linalg.norm(A, 2)
-        res = max(res, np.linalg.norm(A @ Vb - Vb * wb, 2) / nA)
-        orth = max(orth, np.linalg.norm(Vb.T @ Vb - np.eye(n), 2))
-        wo = O.syev(A, "N" if dtype == np.float64 else "N")[0]
-        ev = max(ev, np.abs(wb - wo).max() / nA)
-    return {"max_residual": res, "max_orthogonality": orth, "max_eig_err_vs_oracle": ev}
+    for n in np.unique(ns):
+        idx = np.nonzero(ns == n)[0]
+        n = int(n)
+        A = np.stack([mats[b] for b in idx])
+        Wb = np.stack([w[woff[b]: woff[b] + n] for b in idx]).astype(np.float64)
+        Vb = np.stack([V[aoff[b]: aoff[b] + n * n].reshape(n, n, order="F") for b in idx]).astype(np.float64)
+        Wo = np.stack([w_oracle[woff[b]: woff[b] + n] for b in idx])
+        nA = np.linalg.norm(A, 2, axis=(1, 2))
+        R = A @ Vb - Vb * Wb[:, None, :]
+        res = max(res, float((np.linalg.norm(R, 2, axis=(1, 2)) / nA).max()))
+        G = np.swapaxes(Vb, 1, 2) @ Vb - np.eye(n)
+        orth = max(orth, float(np.linalg.norm(G, 2, axis=(1, 2)).max()))
+        ev = max(ev, float((np.abs(Wb - Wo).max(axis=1) / nA).max()))
+    return {"max_residual": res, "max_orthogonality": orth, "max_eig_err_vs_oracle": ev,
+            "matrices_checked": int(len(ns))}
 
 
 def run_ours(args):
@@ -245,8 +263,7 @@ def run_ours(args):
     nW = int(ns.sum())
     dA64 = torch.from_numpy(A64).to(dev)
     dA32 = torch.from_numpy(A32).to(dev)
-    sample = np.random.Generator(np.random.PCG64(99)).choice(len(ns), size=48, replace=False)
-    sample = np.unique(np.concatenate([sample, np.argsort(-ns)[:8]]))
+    w_oracle = oracle_values(ns, mats)  # accuracy of every result is checked against these
 
     def barrier():
         if ws > 1:
@@ -288,7 +305,7 @@ def run_ours(args):
         counters = plan.stats()
         wh = w.cpu().numpy()
         Vh = V.cpu().numpy()
-        acc = check_sample(ns, mats, wh, Vh, woff, aoff, sample, np.float64 if path != "f32" else np.float32)
+        acc = check_all(ns, mats, wh, Vh, woff, aoff, w_oracle)
         n_bad = int((info.cpu().numpy() != 0).sum())
         results[path] = {
             "eigh_per_s": ws * len(ns) * args.steps / el,
@@ -328,7 +345,7 @@ def run_ours(args):
         barrier()
         el = ev0.elapsed_time(ev1) * 1e-3
         el = max_over_ranks(torch, el, ws, dev)
-        acc = check_sample(ns, mats, w.cpu().numpy(), V.cpu().numpy(), woff, aoff, sample, np.float64)
+        acc = check_all(ns, mats, w.cpu().numpy(), V.cpu().numpy(), woff, aoff, w_oracle)
         graph_res[path] = {"eigh_per_s": ws * len(ns) * args.steps / el, "ms_per_step": 1e3 * el / args.steps,
                            "accuracy": acc, "info_nonzero": int((info.cpu().numpy() != 0).sum()),
                            "launches_per_step": launches_per_step(len(plan_buckets(ns)), GRAPH_PASSES,
@@ -358,6 +375,7 @@ def run_ours(args):
     plan.close()
     el_e2e = max_over_ranks(torch, el_e2e, ws, dev)
     peak = measured_dgemm_tflops(torch) if rank == 0 else None
+    cus = cusolver_batched(torch, ns, mats, dev) if rank == 0 else None
     large = run_large(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
     c4 = run_c4(torch, glagpu, dev) if (rank == 0 and not args.no_large) else None
     c1 = run_c1(torch, glagpu, dev) if rank == 0 else None
@@ -399,7 +417,7 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32 solve + f64 refinement" if hp == "f32_refined" else "f64",
+            "dtype": "f32 solve + double-float (f32 pair) refinement" if hp == "f32_refined" else "f64",
             "data": "synthetic (seeded GOE)",
             "config": {"workload": f"batched eigen!(Hermitian): {len(ns)} GOE matrices, n~U[{NLO},{NHI}], seed {SEED}",
                        "path": hp, "batch": len(ns), "sum_n": int(ns.sum()), "sum_n3": ns3,
@@ -413,11 +431,11 @@ def run_ours(args):
                          # DRAM bytes of one step's k_refine launches (all buckets), from an ncu
                          # capture of the 512-matrix case scaled by the matrix count
                          "traffic": 66.0e6 * len(ns) / 512,
-                         "traffic_note": "bytes per step, profiles/k_refine_traffic_batched_512.md; "
-                                         "algorithmic ~20 sum(n^2) bytes",
+                         "traffic_note": "bytes per step, from an ncu capture of the 512-matrix case "
+                                         "scaled by the matrix count; algorithmic ~20 sum(n^2) bytes",
                          "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, FMA rate (FP32 pipe); "
                                         "MEASURED_PEAKS.json has only HBM and bf16 peaks",
-                         "note": "double-float arithmetic on the FP32 pipe; see profiles/"},
+                         "note": "double-float arithmetic on the FP32 pipe"},
             "roofline_large": large_roofline(large, measured_peaks_file()),
             "fp64_dgemm_tflops_measured": peak,
             "cpu_baseline": cpu,
@@ -435,10 +453,58 @@ def run_ours(args):
             "autotune": {"enabled": not args.no_autotune, "bucket_configs": tuned},
             "c1_single_n64": c1,
             "c5_mixed_forward_adjoint": c5,
+            "cusolver_batched_f64": cus,
+            "julia_probe": julia_probe(),
         }
+        line["summary"] = summary(line)
         print(json.dumps(line), flush=True)
+        for t in summary_lines(line["summary"]):
+            print(t, flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def summary(line):
+    """The figures a reader needs first, collected at the end of the JSON line
+    (the batched headline, the single-matrix n = 2048 / 4096 results, C1, C4
+    and C5)."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+    out = {"c2_graph_eigh_per_s": {p: g(line, "graph", p, "eigh_per_s") for p in ("f32_refined", "f64")},
+           "c2_speedup": line.get("speedup_f32refined_vs_f64"),
+           "c2_refined_accuracy_all_matrices": g(line, "graph", "f32_refined", "accuracy"),
+           "c2_e2e_eigh_per_s": g(line, "e2e", "value"),
+           "c2_cpu_port_eigh_per_s": g(line, "cpu_baseline", "value")}
+    large = line.get("large") or {}
+    for key, r in large.items():
+        acc = g(r, "f32_refined", "accuracy") or {}
+        out[key] = {"f64_ms": g(r, "f64", "ms"), "refined_ms": g(r, "f32_refined", "ms"),
+                    "speedup": r.get("speedup_f32refined_vs_f64"), "cusolver_f64_ms": g(r, "cusolver_f64", "ms"),
+                    "refined_max_err": max([v for v in acc.values() if v is not None], default=None),
+                    "refined_meets_1e13": r.get("refined_meets_1e13")}
+    c1 = line.get("c1_single_n64") or {}
+    out["c1_n64"] = {"gpu_us": c1.get("gpu_us_per_solve"), "cpu_1core_us": c1.get("cpu_oracle_us_per_solve_1core")}
+    c4 = line.get("c4_forward_adjoint") or {}
+    if c4:
+        out["c4_graph_speedup"] = (g(c4, "f32_refined", "graph_matrices_per_s") or 0) / max(
+            g(c4, "f64", "graph_matrices_per_s") or 1e-30, 1e-30)
+    c5 = line.get("c5_mixed_forward_adjoint") or {}
+    if c5:
+        out["c5_speedup"] = c5.get("speedup_f32refined_vs_f64")
+    return out
+
+
+def summary_lines(sm):
+    """The summary as short plain-text lines printed after the JSON line."""
+    lines = ["# summary: " + json.dumps({k: v for k, v in sm.items() if not k.startswith("n")})]
+    for k, v in sm.items():
+        if k.startswith("n") and isinstance(v, dict):
+            lines.append(f"# {k}: " + json.dumps(v))
+    return lines
 
 
 def run_c4(torch, glagpu, dev, reps=3):
@@ -657,12 +723,13 @@ def large_case(kind, n):
     return goe(n, 4), None
 
 
-def run_large(torch, glagpu, dev, n=4096, reps=2):
-    """n x n solves (the large half of the headline metric): plain FP64 GPU
-    path vs FP32 solve + FP64 refinement, time per solve (CUDA events; each
-    execute synchronises), accuracy of every result."""
+def run_large(torch, glagpu, dev, reps=2):
+    """Single-matrix solves (the large half of the headline metric): the
+    precision workload at n = 2048 and n = 4096 and a GOE n = 4096, plain
+    FP64 GPU path vs FP32 solve + refinement, time per solve (CUDA events;
+    each execute synchronises), accuracy of every result."""
     out = {}
-    for kind in ("c3", "goe"):
+    for kind, n in (("c3", 2048), ("c3", 4096), ("goe", 4096)):
         A, lam = large_case(kind, n)
         nA = np.linalg.norm(A, 2) if lam is None else np.abs(lam).max()
         dA = torch.from_numpy(A.ravel(order="F").copy()).to(dev)
@@ -704,6 +771,7 @@ def run_large(torch, glagpu, dev, n=4096, reps=2):
             plan.close()
             del w, V
         res["speedup_f32refined_vs_f64"] = res["f64"]["ms"] / res["f32_refined"]["ms"]
+        res["cusolver_f64"] = cusolver_single(torch, dA.view(n, n), lam, nA)
         # the tensor-core Ozaki GEMM of the refinement, timed alone on this order
         if kind == "goe":
             res["ozaki_gemm"] = time_ozaki(torch, glagpu, dev, n)
@@ -712,6 +780,59 @@ def run_large(torch, glagpu, dev, n=4096, reps=2):
         res["refined_meets_1e13"] = bool(ok)
         out[f"n{n}_{kind}"] = res
     return out
+
+
+def cusolver_single(torch, A, lam, nA, reps=2):
+    """Side comparator for the FP64 denominator, reported only: torch.linalg.eigh
+    (NVIDIA cuSOLVER) on the same FP64 matrix, best of reps after a warm-up.
+    The product never calls it."""
+    try:
+        At = A.t().contiguous()
+        w, V = torch.linalg.eigh(At)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            w, V = torch.linalg.eigh(At)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out = {"ms": best, "what": "torch.linalg.eigh FP64 (cuSOLVER), side comparator only"}
+        if lam is not None:
+            out["eig_err_vs_exact"] = float((w.cpu().numpy() - lam).__abs__().max() / nA)
+        return out
+    except Exception as e:  # a side number: report, never fail the benchmark
+        return {"unavailable": f"{type(e).__name__}: {str(e)[:120]}"}
+
+
+def cusolver_batched(torch, ns, mats, dev, reps=3):
+    """Side comparator for the batched FP64 path, reported only: the workload
+    grouped by order and solved with torch.linalg.eigh on stacked FP64 tensors
+    (cuSOLVER's batched routines), inputs resident, CUDA events around all
+    groups. The product never calls it."""
+    try:
+        groups = []
+        for n in np.unique(ns):
+            idx = np.nonzero(ns == n)[0]
+            groups.append(torch.tensor(np.stack([mats[b] for b in idx]), dtype=torch.float64, device=dev))
+        for g in groups:
+            torch.linalg.eigh(g)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            for g in groups:
+                torch.linalg.eigh(g)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        return {"eigh_per_s": len(ns) / (ms * 1e-3), "ms_per_step": ms, "launch_groups": len(groups),
+                "what": "torch.linalg.eigh FP64 per order group (cuSOLVER), side comparator only"}
+    except Exception as e:
+        return {"unavailable": f"{type(e).__name__}: {str(e)[:120]}"}
 
 
 def time_ozaki(torch, glagpu, dev, n, reps=5):
@@ -863,14 +984,28 @@ def time_oracle(ns, mats, nth):
     return time.perf_counter() - t0
 
 
+def julia_probe():
+    """Whether this host has Julia (the reference itself could then be timed);
+    recorded in the JSON line."""
+    import shutil
+    exe = shutil.which("julia")
+    if not exe:
+        return {"julia": None, "note": "julia not on PATH: the reference arm is the CPU restatement"}
+    try:
+        r = subprocess.run([exe, "--version"], capture_output=True, text=True, timeout=60)
+        return {"julia": exe, "version": r.stdout.strip()}
+    except Exception as e:
+        return {"julia": exe, "version": None, "error": type(e).__name__}
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
     ns, mats = workload()
     nth = os.cpu_count() or 1
-    # each step: a bounded sample (the first 512 matrices) of the workload
-    m = 512
+    # each step: the whole 4096-matrix workload, one matrix per OpenMP thread
+    m = len(ns)
     for _ in range(args.warmup):
         time_oracle(ns[:m], mats[:m], nth)
     tot = 0.0
@@ -884,10 +1019,11 @@ def run_reference(args):
         "config": {"workload": f"batched eigen!(Hermitian): {len(ns)} GOE matrices, n~U[{NLO},{NHI}], seed {SEED}",
                    "path": "reference CPU", "batch": len(ns)},
         "cpu_baseline": {"value": val, "unit": "eigh/s", "cores": nth, "kind": "port",
-                         "sample": f"first {m} matrices of the workload per step; CPU restatement of "
-                                   "GenericLinearAlgebra.jl eigen!(Hermitian) (Julia not installed), "
-                                   f"{nth} OpenMP threads"},
+                         "sample": f"all {m} matrices of the workload per step; CPU restatement of "
+                                   "GenericLinearAlgebra.jl eigen!(Hermitian), "
+                                   f"{nth} OpenMP threads (one matrix per thread)"},
         "e2e": {"value": val, "unit": "eigh/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "julia_probe": julia_probe(),
     }
     print(json.dumps(line), flush=True)
 

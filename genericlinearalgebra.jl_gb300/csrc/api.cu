@@ -37,14 +37,15 @@ namespace gla {
 cudaError_t tridiag_kernels_init();
 cudaError_t chase_kernels_init();
 cudaError_t apply_kernels_init();
+void release_eigenq_cache();
+void release_complex_cache();
+void release_quaternion_cache();
 }  // namespace gla
 
 namespace {
 
 constexpr int kRotPerN2 = 2;    // rotation-log capacity per pass, in units of n^2
 constexpr int kHdrPerN = 3;     // header-log capacity per pass, in units of n
-constexpr int kMaxSweepsPerN = 30;  // chase cap per matrix (src/eigenGeneral.jl:52 uses 30n)
-constexpr int kMaxPasses = 64;
 constexpr int kAsyncPasses = 2;     // chase passes enqueued without a host check
 constexpr int kGraphPasses = 4;     // chase passes of a capture-safe (GLA_FLAG_GRAPH) execute
 constexpr int kMaxBuckets = 8;      // size buckets of width 16 over (0, 128]
@@ -217,7 +218,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->uplo = uplo;
   p->algo = (flags & 3) == GLA_ALG_QR ? kAlgoQR : kAlgoQL;
   p->batch = batch;
-  p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? 0x1p-52 : (double)0x1p-23f);
+  p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? kTolF64 : kTolF32);
   p->timing = (flags & GLA_FLAG_TIMING) != 0;
   p->graph = (flags & GLA_FLAG_GRAPH) != 0;
   p->n.assign(n, n + batch);
@@ -944,6 +945,33 @@ int gla_gemm_df_last_ms(float* slice_ms, float* gemm_ms) {
   GLA_CUDA(cudaEventSynchronize(g_gemm_ev[2]));
   GLA_CUDA(cudaEventElapsedTime(slice_ms, g_gemm_ev[0], g_gemm_ev[1]));
   GLA_CUDA(cudaEventElapsedTime(gemm_ms, g_gemm_ev[1], g_gemm_ev[2]));
+  return 0;
+}
+
+int gla_release_workspaces(void) {
+  // every cached buffer may still be in use by queued work on any stream
+  GLA_CUDA(cudaDeviceSynchronize());
+  {
+    std::lock_guard<std::mutex> lk(g_single_mu);
+    for (auto& kv : g_single) {
+      gla_plan_destroy(kv.second.plan);
+      cudaFree(kv.second.buf);
+      cudaFree(kv.second.dinfo);
+    }
+    g_single.clear();
+    for (auto& kv : g_stev_large) large_destroy(kv.second);
+    g_stev_large.clear();
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_gemm_mu);
+    if (g_gemm_w) oz_destroy(g_gemm_w);
+    g_gemm_w = nullptr;
+    g_gemm_timed = false;
+  }
+  release_eigenq_cache();
+  release_complex_cache();
+  release_quaternion_cache();
+  GLA_CUDA(cudaGetLastError());
   return 0;
 }
 

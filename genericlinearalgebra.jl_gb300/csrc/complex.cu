@@ -249,6 +249,18 @@ cudaError_t grow(P** p, size_t* cap, size_t need) {
 
 }  // namespace
 
+namespace gla {
+// Frees the buffers cached by gla_zheev (the caller has drained the device).
+void release_complex_cache() {
+  std::lock_guard<std::mutex> lk(g_z_mu);
+  cudaFree(g_z.E);
+  cudaFree(g_z.w2);
+  cudaFree(g_z.scratch);
+  cudaFree(g_z.idx);
+  g_z = ZWork();
+}
+}  // namespace gla
+
 extern "C" {
 
 int gla_zheev(char jobz, char uplo, int64_t n, const double* A, int64_t lda, double* w, double* V, int64_t ldv,

@@ -151,6 +151,22 @@ cudaError_t q_tmp(QCtx* q, size_t need, cudaStream_t st) {
   return e;
 }
 
+}  // namespace
+
+// Frees the per-order contexts cached by gla_dsytrd / gla_dormtr (the caller
+// has drained the device).
+void release_eigenq_cache() {
+  std::lock_guard<std::mutex> lk(g_q_mu);
+  for (auto& kv : g_q) {
+    large_destroy(kv.second.c);
+    cudaFree(kv.second.tmp);
+    cudaFree(kv.second.frev);
+  }
+  g_q.clear();
+}
+
+namespace {
+
 #define Q_CUDA(x)                                   \
   do {                                              \
     cudaError_t e_ = (x);                           \

@@ -11,6 +11,14 @@ namespace gla {
 
 enum TypeCode { kF64 = 0, kF32 = 1, kF32FromF64 = 2 };
 
+// Limits shared by every driver of the small-matrix kernels (plans, the
+// single-matrix entry points and the allocation-free one), so that they stop
+// on the same conditions.
+constexpr int kMaxSweepsPerN = 30;  // chase cap per matrix: 30 n sweeps (src/eigenGeneral.jl:52 uses 30n)
+constexpr int kMaxPasses = 64;      // chase passes before a full rotation log is given up on
+constexpr double kTolF64 = 0x1p-52;  // default deflation tolerance, eps(Float64)
+constexpr double kTolF32 = (double)0x1p-23f;  // eps(Float32)
+
 size_t tridiag_smem_bytes(int n, int nt, int elem);
 size_t chase_smem_bytes(int nmax, int elem);
 size_t apply_smem_bytes(int n, int elem);

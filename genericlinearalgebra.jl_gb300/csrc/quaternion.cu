@@ -314,6 +314,18 @@ int check_args(char jobz, char uplo, int64_t n, const double* A, int64_t lda, co
 
 }  // namespace
 
+namespace gla {
+// Frees the buffers cached by gla_qheev (the caller has drained the device).
+void release_quaternion_cache() {
+  std::lock_guard<std::mutex> lk(g_qh_mu);
+  cudaFree(g_qh.E);
+  cudaFree(g_qh.w4);
+  cudaFree(g_qh.scratch);
+  cudaFree(g_qh.idx);
+  g_qh = QWork();
+}
+}  // namespace gla
+
 extern "C" {
 
 int gla_qheev(char jobz, char uplo, int64_t n, const double* A, int64_t lda, double* w, double* V, int64_t ldv,

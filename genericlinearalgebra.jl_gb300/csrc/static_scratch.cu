@@ -145,10 +145,10 @@ extern "C" int gla_dsyev_static(char jobz, char uplo, int64_t n, double* A, int6
   GLA_CUDA(launch_tridiag(kF64, wantq, 1, nt, tridiag_smem_bytes(nn, nt, 8), st, desc, perm, Q, uplo == 'L', d, e, Q,
                           dinfo, cst, nullptr));
   if (wantq) {
-    for (int pass = 0; pass < 64; pass++) {
+    for (int pass = 0; pass < kMaxPasses; pass++) {
       GLA_CUDA(cudaMemsetAsync(pending, 0, sizeof(int), st));
       GLA_CUDA(launch_chase(kF64, kAlgoQL, 1, chase_smem_bytes(nn, 8), st, desc, perm, d, e, cst, rot, hdr, dinfo,
-                            0x1p-52, 30, pending, stats));
+                            kTolF64, kMaxSweepsPerN, pending, stats));
       GLA_CUDA(launch_apply(kF64, 1, nt, apply_smem_bytes(nn, 8), st, desc, perm, Q, d, w, cst, rot, hdr, dinfo,
                             nullptr));
       int more = 0;
@@ -160,7 +160,7 @@ extern "C" int gla_dsyev_static(char jobz, char uplo, int64_t n, double* A, int6
                                cudaMemcpyDeviceToDevice, st));
   } else {
     GLA_CUDA(launch_chase(kF64, kAlgoPWK, 1, chase_smem_bytes(nn, 8), st, desc, perm, d, e, cst, nullptr, nullptr,
-                          dinfo, 0x1p-52, 30, pending, stats));
+                          dinfo, kTolF64, kMaxSweepsPerN, pending, stats));
     GLA_CUDA(launch_sort_values(kF64, 1, st, desc, perm, d, w, dinfo, nullptr));
   }
   GLA_CUDA(cudaMemcpyAsync(info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -15,7 +15,8 @@ and the functions here that mirror it:
   eigen!(Hermitian{Quaternion}) (test/eigenselfadjoint.jl:54-84) -> eigen(QuaternionMatrix(A))
   numnegevals                   src/tridiag.jl:20-36 -> numnegevals(T, sigma)
   keyword tol = eps(T)          :566-630   -> tol=None (eps of the precision)
-  sortby = eigsortby (ascending)           -> always ascending (the default)
+  keyword sortby = eigsortby    :592-599   -> sortby=eigsortby (ascending), any key function,
+                                              or None (no particular order)
   LinearAlgebra.Eigen                      -> Eigen(values, vectors)
 
 Beside the reference's plain path, precision="f32_refined" runs the FP32
@@ -449,44 +450,83 @@ def _qheev(Q, jobz, uplo):
     return w if on_dev else w.cpu().numpy()
 
 
-def eigen(A, uplo="L", tol=None, precision="f64", alg="QL"):
-    """eigen(Hermitian(A, uplo)) / eigen(SymTridiagonal): ascending values and
-    the matching orthonormal eigenvectors (columns). Complex input is a
-    complex Hermitian matrix (FP64, gla_zheev); a QuaternionMatrix a
+def eigsortby(x):
+    """The default sort key of eigen!/eigvals! (LinearAlgebra.eigsortby for
+    real eigenvalues): the value itself, i.e. ascending order."""
+    return x
+
+
+def _sorted_by(vals, vecs, sortby):
+    """sorteig!(vals, vecs, sortby) (src/eigenSelfAdjoint.jl:598): a stable
+    permutation of the device's ascending output by the key sortby(value)
+    (ties keep their ascending order), applied to the values and to the
+    eigenvector columns. sortby None or eigsortby leaves the ascending order
+    (None asks for no particular order)."""
+    if sortby is None or sortby is eigsortby:
+        return vals, vecs
+    host = vals.cpu().numpy() if _is_torch(vals) else np.asarray(vals)
+    keys = [sortby(float(x)) for x in host]
+    perm = sorted(range(len(keys)), key=lambda i: keys[i])  # Python's sort is stable
+    if _is_torch(vals):
+        torch = _torch()
+        p = torch.tensor(perm, dtype=torch.long, device=vals.device)
+        return vals[p], (vecs[:, p] if vecs is not None else None)
+    p = np.asarray(perm, dtype=np.int64)
+    return vals[p], (vecs[:, p] if vecs is not None else None)
+
+
+def eigen(A, uplo="L", tol=None, precision="f64", alg="QL", sortby=eigsortby):
+    """eigen(Hermitian(A, uplo)) / eigen(SymTridiagonal): eigenvalues and the
+    matching orthonormal eigenvectors (columns), ascending unless sortby
+    names another key (as the reference's sortby keyword). Complex input is
+    a complex Hermitian matrix (FP64, gla_zheev); a QuaternionMatrix a
     quaternion Hermitian one (FP64, gla_qheev)."""
     if isinstance(A, SymTridiagonal):
-        return _tridiag(A, "V", alg, tol)
-    if isinstance(A, QuaternionMatrix):
+        r = _tridiag(A, "V", alg, tol)
+    elif isinstance(A, QuaternionMatrix):
         if precision != "f64" or tol is not None:
             raise ValueError("quaternion Hermitian input: FP64 with the default tolerance only")
-        return _qheev(A, "V", uplo)
-    if _is_complex(A):
+        r = _qheev(A, "V", uplo)
+    elif _is_complex(A):
         if precision != "f64" or tol is not None:
             raise ValueError("complex Hermitian input: FP64 with the default tolerance only")
-        return _zheev(A, "V", uplo)
-    return eigen_batched([A], uplo=uplo, tol=tol, precision=precision, alg=alg)[0]
+        r = _zheev(A, "V", uplo)
+    else:
+        r = eigen_batched([A], uplo=uplo, tol=tol, precision=precision, alg=alg)[0]
+    if sortby is None or sortby is eigsortby:
+        return r
+    return Eigen(*_sorted_by(r.values, r.vectors, sortby))
 
 
-def eigvals(A, uplo="L", tol=None, precision="f64", irange=None, vl=None, vu=None, abstol=0.0):
-    """eigvals(Hermitian(A, uplo)) / eigvals(SymTridiagonal): ascending values.
-    For SymTridiagonal input, irange = (il, iu) (1-based, inclusive, as
-    Julia's eigvals(T, il:iu)) or vl < lambda <= vu (eigvals(T, vl, vu))
-    select a subset, computed by Sturm-count multisection (gla_dstebz)."""
+def eigvals(A, uplo="L", tol=None, precision="f64", irange=None, vl=None, vu=None, abstol=0.0, sortby=eigsortby):
+    """eigvals(Hermitian(A, uplo)) / eigvals(SymTridiagonal): the eigenvalues,
+    ascending unless sortby names another key. For SymTridiagonal input,
+    irange = (il, iu) (1-based, inclusive, as Julia's eigvals(T, il:iu)) or
+    vl < lambda <= vu (eigvals(T, vl, vu)) select a subset, computed by
+    Sturm-count multisection (gla_dstebz)."""
     if isinstance(A, SymTridiagonal):
         if irange is not None or vl is not None or vu is not None:
             return _tridiag_subset(A, irange, vl, vu, abstol)
-        return _tridiag(A, "N", "QL", tol)
-    if irange is not None or vl is not None or vu is not None:
+        w = _tridiag(A, "N", "QL", tol)
+    elif irange is not None or vl is not None or vu is not None:
         raise ValueError("eigenvalue subsets are available for SymTridiagonal input")
-    if isinstance(A, QuaternionMatrix):
+    elif isinstance(A, QuaternionMatrix):
         if precision != "f64" or tol is not None:
             raise ValueError("quaternion Hermitian input: FP64 with the default tolerance only")
-        return _qheev(A, "N", uplo)
-    if _is_complex(A):
+        w = _qheev(A, "N", uplo)
+    elif _is_complex(A):
         if precision != "f64" or tol is not None:
             raise ValueError("complex Hermitian input: FP64 with the default tolerance only")
-        return _zheev(A, "N", uplo)
-    return eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
+        w = _zheev(A, "N", uplo)
+    else:
+        w = eigvals_batched([A], uplo=uplo, tol=tol, precision=precision)[0]
+    return _sorted_by(w, None, sortby)[0]
+
+
+def release_workspaces():
+    """Free the device workspaces the single-call entry points cache per order
+    (gla_release_workspaces); waits for the device first."""
+    _lib.check(_lib.load().gla_release_workspaces(), "gla_release_workspaces")
 
 
 def _tridiag_dev(T):
@@ -644,6 +684,7 @@ def autotune_load(path):
 
 
 __all__ = ["Eigen", "Plan", "SymTridiagonal", "eigen", "eigen2", "eigvals", "eigen_batched", "eigvals_batched", "eigh_autograd",
-           "autotune_clear", "autotune_save", "autotune_load", "numnegevals", "symtri", "EigenQ",
+           "autotune_clear", "autotune_save", "autotune_load", "numnegevals", "symtri", "EigenQ", "eigsortby",
+           "release_workspaces",
            "SymmetricTridiagonalFactorization", "QuaternionMatrix",
            "DimensionMismatch", "NonConvergenceError", "NonFiniteError", "GLAError", "GLA_MAX_SMALL_N", "GLA_MAX_N"]

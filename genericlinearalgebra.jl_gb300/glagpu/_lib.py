@@ -70,6 +70,7 @@ SIGNATURES = {
     "gla_ssyev": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
     "gla_dstev": ([_ch, _i64, _vp, _vp, _vp, _i64, _int, C.POINTER(_int), _vp], _int),
     "gla_dsyev_static": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
+    "gla_release_workspaces": ([], _int),
 }
 
 _lib = None

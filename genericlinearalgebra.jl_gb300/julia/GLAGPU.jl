@@ -6,9 +6,18 @@
 #   eigen!(::Hermitian/Symmetric{<:Real})  (:626-630)  -> GLAGPU.eigen!
 #   eigvals!(::Hermitian/Symmetric{<:Real}) (:584-588) -> GLAGPU.eigvals!
 #   eigen!(::SymTridiagonal) / eigvals!     (:581,:623) -> GLAGPU.eigen! / eigvals!
-#   keyword tol = eps(T), sortby = eigsortby (ascending only), alg ignored
+#   keyword tol = eps(T), sortby = eigsortby (any key: a stable permutation
+#   as sorteig! :598 applies), alg ignored
 # and returns LinearAlgebra.Eigen like the reference. A nonzero per-matrix
 # info raises, as src/lapack.jl:62 turns LAPACK's info into LAPACKException.
+#
+# The drop-in: a matrix held in GPU memory (GPUMatrix) wrapped in Hermitian or
+# Symmetric. For those wrappers this module adds methods to LinearAlgebra's
+# own eigen!, eigvals!, eigen and eigvals, so unqualified calls
+#     E = eigen!(Hermitian(dA))      # dA::GPUMatrix{Float64}
+# reach the GPU: stdlib's LAPACK method only takes StridedMatrix storage, and
+# GenericLinearAlgebra's generic eigen!(::Hermitian) is less specific than a
+# method on Hermitian{T,GPUMatrix{T}}, so these win dispatch without piracy.
 #
 # Host Matrix inputs go through gla_plan_execute_host (the library copies to
 # and from the GPU); batched calls solve many matrices per launch sequence.
@@ -114,21 +123,157 @@ eigvals_batched(mats; uplo = 'L', kw...) = _batched(mats, 'N', uplo; kw...)[1]
 
 uplochar(A) = A.uplo == 'L' ? 'L' : 'U'
 
+# sorteig!(values, vectors, sortby) (:598): the device returns ascending
+# values; any other key is applied as a stable permutation of that order
+# (sortby === nothing leaves it).
+function _sortby!(w::AbstractVector, V, sortby)
+    (sortby === nothing || sortby === LinearAlgebra.eigsortby) && return w, V
+    p = sortperm(w; by = sortby)  # stable: ties keep their ascending order
+    return w[p], V === nothing ? nothing : V[:, p]
+end
+
 # eigen!/eigvals! on Hermitian/Symmetric real matrices (the reference's :614-630 and :572-588).
 function eigen!(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; tol = eps(T), sortby = LinearAlgebra.eigsortby,
                 alg = nothing) where {T<:Union{Float32,Float64}}
-    sortby === LinearAlgebra.eigsortby || throw(ArgumentError("only the ascending eigsortby order is supported"))
     prec = T === Float32 ? GLA_PREC_F32 : GLA_PREC_F64
     E = eigen_batched([A.data]; uplo = uplochar(A), precision = prec, tol = Float64(tol))[1]
     copyto!(A.data, E.vectors)  # like eigen!, the input storage is consumed
-    return E
+    return LinearAlgebra.Eigen(_sortby!(E.values, E.vectors, sortby)...)
 end
 
 function eigvals!(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; tol = eps(T),
                   sortby = LinearAlgebra.eigsortby, alg = nothing) where {T<:Union{Float32,Float64}}
     prec = T === Float32 ? GLA_PREC_F32 : GLA_PREC_F64
-    return eigvals_batched([A.data]; uplo = uplochar(A), precision = prec, tol = Float64(tol))[1]
+    w = eigvals_batched([A.data]; uplo = uplochar(A), precision = prec, tol = Float64(tol))[1]
+    return _sortby!(w, nothing, sortby)[1]
 end
+
+# ---------------------------------------------------------------- GPU-resident matrices
+#
+# GPUMatrix{T}: an n x n column-major matrix in device memory, allocated and
+# copied with the CUDA runtime (libcudart; GLAGPU_CUDART overrides the path).
+# It is an AbstractMatrix (size, element access by one-element copies), so
+# Hermitian(dA) and Symmetric(dA) are ordinary LinearAlgebra wrappers; the
+# eigen!/eigvals!/eigen/eigvals methods below are LinearAlgebra's functions
+# extended for them, and call gla_dsyev / gla_ssyev on the device pointer.
+const libcudart = get(ENV, "GLAGPU_CUDART", "libcudart.so")
+
+cudacheck(e) = e == 0 ? nothing : throw(GLAException(Cint(-1000 - e), statusmsg(Cint(-1000 - e))))
+
+mutable struct GPUMatrix{T<:Union{Float32,Float64}} <: AbstractMatrix{T}
+    ptr::Ptr{T}
+    n::Int
+    function GPUMatrix{T}(::UndefInitializer, n::Integer) where {T}
+        p = Ref{Ptr{Cvoid}}(C_NULL)
+        cudacheck(ccall((:cudaMalloc, libcudart), Cint, (Ref{Ptr{Cvoid}}, Csize_t), p, max(n * n, 1) * sizeof(T)))
+        M = new{T}(Ptr{T}(p[]), Int(n))
+        finalizer(M) do m
+            m.ptr == C_NULL || ccall((:cudaFree, libcudart), Cint, (Ptr{Cvoid},), m.ptr)
+            m.ptr = C_NULL
+        end
+        return M
+    end
+end
+
+const cudaMemcpyHostToDevice = Cint(1)
+const cudaMemcpyDeviceToHost = Cint(2)
+const cudaMemcpyDeviceToDevice = Cint(3)
+_memcpy(dst, src, bytes, kind) =
+    cudacheck(ccall((:cudaMemcpy, libcudart), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Csize_t, Cint), dst, src, bytes, kind))
+
+function GPUMatrix(A::AbstractMatrix{T}) where {T<:Union{Float32,Float64}}
+    n = LinearAlgebra.checksquare(A)
+    M = GPUMatrix{T}(undef, n)
+    h = Matrix{T}(A)
+    _memcpy(M.ptr, h, n * n * sizeof(T), cudaMemcpyHostToDevice)
+    return M
+end
+Base.size(M::GPUMatrix) = (M.n, M.n)
+Base.IndexStyle(::Type{<:GPUMatrix}) = IndexCartesian()
+function Base.getindex(M::GPUMatrix{T}, i::Int, j::Int) where {T}
+    checkbounds(M, i, j)
+    r = Ref{T}()
+    _memcpy(r, M.ptr + ((j - 1) * M.n + (i - 1)) * sizeof(T), sizeof(T), cudaMemcpyDeviceToHost)
+    return r[]
+end
+function Base.setindex!(M::GPUMatrix{T}, v, i::Int, j::Int) where {T}
+    checkbounds(M, i, j)
+    r = Ref{T}(convert(T, v))
+    _memcpy(M.ptr + ((j - 1) * M.n + (i - 1)) * sizeof(T), r, sizeof(T), cudaMemcpyHostToDevice)
+    return v
+end
+function Base.Array(M::GPUMatrix{T}) where {T}
+    h = Matrix{T}(undef, M.n, M.n)
+    M.n == 0 || _memcpy(h, M.ptr, M.n * M.n * sizeof(T), cudaMemcpyDeviceToHost)
+    return h
+end
+Base.Matrix(M::GPUMatrix) = Array(M)
+function Base.copy(M::GPUMatrix{T}) where {T}
+    C = GPUMatrix{T}(undef, M.n)
+    M.n == 0 || _memcpy(C.ptr, M.ptr, M.n * M.n * sizeof(T), cudaMemcpyDeviceToDevice)
+    return C
+end
+
+const HermSymGPU{T} = Union{Hermitian{T,GPUMatrix{T}},Symmetric{T,GPUMatrix{T}}}
+
+# In place on the device: the storage of A becomes the eigenvectors (as
+# LAPACK's dsyev and the reference's eigen! consume their input).
+function _syev_gpu!(jobz::Char, A::HermSymGPU{T}, tol) where {T}
+    D = A.data
+    n = D.n
+    tol == eps(T) || tol == 0 || throw(ArgumentError("GPUMatrix input: the default tolerance eps($T) only"))
+    wbuf = Ref{Ptr{Cvoid}}(C_NULL)
+    cudacheck(ccall((:cudaMalloc, libcudart), Cint, (Ref{Ptr{Cvoid}}, Csize_t), wbuf, max(n, 1) * sizeof(T)))
+    info = Ref{Cint}(0)
+    try
+        rc = T === Float64 ?
+            ccall((:gla_dsyev, libglagpu), Cint, (UInt8, UInt8, Int64, Ptr{T}, Int64, Ptr{Cvoid}, Ref{Cint}, Ptr{Cvoid}),
+                  UInt8(jobz), UInt8(uplochar(A)), n, D.ptr, max(n, 1), wbuf[], info, C_NULL) :
+            ccall((:gla_ssyev, libglagpu), Cint, (UInt8, UInt8, Int64, Ptr{T}, Int64, Ptr{Cvoid}, Ref{Cint}, Ptr{Cvoid}),
+                  UInt8(jobz), UInt8(uplochar(A)), n, D.ptr, max(n, 1), wbuf[], info, C_NULL)
+        check(rc)
+        raise_info(Cint[info[]])
+        vals = Vector{T}(undef, n)
+        n == 0 || _memcpy(vals, wbuf[], n * sizeof(T), cudaMemcpyDeviceToHost)
+        return vals
+    finally
+        ccall((:cudaFree, libcudart), Cint, (Ptr{Cvoid},), wbuf[])
+    end
+end
+
+# Column permutation of a device matrix (n device-to-device column copies).
+function _permutecols(V::GPUMatrix{T}, p) where {T}
+    P = GPUMatrix{T}(undef, V.n)
+    col = V.n * sizeof(T)
+    for (k, j) in enumerate(p)
+        _memcpy(P.ptr + (k - 1) * col, V.ptr + (j - 1) * col, col, cudaMemcpyDeviceToDevice)
+    end
+    return P
+end
+
+function LinearAlgebra.eigen!(A::HermSymGPU{T}; tol = eps(T), sortby = LinearAlgebra.eigsortby,
+                              alg = nothing) where {T<:Union{Float32,Float64}}
+    w = _syev_gpu!('V', A, tol)
+    V = A.data
+    if !(sortby === nothing || sortby === LinearAlgebra.eigsortby)
+        p = sortperm(w; by = sortby)
+        w = w[p]
+        V = _permutecols(V, p)
+    end
+    return LinearAlgebra.Eigen(w, V)  # eigenvectors stay on the device
+end
+function LinearAlgebra.eigvals!(A::HermSymGPU{T}; tol = eps(T), sortby = LinearAlgebra.eigsortby,
+                                alg = nothing) where {T<:Union{Float32,Float64}}
+    return _sortby!(_syev_gpu!('N', A, tol), nothing, sortby)[1]
+end
+LinearAlgebra.eigen(A::Hermitian{T,GPUMatrix{T}}; kw...) where {T<:Union{Float32,Float64}} =
+    LinearAlgebra.eigen!(Hermitian(copy(A.data), Symbol(A.uplo)); kw...)
+LinearAlgebra.eigen(A::Symmetric{T,GPUMatrix{T}}; kw...) where {T<:Union{Float32,Float64}} =
+    LinearAlgebra.eigen!(Symmetric(copy(A.data), Symbol(A.uplo)); kw...)
+LinearAlgebra.eigvals(A::Hermitian{T,GPUMatrix{T}}; kw...) where {T<:Union{Float32,Float64}} =
+    LinearAlgebra.eigvals!(Hermitian(copy(A.data), Symbol(A.uplo)); kw...)
+LinearAlgebra.eigvals(A::Symmetric{T,GPUMatrix{T}}; kw...) where {T<:Union{Float32,Float64}} =
+    LinearAlgebra.eigvals!(Symmetric(copy(A.data), Symbol(A.uplo)); kw...)
 
 # FP32 solve + FP64 Ogita-Aishima refinement (no reference counterpart).
 eigen_refined(A::Union{Hermitian{Float64},Symmetric{Float64}}) =
@@ -280,5 +425,7 @@ function eigvals(T::SymTridiagonal{Float64}, vl::Real, vu::Real; abstol = 0.0)
     iu = numnegevals(T, vu)
     return iu < il ? Float64[] : eigvals(T, il:iu; abstol)
 end
+
+export GPUMatrix
 
 end # module

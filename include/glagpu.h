@@ -194,6 +194,19 @@ int gla_dsyev(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w
 int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, int* info, void* stream);
 
 /*
+ * Frees the device workspaces that the single-call entry points keep for the
+ * life of the process, one per distinct order or size: gla_dsyev, gla_ssyev,
+ * gla_dstev, gla_gemm_df, gla_zheev, gla_qheev, gla_dsytrd and gla_dormtr.
+ * Plans are the caller's and are not touched. Waits for the whole device
+ * first (cudaDeviceSynchronize), since queued work may still use the
+ * buffers; the next call of an entry point allocates its workspace again.
+ * Call it when no other host thread is inside one of those entry points.
+ * No counterpart in the reference (Julia's garbage collector owns its
+ * workspaces).
+ */
+int gla_release_workspaces(void);
+
+/*
  * gla_dsyev without any device allocation: same arguments, results and
  * synchronisation as gla_dsyev, for callers that cannot call cudaMalloc when
  * they need the decomposition (e.g. an application whose memory pool already
@@ -206,8 +219,10 @@ int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, 
  * about 660 KB that every GPU loading the library holds until exit. The
  * first call on a device looks up that array's device address (and sets the
  * kernels' shared-memory limits), so make it before any stream capture.
- * All calls share the array: calls whose GPU work overlaps (other streams,
- * other host threads on the same device) race and must be serialised.
+ * Like gla_dsyev, every call reads info back to the host and waits for its
+ * stream before returning. All calls share the array: calls whose GPU work
+ * overlaps (other streams, other host threads on the same device) race and
+ * must be serialised.
  */
 int gla_dsyev_static(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w, int* info, void* stream);
 

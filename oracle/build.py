@@ -4,6 +4,11 @@ The reference (GenericLinearAlgebra.jl) is pure Julia with no compiled
 sources, so there is no `oracle/_ref` build; the oracle is the C++
 restatement in gla_ref.hpp. Compiled with -ffp-contract=off so that x86_64
 and aarch64 hosts produce the same bits (no FMA contraction, as in Julia).
+No -march=native: the same source must build and give the same results on
+the x86_64 build host and the aarch64 (Grace) GPU host, so the flags name no
+host-specific instruction set; with contraction off and no -ffast-math the
+compiler may not reassociate the reductions anyway, so a native target would
+change speed only through wider loads.
 """
 import os
 import platform

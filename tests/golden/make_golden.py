@@ -10,6 +10,7 @@ Sources:
     mpmath restatement of the reference algorithm (oracle/gla_ref_mp.py), the
     stand-in for running the reference on BigFloat.
 """
+import argparse
 import json
 import os
 import re
@@ -22,8 +23,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from oracle import gla_ref_mp as MP  # noqa: E402
 
-REF_TEST = "/root/reference/test/eigenselfadjoint.jl"
+REF_TEST_REL = os.path.join("test", "eigenselfadjoint.jl")
 DIGITS = 75
+LARGE_CASES = [(64, 1), (128, 7)]
 
 
 def s(x):
@@ -56,8 +58,33 @@ def goe(n, seed):
     return (B + B.T) / 2
 
 
+def main_large():
+    out = {"source": "256-bit restatement of GenericLinearAlgebra.jl v0.4.0 eigen!(Hermitian) "
+                     "(oracle/gla_ref_mp.py) on seeded GOE matrices",
+           "precision_bits": MP.PREC, "goe": []}
+    for n, seed in LARGE_CASES:
+        A = goe(n, seed)
+        w, V = MP.syev(A.tolist(), "V")
+        out["goe"].append({"n": n, "seed": seed, "A": [[float(v).hex() for v in row] for row in A],
+                           "w": [s(x) for x in w], "V": [[float(x) for x in row] for row in V]})
+        print("goe", n, "done", flush=True)
+    with open(os.path.join(HERE, "golden_large.json"), "w") as f:
+        json.dump(out, f)
+    print("wrote", os.path.join(HERE, "golden_large.json"))
+
+
 def main():
-    text = open(REF_TEST).read()
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("GLA_REFERENCE", ""),
+                    help="GenericLinearAlgebra.jl checkout (read as text only)")
+    ap.add_argument("--large", action="store_true", help="write golden_large.json instead")
+    args = ap.parse_args()
+    if args.large:
+        main_large()
+        return
+    if not args.reference:
+        ap.error("name the reference checkout with --reference or GLA_REFERENCE")
+    text = open(os.path.join(args.reference, REF_TEST_REL)).read()
     out = {"source": "GenericLinearAlgebra.jl v0.4.0 test/eigenselfadjoint.jl + 256-bit restatement",
            "precision_bits": MP.PREC}
     M = parse_issue123(text)

@@ -5,11 +5,22 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.json")
+GOLDEN_LARGE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden_large.json")
 
 
 def golden():
     with open(GOLDEN) as f:
         return json.load(f)
+
+
+def golden_large(n):
+    """The 256-bit fixture of order n in golden_large.json: (A, w256, V256),
+    w256 the eigenvalues rounded to float64, V256 the eigenvectors."""
+    import mpmath
+    with open(GOLDEN_LARGE) as f:
+        g = [c for c in json.load(f)["goe"] if c["n"] == n][0]
+    A = from_hex(g["A"])
+    return A, np.array([float(mpmath.mpf(v)) for v in g["w"]]), np.array(g["V"]), g["seed"]
 
 
 def goe(n, seed):

@@ -12,7 +12,7 @@ eigenvectors by residual, orthogonality and sign-normalised comparison):
 import numpy as np
 import pytest
 
-from helpers import from_hex, goe, golden, orth, prescribed, residual, sym_from, vec_parity
+from helpers import from_hex, goe, golden, golden_large, orth, prescribed, residual, sym_from, vec_parity
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -320,3 +320,22 @@ def test_cuda_graph_capture_and_replay(G, precision):
         torch.cuda.synchronize()
         assert (info.cpu().numpy() == 0).all()
         assert torch.equal(w, w2) and torch.equal(V, V2)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32_refined"])
+def test_goe_large_against_256bit(G, precision):
+    # the single-matrix workload (GOE n = 64, seed 1) and a GOE n = 128, solved
+    # alone and together in one batch, against the 256-bit restatement
+    import torch
+    cases = [golden_large(64), golden_large(128)]
+    single = [G.eigen(torch.tensor(A, device="cuda"), precision=precision) for A, _, _, _ in cases]
+    batched = G.eigen_batched([torch.tensor(A, device="cuda") for A, _, _, _ in cases], precision=precision)
+    for (A, w256, V256, _), r1, r2 in zip(cases, single, batched):
+        n = A.shape[0]
+        nA = np.linalg.norm(A, 2)
+        tol = 8 * n * EPS64 * nA if precision == "f64" else 1e-13 * nA
+        for r in (r1, r2):
+            w, V = r.values.cpu().numpy(), r.vectors.cpu().numpy()
+            assert np.abs(w - w256).max() <= tol
+            assert residual(A, V, w) <= 1e-13 and orth(V) <= 1e-13
+            assert vec_parity(A, V, V256, w256, tol_factor=1.0 if precision == "f64" else 10.0) <= 1.0

@@ -51,6 +51,44 @@ def test_f64_goe_vs_oracle(G, n):
     assert np.all(np.abs(dots[ok] - 1) <= 1e-6)
 
 
+def test_f64_goe_vs_oracle_n640(G):
+    # the oracle (the reference's QL restated) at the largest order it solves
+    # in a few seconds
+    n = 640
+    A = goe(n, 1000 + n)
+    ws, Vs, info = solve(G, [A])
+    assert info[0] == 0
+    wo, _, _ = O.syev(A)
+    nA = np.linalg.norm(A, 2)
+    assert np.max(np.abs(ws[0] - wo)) <= 1e-13 * nA
+    assert residual(A, Vs[0], ws[0]) <= 1e-13
+    assert orth(Vs[0]) <= 1e-13
+
+
+def c3_case(n):
+    """The precision workload at order n: A = Q diag(lam) Q', Q Haar (seed 3),
+    lam = +-logspace(-6, 0, n) with random signs (cond 1e6)."""
+    rng = np.random.default_rng(3)
+    lam = np.logspace(-6, 0, n) * rng.choice([-1.0, 1.0], n)
+    return prescribed(lam, 3), np.sort(lam)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32_refined"])
+def test_c3_n2048(G, precision):
+    # single n = 2048 of the precision workload, plain FP64 and FP32 + refinement:
+    # eigenvalues against the exact spectrum and against LAPACK, residual and
+    # orthogonality, all <= 1e-13 (relative to ||A|| = max |lam| = 1)
+    n = 2048
+    A, lam = c3_case(n)
+    ws, Vs, info = solve(G, [A], precision=precision)
+    assert info[0] == 0
+    w, V = ws[0], Vs[0]
+    assert np.max(np.abs(w - lam)) <= 1e-13
+    assert np.max(np.abs(w - np.linalg.eigvalsh(A))) <= 1e-13
+    assert residual(A, V, w) <= 1e-13
+    assert orth(V) <= 1e-13
+
+
 @pytest.mark.parametrize("n", [513, 1024])
 def test_f64_goe_vs_lapack(G, n):
     A = goe(n, 2000 + n)

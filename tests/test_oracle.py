@@ -117,6 +117,23 @@ def test_goe_against_256bit(n, seed):
         assert abs(mpmath.mpf(whi[i]) + mpmath.mpf(wlo[i]) - mpmath.mpf(g["w"][i])) <= 1e-30 * nA
 
 
+@pytest.mark.parametrize("n", [64, 128])
+def test_goe_large_against_256bit(n):
+    # the single-matrix workload (GOE n = 64, seed 1) and a GOE n = 128, at the
+    # orders of the reference's own BigFloat testsets (test/eigenselfadjoint.jl:5-52)
+    from helpers import golden_large
+    A, w256, V256, seed = golden_large(n)
+    assert np.array_equal(A, goe(n, seed))  # the fixture holds the seeded input bit for bit
+    nA = np.linalg.norm(A, 2)
+    for uplo in "LU":
+        w, V, info = O.syev(A, "V", uplo)
+        assert info == 0
+        assert np.abs(w - w256).max() <= 4 * n * 2.2e-16 * nA
+        assert vec_parity(A, V, V256, w256) <= 1.0
+    # the 256-bit eigenpairs themselves: residual and orthogonality at float64 rounding
+    assert residual(A, V256, w256) <= 4 * 2.2e-16 * n and orth(V256) <= 4 * 2.2e-16 * n
+
+
 def test_against_lapack():
     rng = np.random.default_rng(9)
     for n in [2, 3, 7, 31, 64, 100, 128]:

@@ -73,3 +73,45 @@ def test_static_rejects_orders_above_the_limit(env):
                             C.c_void_p(w.data_ptr()), C.byref(info), None)
     assert rc == lib.GLA_ERR_STATIC_TOO_LARGE
     assert b"GLA_STATIC_MAX_N" in L.gla_status_string(rc)
+
+
+def test_static_call_allocates_no_device_memory(env):
+    # cudaMemGetInfo (torch.cuda.mem_get_info) sees every device allocation,
+    # raw cudaMalloc included, unlike the caching allocator's statistics
+    torch, L, _ = env
+    A = goe(96, 31)
+    call(torch, L, L.gla_dsyev_static, A, "V", "L")  # warm-up: the per-device set-up
+    cases = [(77, b"V"), (77, b"N"), (96, b"V"), (5, b"N")]
+    bufs = []
+    for n, _ in cases:  # every device buffer exists before the first reading
+        b = torch.zeros((96, 96), dtype=torch.float64, device="cuda")
+        b[:n, :n] = torch.tensor(goe(n, 40 + n), device="cuda")
+        bufs.append(b)
+    w = torch.empty(96, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    info = C.c_int(0)
+    for (n, jobz), buf in zip(cases, bufs):
+        rc = L.gla_dsyev_static(jobz, b"L", n, C.c_void_p(buf.data_ptr()), 96, C.c_void_p(w.data_ptr()),
+                                C.byref(info), None)
+        assert rc == 0 and info.value == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] >= free0
+
+
+def test_static_recovers_after_a_failed_call(env):
+    # a call stopped early by non-finite input must leave nothing behind that
+    # changes the next call's result
+    torch, L, _ = env
+    n = 50
+    A = goe(n, 77)
+    Abad = A.copy()
+    Abad[7, 3] = Abad[3, 7] = np.nan
+    rb, infb, _, _ = call(torch, L, L.gla_dsyev_static, Abad, "V", "L")
+    assert rb == 1 and infb != 0
+    rs, infs, ws, Vs = call(torch, L, L.gla_dsyev_static, A, "V", "L")
+    ra, infa, wa, Va = call(torch, L, L.gla_dsyev, A, "V", "L")
+    assert rs == 0 and infs == 0 and ra == 0 and infa == 0
+    assert np.abs(ws - wa).max() <= 8 * n * EPS64 * np.linalg.norm(A, 2)
+    assert residual(A, Vs, ws) <= 1e-13 and orth(Vs) <= 1e-13
+    assert vec_parity(A, Vs, Va, wa) <= 1.0
