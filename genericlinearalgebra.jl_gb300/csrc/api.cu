@@ -147,6 +147,7 @@ struct gla_plan_s {
   // a phase's time is the sum over buckets of its kernels' stream time
   bool timing = false;
   bool graph = false;  // capture-safe execute (no host synchronisation)
+  bool stein = false;  // F32_REFINED: FP32 stage by bisection + twisted factorisation (small_stein.cuh)
   cudaEvent_t tev[kMaxBuckets][GLA_NUM_PHASES][2] = {};
   bool tused[kMaxBuckets][GLA_NUM_PHASES] = {};
   void mark(int b, int phase, int end, cudaStream_t st) {
@@ -206,7 +207,8 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     // large orders: no capture-safe mode (their solves synchronise)
     if (any_large && (flags & GLA_FLAG_GRAPH)) return -8;
   }
-  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH | GLA_FLAG_AUTOTUNE)) != 0 ||
+  if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH | GLA_FLAG_AUTOTUNE |
+                 GLA_FLAG_REFINE_QL)) != 0 ||
       (flags & 3) > GLA_ALG_QR)
     return -8;
   GLA_CUDA(ensure_init());
@@ -221,6 +223,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? kTolF64 : kTolF32);
   p->timing = (flags & GLA_FLAG_TIMING) != 0;
   p->graph = (flags & GLA_FLAG_GRAPH) != 0;
+  p->stein = precision == GLA_PREC_F32_REFINED && !(flags & GLA_FLAG_REFINE_QL);
   p->n.assign(n, n + batch);
 
   // ---- descriptors and offsets
@@ -366,7 +369,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     return -1000 - (int)err;
   }
   if (flags & GLA_FLAG_AUTOTUNE) {
-    int rc = autotune_plan(p, flags & (3 | GLA_FLAG_SMALL_LOG));
+    int rc = autotune_plan(p, flags & (3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_REFINE_QL));
     if (rc) {
       gla_plan_destroy(p);
       return rc;
@@ -580,8 +583,9 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
     cudaStream_t s = bk.stream;
     GLA_CUDA(cudaStreamWaitEvent(s, p->fork, 0));
     p->mark(b, GLA_PHASE_TRIDIAG, 0, s);
-    GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt_tri, tridiag_smem_bytes(bk.nmax, bk.nt_tri, el), s, p->d_desc,
-                            p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, Q, info, p->d_cst, p->d_scale));
+    GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt_tri, tridiag_smem_bytes(bk.nmax, bk.nt_tri, el, p->stein), s,
+                            p->d_desc, p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, Q, info, p->d_cst,
+                            p->d_scale, p->stein, wq));
     p->mark(b, GLA_PHASE_TRIDIAG, 1, s);
     if (wantq) {
       const int npass = p->graph ? kGraphPasses : kAsyncPasses;
@@ -1079,7 +1083,7 @@ __global__ void k_tune_fill(T* A, int n, long long total) {
 }
 
 struct TuneKey {
-  int fam;  // 0: FP64 kernels, 1: FP32 kernels
+  int fam;  // 0: FP64 kernels, 1: FP32 kernels, 2: FP32 + refinement with the in-kernel tridiagonal solver
   char jobz;
   int range;   // orders 16 range + 1 .. 16 (range + 1)
   int cclass;  // floor(log2(matrices in the bucket))
@@ -1131,8 +1135,10 @@ int tune_probe(int prec, char jobz, int n, int count, int base_flags, int tri_mu
 int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
   const int n = 16 * (k.range + 1);
   count = std::max(1, std::min(count, kTuneMaxCount));
-  const int prec = k.fam == 0 ? GLA_PREC_F64 : GLA_PREC_F32;
-  const size_t el = k.fam == 0 ? 8 : 4;
+  // family 2: FP32 + refinement with the in-kernel tridiagonal solver (its
+  // tridiagonalisation kernel does the FP32 solve; FP64 input)
+  const int prec = k.fam == 0 ? GLA_PREC_F64 : (k.fam == 1 ? GLA_PREC_F32 : GLA_PREC_F32_REFINED);
+  const size_t el = k.fam == 1 ? 4 : 8;
   void *A = nullptr, *w = nullptr, *V = nullptr;
   int* info = nullptr;
   const long long total = (long long)count * n * n;
@@ -1141,7 +1147,7 @@ int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
   if (e == cudaSuccess) e = cudaMalloc(&w, el * (size_t)count * n);
   if (e == cudaSuccess) e = cudaMalloc((void**)&info, sizeof(int) * count);
   if (e == cudaSuccess) {
-    if (k.fam == 0)
+    if (k.fam != 1)
       k_tune_fill<double><<<1024, 256>>>((double*)A, n, total);
     else
       k_tune_fill<float><<<1024, 256>>>((float*)A, n, total);
@@ -1164,7 +1170,7 @@ int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
   // plan, where all buckets share the SMs: a warp pays its FP64 (and most
   // FP32) issue slots for 32 lanes whatever the number active
   for (int lpw : {4, 8, 16, 32}) {
-    if (rc) break;
+    if (rc || k.fam == 2) break;  // family 2 chases only the rare matrices its solver leaves
     float t = 0, c = 0;
     rc = tune_probe(prec, k.jobz, n, count, base_flags, best.tri_mult, lpw, A, w, V, info, &t, &c);
     if (rc == 0 && c < best.chase_ms) {
@@ -1182,7 +1188,7 @@ int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
 }
 
 int autotune_plan(gla_plan_t p, int base_flags) {
-  const int fam = p->prec == GLA_PREC_F64 ? 0 : 1;
+  const int fam = p->prec == GLA_PREC_F64 ? 0 : (p->stein ? 2 : 1);
   const char jz = p->prec == GLA_PREC_F32_REFINED ? 'V' : p->jobz;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   for (Bucket& bk : p->buckets) {

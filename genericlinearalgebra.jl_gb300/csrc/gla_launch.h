@@ -19,16 +19,20 @@ constexpr int kMaxPasses = 64;      // chase passes before a full rotation log i
 constexpr double kTolF64 = 0x1p-52;  // default deflation tolerance, eps(Float64)
 constexpr double kTolF32 = (double)0x1p-23f;  // eps(Float32)
 
-size_t tridiag_smem_bytes(int n, int nt, int elem);
+size_t tridiag_smem_bytes(int n, int nt, int elem, bool stein = false);
 size_t chase_smem_bytes(int nmax, int elem);
 size_t apply_smem_bytes(int n, int elem);
 
 // Raise the dynamic shared-memory limit of every kernel instantiation once.
 cudaError_t small_kernels_init();
 
+// stein (kF32FromF64 with Q only): the CTA also solves the tridiagonal
+// (bisection + twisted factorisation) and writes X = Q Y and the eigenvalues
+// (to w) for every matrix it does not leave to the QL chase.
 cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
                            const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
-                           void* Q, int* info, ChaseState* cst, int* scale_exp);
+                           void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein = false,
+                           void* w = nullptr);
 
 cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,

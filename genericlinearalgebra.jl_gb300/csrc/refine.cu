@@ -287,10 +287,11 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     // orthogonality, and leaving it changes the residual by less than the
     // floor; rotations below 1e-8 cost nothing and are kept
     const float tfloor = (float)(1e-14 * lmax_s);
-    float emax = 0.f;
+    float emax = 0.f, rmax = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
       const int i = idx % n, j = idx / n;
       const float rhalf = 0.5f * (cR[idx].hi + cR[idx].lo);
+      rmax = fmaxf(rmax, fabsf(rhalf));
       float e = rhalf;
       if (cid[i] != cid[j]) {
         const float gap = (float)(lam[j] - lam[i]);
@@ -303,6 +304,7 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
       emax = fmaxf(emax, fabsf(e));
     }
     emax = block_max_f(emax, red);
+    rmax = 2.f * block_max_f(rmax, red);
     // ---- X <- X + X E (FP32 product, see above), then Rayleigh-Ritz inside clusters
     tile_gemm_f32(
         n, [&](int i, int k) { return it == 0 ? X0[(size_t)k * n + i] : X[(size_t)k * n + i].hi; },
@@ -348,11 +350,48 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
         if (tid < 32) jacobi_warp(k, C, Z);
         __syncthreads();
         if (offc > 0x1p-30f * fmaxf(anorm, 1e-30f) && tid == 0) flag_s = 1;
-        // Y[:, J] <- Y[:, J] Z  (temporary in X, whose old values are no longer needed)
+        // Z is orthogonal only to FP32 rounding (its Jacobi sweeps leave up to
+        // ~1e-6); rotating by it every iteration would re-inject that much
+        // non-orthogonality and stall the iteration there. Two Newton-Schulz
+        // steps in double-float, Z <- Z (I + (I - Z'Z)/2), take it to ~1e-15:
+        // Z keeps the high parts, Zl (over C, no longer needed) the low parts,
+        // G = I - Z'Z (small, FP32 suffices) goes to T1 (consumed by the
+        // update above) and the FP32 correction Z G / 2 to the storage of X
+        // (whose old values are no longer needed).
+        float* Zl = C;
+        float* G = T1;
+        float* Cr = reinterpret_cast<float*>(X);
+        for (int idx = tid; idx < k * k; idx += kRT) Zl[idx] = 0.f;
+        __syncthreads();
+        for (int ns = 0; ns < 2; ns++) {
+          for (int idx = tid; idx < k * k; idx += kRT) {
+            const int a = idx % k, b = idx / k;
+            df64 g = df_make(a == b ? 1.f : 0.f, 0.f);
+            for (int q = 0; q < k; q++)
+              g = df_mac(g, df_make(-Z[a * k + q], -Zl[a * k + q]), df_make(Z[b * k + q], Zl[b * k + q]));
+            G[idx] = g.hi + g.lo;
+          }
+          __syncthreads();
+          for (int idx = tid; idx < k * k; idx += kRT) {
+            const int a = idx % k, b = idx / k;
+            float acc = 0.f;
+            for (int q = 0; q < k; q++) acc = fmaf(Z[q * k + a], G[b * k + q], acc);
+            Cr[idx] = 0.5f * acc;
+          }
+          __syncthreads();
+          for (int idx = tid; idx < k * k; idx += kRT) {
+            const df64 z = df_add(df_make(Z[idx], Zl[idx]), df_make(Cr[idx], 0.f));
+            Z[idx] = z.hi;
+            Zl[idx] = z.lo;
+          }
+          __syncthreads();
+        }
+        // Y[:, J] <- Y[:, J] Z  (temporary in X)
         for (int idx = tid; idx < n * k; idx += kRT) {
           const int i = idx % n, b = idx / n;
           df64 acc = zero;
-          for (int q = 0; q < k; q++) acc = df_mac(acc, Y[(size_t)ord[r0 + q] * n + i], Z[b * k + q]);
+          for (int q = 0; q < k; q++)
+            acc = df_mac(acc, Y[(size_t)ord[r0 + q] * n + i], df_make(Z[b * k + q], Zl[b * k + q]));
           X[(size_t)b * n + i] = acc;
         }
         __syncthreads();
@@ -377,7 +416,10 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     // 2^-47 ||A|| / gap at the tightest gaps, and the iterate is at the
     // accuracy floor of the scheme
     const bool quad = (double)emax * emax * lmax_s < 1e-14 * gmin_s;
-    const bool stalled = it > 0 && emax < 1e-6f && emax > 0.25f * emax_prev;
+    // (a stall counts only once the orthogonality defect of the iterate is
+    // below 1e-13 entrywise, its rounding floor in double-float being about
+    // 2e-14: the noise then sits in the tight-gap rotations)
+    const bool stalled = it > 0 && emax < 1e-6f && emax > 0.25f * emax_prev && rmax <= 1e-13f;
     emax_prev = emax;
     if (flag_s == 0 && (quad || stalled || delta <= 1e-13f * anorm)) {
       converged = true;

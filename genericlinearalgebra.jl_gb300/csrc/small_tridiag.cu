@@ -18,6 +18,7 @@
 //   reflectors (H_k applied only to the already-formed trailing block).
 #include "gla_launch.h"
 #include "gla_small.cuh"
+#include "small_stein.cuh"
 
 namespace gla {
 
@@ -61,17 +62,65 @@ GLA_DEV void block_sum_max(T v, unsigned long long m, T* red, unsigned long long
 // (stride ld across the lanes of a warp) spread over all shared-memory banks.
 GLA_DEV int stage_ld(int n) { return (n + 1) | 1; }
 
-size_t tridiag_smem_bytes(int n, int nt, int elem) {
+size_t tridiag_smem_bytes(int n, int nt, int elem, bool stein) {
   // redm[32] u64 | red[32] (8-byte slots) | S[n*ld] | vv,uu,ww,taus [n] | part[8*nt]
+  // [| the FP32 tridiagonal solver's arrays (stein, float only)]
   const size_t ld = (size_t)((n + 1) | 1);
-  return 512 + (size_t)elem * ((size_t)n * ld + 4 * (size_t)n + 8 * (size_t)nt);
+  return 512 + (size_t)elem * ((size_t)n * ld + 4 * (size_t)n + 8 * (size_t)nt) +
+         (stein ? 4 * stein_extra_words(n) : 0);
 }
 
-template <class T, class Tin, bool WANTQ>
+// X = Q Y (n x n, Q column-major in S with leading dimension ld, Y row-major
+// in Ys with leading dimension ldy), stored column-major to Xg. Thread
+// tiles of 8 x 8 outputs with rows and columns strided by ceil(n/8), so that
+// the threads of a warp read consecutive (or identical) shared words.
+GLA_DEV void small_gemm_qy(int n, const float* __restrict__ S, int ld, const float* __restrict__ Ys, int ldy,
+                           float* __restrict__ Xg) {
+  const int nt8 = (n + 7) >> 3;
+  for (int t = threadIdx.x; t < nt8 * nt8; t += blockDim.x) {
+    const int ti = t % nt8, tk = t / nt8;
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+#pragma unroll
+      for (int v = 0; v < 8; v++) acc[u][v] = 0.f;
+    int iu[8], kv[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      iu[u] = min(ti + nt8 * u, n - 1);  // clamped: rows/columns past n are computed and not stored
+      kv[u] = min(tk + nt8 * u, n - 1);
+    }
+    for (int j = 0; j < n; j++) {
+      float q[8], y[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) q[u] = S[(size_t)j * ld + iu[u]];
+#pragma unroll
+      for (int v = 0; v < 8; v++) y[v] = Ys[(size_t)j * ldy + kv[v]];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+#pragma unroll
+        for (int v = 0; v < 8; v++) acc[u][v] = fmaf(q[u], y[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+#pragma unroll
+      for (int v = 0; v < 8; v++) {
+        const int i = ti + nt8 * u, k = tk + nt8 * v;
+        if (i < n && k < n) Xg[(size_t)k * n + i] = acc[u][v];
+      }
+  }
+}
+
+// STEIN (float only, FP32 + refinement path): after forming Q, solve the
+// tridiagonal in the same CTA (small_stein.cuh) and write X = Q Y and the
+// ascending eigenvalues (times 2^scale) to wout, marking the matrix done for
+// the chase; a matrix the solver leaves to the QL chase gets Q as usual.
+template <class T, class Tin, bool WANTQ, bool STEIN>
 __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                  const Tin* __restrict__ A, int lower, T* __restrict__ dout,
                                                  T* __restrict__ eout, T* __restrict__ Qout, int* __restrict__ info,
-                                                 ChaseState* __restrict__ cst, int* __restrict__ scale_exp) {
+                                                 ChaseState* __restrict__ cst, int* __restrict__ scale_exp,
+                                                 T* __restrict__ wout) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int mid = perm[blockIdx.x];
   const SmallDesc dsc = descs[mid];
@@ -247,8 +296,13 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
   T* dg = dout + dsc.w_off;
   T* eg = eout + dsc.w_off;
   for (int i = tid; i < n; i += NT) {
-    dg[i] = S[(size_t)i * ld + i];
-    eg[i] = (i + 1 < n) ? S[(size_t)i * ld + i + 1] : T(0);
+    const T di = S[(size_t)i * ld + i], ei = (i + 1 < n) ? S[(size_t)i * ld + i + 1] : T(0);
+    dg[i] = di;
+    eg[i] = ei;
+    if (STEIN) {  // uu, ww are free after the reduction: d and e for the tridiagonal solver
+      uu[i] = di;
+      ww[i] = ei;
+    }
   }
   if (!WANTQ) return;
   __syncthreads();
@@ -300,14 +354,103 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
   for (int r = tid; r < n; r += NT) S[r] = (r == 0) ? T(1) : T(0);
   __syncthreads();
   T* Qg = Qout + dsc.a_off;
+  if constexpr (STEIN) {
+    const int ldy = stein_ldy(n);
+    float* Ys = part + 8 * NT;
+    float* e2s = Ys + (size_t)n * ldy;
+    float* lams = e2s + n;
+    int* misc = reinterpret_cast<int*>(lams + n);  // [0] give up, [1] clusters, [2 + 2c], [3 + 2c] bounds
+    const float* dd = uu;
+    const float* ee = ww;
+    // Gershgorin interval, ||T|| bound, pivmin (LAPACK dstebz's safeguards)
+    float glo = 3.0e38f, ghi = -3.0e38f, e2max = 0.f;
+    for (int i = tid; i < n; i += NT) {
+      const float ai = (i > 0 ? fabsf(ee[i - 1]) : 0.f) + (i + 1 < n ? fabsf(ee[i]) : 0.f);
+      glo = fminf(glo, dd[i] - ai);
+      ghi = fmaxf(ghi, dd[i] + ai);
+      const float e2 = (i + 1 < n) ? ee[i] * ee[i] : 0.f;
+      e2s[i] = e2;
+      e2max = fmaxf(e2max, e2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+      ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+      e2max = fmaxf(e2max, __shfl_xor_sync(0xffffffffu, e2max, o));
+    }
+    // red (32 8-byte slots) holds the per-warp minima and maxima, redm the e^2 maxima
+    float* fred = reinterpret_cast<float*>(red);
+    float* fred2 = reinterpret_cast<float*>(redm);
+    if ((tid & 31) == 0) {
+      fred[tid >> 5] = glo;
+      fred[32 + (tid >> 5)] = ghi;
+      fred2[tid >> 5] = e2max;
+    }
+    if (tid == 0) misc[0] = 0;
+    __syncthreads();
+    for (int w = 0; w < (NT >> 5); w++) {
+      glo = fminf(glo, fred[w]);
+      ghi = fmaxf(ghi, fred[32 + w]);
+      e2max = fmaxf(e2max, fred2[w]);
+    }
+    const float tnorm = fmaxf(fabsf(glo), fabsf(ghi));
+    const float pivmin = 0x1p-100f * fmaxf(1.f, e2max);
+    const float widen = 2.f * (float)n * prec<float>::eps * tnorm + 2.f * pivmin;
+    glo -= widen;
+    ghi += widen;
+    const float atol = 2.f * prec<float>::eps * tnorm + 4.f * pivmin;
+    if (tid < n) lams[tid] = eig_bisect(n, dd, e2s, tid, glo, ghi, atol, pivmin);
+    __syncthreads();
+    // strict: a zero gap is tight even when ||T|| = 0
+    if (tid + 1 < n && !(lams[tid + 1] - lams[tid] > kTightGap * tnorm)) misc[0] = 1;
+    __syncthreads();
+    if (misc[0] == 0) {
+      if (tid < n && !twisted_vector(n, dd, ee, e2s, lams[tid], pivmin, Ys, ldy, tid)) misc[0] = 1;
+      if (tid == 0) {  // clusters of two or more eigenvalues within kLooseGap ||T||
+        int nc = 0, s0 = 0;
+        for (int k = 1; k <= n; k++) {
+          if (k == n || lams[k] - lams[k - 1] > kLooseGap * tnorm) {
+            if (k - s0 >= 2) {
+              misc[2 + 2 * nc] = s0;
+              misc[3 + 2 * nc] = k;
+              nc++;
+            }
+            s0 = k;
+          }
+        }
+        misc[1] = nc;
+      }
+      __syncthreads();
+      const int nc = misc[1];
+      for (int c = tid >> 5; c < nc; c += NT >> 5)
+        if (!mgs_cluster(n, Ys, ldy, misc[2 + 2 * c], misc[3 + 2 * c]) && (tid & 31) == 0) misc[0] = 1;
+      __syncthreads();
+    }
+    if (misc[0] == 0) {
+      small_gemm_qy(n, S, ld, Ys, ldy, Qg);
+      for (int k = tid; k < n; k += NT) wout[dsc.w_off + k] = sexp ? ldexpf(lams[k], sexp) : lams[k];
+      if (tid == 0) {
+        ChaseState st;
+        st.bs = n;
+        st.nsweeps = 0;
+        st.nrot = 0;
+        st.nhdr = 0;
+        st.status = kChaseDone;
+        st.applied = 1;
+        cst[mid] = st;
+      }
+      return;
+    }
+    // left to the QL chase: Q below, the chase state stays "running"
+  }
   for (int j = 0; j < n; j++)
     for (int i = tid; i < n; i += NT) Qg[(size_t)j * n + i] = S[(size_t)j * ld + i];
 }
 
 
-template <class T, class Tin, bool Q> static void set_tri_attr() {
-  cudaFuncSetAttribute(k_tridiag<T, Tin, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)tridiag_smem_bytes(kSmallMaxN, 256, sizeof(T)));
+template <class T, class Tin, bool Q, bool ST = false> static void set_tri_attr() {
+  cudaFuncSetAttribute(k_tridiag<T, Tin, Q, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tridiag_smem_bytes(kSmallMaxN, 256, sizeof(T), ST));
 }
 
 cudaError_t tridiag_kernels_init() {
@@ -317,24 +460,27 @@ cudaError_t tridiag_kernels_init() {
   set_tri_attr<float, float, false>();
   set_tri_attr<float, double, true>();
   set_tri_attr<float, double, false>();
+  set_tri_attr<float, double, true, true>();
   return cudaGetLastError();
 }
 
 cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
                            const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
-                           void* Q, int* info, ChaseState* cst, int* scale_exp) {
+                           void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein, void* w) {
   if (nblocks <= 0) return cudaSuccess;
-#define GLA_TRI(T, Tin, WQ) \
-  k_tridiag<T, Tin, WQ><<<nblocks, nt, smem, st>>>(descs, perm, (const Tin*)A, lower, (T*)d, (T*)e, (T*)Q, info, cst, scale_exp)
+#define GLA_TRI(T, Tin, WQ, ST)                                                                                 \
+  k_tridiag<T, Tin, WQ, ST><<<nblocks, nt, smem, st>>>(descs, perm, (const Tin*)A, lower, (T*)d, (T*)e, (T*)Q, \
+                                                       info, cst, scale_exp, (T*)w)
   if (tcode == kF64) {
-    if (wantq) GLA_TRI(double, double, true);
-    else GLA_TRI(double, double, false);
+    if (wantq) GLA_TRI(double, double, true, false);
+    else GLA_TRI(double, double, false, false);
   } else if (tcode == kF32) {
-    if (wantq) GLA_TRI(float, float, true);
-    else GLA_TRI(float, float, false);
+    if (wantq) GLA_TRI(float, float, true, false);
+    else GLA_TRI(float, float, false, false);
   } else {
-    if (wantq) GLA_TRI(float, double, true);
-    else GLA_TRI(float, double, false);
+    if (wantq && stein) GLA_TRI(float, double, true, true);
+    else if (wantq) GLA_TRI(float, double, true, false);
+    else GLA_TRI(float, double, false, false);
   }
 #undef GLA_TRI
   return cudaGetLastError();

@@ -68,6 +68,13 @@ extern "C" {
  * on synthetic matrices of the bucket's order and count (synchronizes the
  * device; a few seconds for a fresh table) and added. See gla_autotune_*. */
 #define GLA_FLAG_AUTOTUNE 32
+/* Flag bit (GLA_PREC_F32_REFINED, orders <= 128): run the FP32 stage with the
+ * reference's QL chase (as GLA_PREC_F32 does) instead of the default
+ * per-eigenvalue solver (bisection on Sturm counts plus one twisted
+ * factorisation per eigenvector, inside the tridiagonalisation kernel, with
+ * the QL chase only for matrices whose eigenvalues come within 2e-5 ||T||
+ * of each other). Both feed the same refinement. */
+#define GLA_FLAG_REFINE_QL 64
 
 /* Phases reported by gla_plan_phase_times. */
 #define GLA_PHASE_TRIDIAG 0 /* symtri! + Array(Q)          */
