@@ -1042,8 +1042,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch shapes instead of the autotuner's")
     ap.add_argument("--solve", type=int, default=0,
                     help="profiling: two solves of one GOE matrix of this order on the first of --paths")
-    ap.add_argument("--c3-solve", action="store_true",
-                    help="profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix only")
+    ap.add_argument("--c3-solve", type=int, default=0, metavar="N",
+                    help="profiling: two FP32 + refinement solves of the cond-1e6 matrix of order N only")
     ap.add_argument("--c4", action="store_true",
                     help="only the differentiation workload (forward + adjoint, eager and one CUDA graph)")
     ap.add_argument("--cpu-lapack", type=int, default=0,
@@ -1086,14 +1086,15 @@ def main():
         print(json.dumps({"n": n, "path": prec, "info": int(info.item())}), flush=True)
         return
     if args.c3_solve:
-        # profiling: two FP32 + refinement solves of the n = 4096 cond-1e6 matrix
+        # profiling: two FP32 + refinement solves of the cond-1e6 matrix of order N
         import torch
         import glagpu
-        A, lam = large_case("c3", 4096)
-        plan = glagpu.Plan([4096], precision="f32_refined")
+        N = args.c3_solve
+        A, lam = large_case("c3", N)
+        plan = glagpu.Plan([N], precision="f32_refined")
         Ad = plan.pack([A], device="cuda")
-        w = torch.empty(4096, dtype=torch.float64, device="cuda")
-        V = torch.empty(4096 * 4096, dtype=torch.float64, device="cuda")
+        w = torch.empty(N, dtype=torch.float64, device="cuda")
+        V = torch.empty(N * N, dtype=torch.float64, device="cuda")
         info = torch.zeros(1, dtype=torch.int32, device="cuda")
         for _ in range(2):
             plan.execute(Ad, w, V, info)

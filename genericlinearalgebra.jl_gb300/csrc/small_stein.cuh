@@ -21,8 +21,8 @@
 //   4. X = Q Y, the eigenvectors of the dense matrix (columns ascending).
 //
 // A matrix whose eigenvalues come within kTightGap ||T|| of each other
-// (there the FP32 vectors of distinct eigenvalues stop being
-// distinguishable), or whose vectors degenerate, is left to the QL chase:
+// (there FP32 bisection no longer separates them), or whose vectors
+// degenerate, is left to the QL chase:
 // the CTA then writes Q as the plain path does and the chase and
 // rotation-replay kernels finish it. The refinement that follows restores
 // FP64 accuracy for both.
@@ -32,7 +32,13 @@
 namespace gla {
 
 constexpr float kLooseGap = 1e-3f;  // cluster bound (re-orthogonalise inside)
-constexpr float kTightGap = 2e-5f;  // at or below: leave the matrix to the QL chase
+// At or below kTightGap ||T|| (8 ulps of ||T||) leave the matrix to the QL
+// chase. Above it the FP32 vectors of a close pair are each off by up to
+// ~eps ||T|| / gap inside the pair's invariant subspace, which the
+// Gram-Schmidt step and the refinement's Ritz rotation remove; a pair whose
+// vectors come out nearly parallel fails the Gram-Schmidt norm test and
+// goes to the chase as well.
+constexpr float kTightGap = 1e-6f;
 
 // 1/x from the MUFU seed (one rounding; the recurrences tolerate it: a
 // relative perturbation of the pivots of a few ulps).

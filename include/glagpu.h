@@ -72,7 +72,7 @@ extern "C" {
  * reference's QL chase (as GLA_PREC_F32 does) instead of the default
  * per-eigenvalue solver (bisection on Sturm counts plus one twisted
  * factorisation per eigenvector, inside the tridiagonalisation kernel, with
- * the QL chase only for matrices whose eigenvalues come within 2e-5 ||T||
+ * the QL chase only for matrices whose eigenvalues come within 1e-6 ||T||
  * of each other). Both feed the same refinement. */
 #define GLA_FLAG_REFINE_QL 64
 
