@@ -39,6 +39,9 @@ for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
         sys.path.insert(0, _p)
 
 METRIC = "eigh/s (batch n≤128) & n=4096 time at 1e-13 resid: FP32+refine vs FP64 GPU"
+# DRAM bytes (read + write) of the eight k_refine launches of one step of the
+# 1024-matrix workload (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+REFINE_DRAM_BYTES_PER_1024 = None
 BATCH = 4096
 NLO, NHI = 8, 128
 SEED = 2
@@ -77,22 +80,38 @@ def launches_per_step(n_buckets, passes, refined, graph):
     return n_buckets * (1 + 2 * passes + (1 if refined else 0) + (1 if graph else 0))
 
 
-def chase_roofline(counters, chase_ms, ops_peak, pipe):
-    """Roofline figures of k_chase, the kernel with the largest share of the
-    batched step's ncu launch list. Algorithmic work: 16 operations per
-    rotation of the shifted-QL recurrence (src/eigenSelfAdjoint.jl:389-405:
-    the Givens rotation's hypot, square root and two divisions, e, gamma, d
-    and the next pi), times the rotations the chase applied (the plan's
-    counter); achieved = that over the summed chase time of all size buckets;
-    peak = the pipe's measured FMA rate. One lane runs one matrix's serial
-    recurrence, so the kernel is latency-bound and frac is small by
-    construction: the buckets' streams overlap it with the other phases."""
-    ops = 16.0 * counters["rotations"]
-    achieved = ops / (chase_ms * 1e-3) / 1e12 if chase_ms > 0 else 0.0
-    return {"kernel": "k_chase", "bound": "latency", "achieved": achieved, "peak": ops_peak,
-            "unit": f"T {pipe} ops/s", "frac": (achieved / ops_peak) if ops_peak else None, "traffic": None,
-            "note": "serial recurrence, one lane per matrix; leads the batched step's ncu launch list; "
-                    "k_refine, the throughput kernel, is roofline_refine"}
+def refine_roofline(achieved, peak_ops, batch):
+    """k_refine, the largest share of the batched refined step's ncu launch
+    list: double-float Ogita-Aishima products on the FP32 pipe. achieved =
+    FP32 operations per second, counted as 13 instructions per double-float
+    multiply-add (TwoProduct 2, TwoSum 6, 2 adds, QuickTwoSum 3) and ~3 n^3
+    multiply-adds per iteration (A X, X'(AX), X'X as symmetric halves, X E),
+    over the refinement's phase time (CUDA events on each size bucket's
+    stream); peak = the FP32 FMA rate of cuBLAS SGEMM measured in this run.
+    traffic: DRAM bytes of one step's k_refine launches from an ncu capture
+    of the 1024-matrix case (same order distribution) scaled by the matrix
+    count; the algorithmic bytes are ~20 sum(n^2) = 0.48 GB per step, the
+    rest is the per-matrix double-float scratch (56 n^2 bytes) that no
+    longer fits in L2 at this batch size."""
+    return {"kernel": "k_refine", "bound": "fp32", "achieved": achieved, "peak": peak_ops, "unit": "T FP32 ops/s",
+            "frac": (achieved / peak_ops) if peak_ops else None,
+            "traffic": REFINE_DRAM_BYTES_PER_1024 * batch / 1024 if REFINE_DRAM_BYTES_PER_1024 else None,
+            "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, FMA rate (FP32 pipe); "
+                           "MEASURED_PEAKS.json has only HBM and bf16 peaks"}
+
+
+def tridiag_roofline(ns, tri_ms, peak_ops):
+    """k_tridiag with the in-kernel FP32 tridiagonal solver (the second share
+    of the launch list): (4/3 + 4/3 + 2) n^3 flops per matrix (reduction, Q
+    formation, X = Q Y; the O(n^2) bisection and vectors not counted), over
+    the tridiagonalisation phase time; peak = twice the FP32 FMA rate.
+    Latency-bound (one CTA per matrix, n dependent reflector steps, 2.1
+    barrier stalls per issue), so the fraction is small by construction."""
+    flops = (4.0 / 3.0 + 4.0 / 3.0 + 2.0) * float((ns.astype(np.float64) ** 3).sum())
+    achieved = flops / (tri_ms * 1e-3) / 1e12 if tri_ms > 0 else 0.0
+    return {"kernel": "k_tridiag (with the FP32 tridiagonal solver)", "bound": "latency", "achieved": achieved,
+            "peak": 2.0 * peak_ops if peak_ops else None, "unit": "TFLOP/s FP32",
+            "frac": achieved / (2.0 * peak_ops) if peak_ops else None, "traffic": None}
 
 
 def replica_seed(rank):
@@ -423,19 +442,8 @@ def run_ours(args):
                        "path": hp, "batch": len(ns), "sum_n": int(ns.sum()), "sum_n3": ns3,
                        "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}",
                        "timing": "CUDA-graph replay of the whole batched solve (plan with GLA_FLAG_GRAPH)"},
-            "roofline": chase_roofline(c, ph.get("chase", 0.0), peak_ops if hp == "f32_refined" else
-                                       (peak / 2.0 if peak else None), "FP32" if hp == "f32_refined" else "FP64"),
-            "roofline_refine": {"kernel": "k_refine", "bound": "fp32",
-                         "achieved": achieved, "peak": peak_ops, "unit": "T FP32 ops/s",
-                         "frac": (achieved / peak_ops) if peak_ops else None,
-                         # DRAM bytes of one step's k_refine launches (all buckets), from an ncu
-                         # capture of the 512-matrix case scaled by the matrix count
-                         "traffic": 66.0e6 * len(ns) / 512,
-                         "traffic_note": "bytes per step, from an ncu capture of the 512-matrix case "
-                                         "scaled by the matrix count; algorithmic ~20 sum(n^2) bytes",
-                         "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, FMA rate (FP32 pipe); "
-                                        "MEASURED_PEAKS.json has only HBM and bf16 peaks",
-                         "note": "double-float arithmetic on the FP32 pipe"},
+            "roofline": refine_roofline(achieved, peak_ops, len(ns)),
+            "roofline_tridiag": tridiag_roofline(ns, ph.get("tridiag", 0.0), peak_ops),
             "roofline_large": large_roofline(large, measured_peaks_file()),
             "fp64_dgemm_tflops_measured": peak,
             "cpu_baseline": cpu,

@@ -147,7 +147,7 @@ struct gla_plan_s {
   // a phase's time is the sum over buckets of its kernels' stream time
   bool timing = false;
   bool graph = false;  // capture-safe execute (no host synchronisation)
-  bool stein = false;  // F32_REFINED: FP32 stage by bisection + twisted factorisation (small_stein.cuh)
+  bool stein = false;  // FP32 stage by bisection + twisted factorisation (small_stein.cuh)
   cudaEvent_t tev[kMaxBuckets][GLA_NUM_PHASES][2] = {};
   bool tused[kMaxBuckets][GLA_NUM_PHASES] = {};
   void mark(int b, int phase, int end, cudaStream_t st) {
@@ -208,7 +208,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     if (any_large && (flags & GLA_FLAG_GRAPH)) return -8;
   }
   if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH | GLA_FLAG_AUTOTUNE |
-                 GLA_FLAG_REFINE_QL)) != 0 ||
+                 GLA_FLAG_REFINE_QL | GLA_FLAG_F32_BISECT)) != 0 ||
       (flags & 3) > GLA_ALG_QR)
     return -8;
   GLA_CUDA(ensure_init());
@@ -223,7 +223,8 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->tol = tol > 0 ? tol : (precision == GLA_PREC_F64 ? kTolF64 : kTolF32);
   p->timing = (flags & GLA_FLAG_TIMING) != 0;
   p->graph = (flags & GLA_FLAG_GRAPH) != 0;
-  p->stein = precision == GLA_PREC_F32_REFINED && !(flags & GLA_FLAG_REFINE_QL);
+  p->stein = (precision == GLA_PREC_F32_REFINED && !(flags & GLA_FLAG_REFINE_QL)) ||
+             (precision == GLA_PREC_F32 && (flags & GLA_FLAG_F32_BISECT));
   p->n.assign(n, n + batch);
 
   // ---- descriptors and offsets
@@ -344,7 +345,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     const int nb = (int)n[b];
     if (p->large_ctx.count(nb)) continue;
     LargeCtx* c = nullptr;
-    int rc = large_create(&c, nb, precision == GLA_PREC_F64);
+    int rc = large_create(&c, nb, precision == GLA_PREC_F64, precision == GLA_PREC_F32_REFINED);
     if (rc) {
       gla_plan_destroy(p);
       return rc;
@@ -482,6 +483,9 @@ int plan_stev_batched(gla_plan_s* p, int tcode, const void* din, const void* ein
     const Bucket& bk = p->buckets[b];
     GLA_CUDA(launch_init_tridiagonal(work_t, bk.count, st, p->d_desc, p->d_perm_bucket + bk.start, din, ein, p->d_d,
                                      p->d_e, Q, info, p->d_cst, true));
+    if (p->stein && work_t == kF32)  // the chase passes below then finish only the matrices it leaves
+      GLA_CUDA(launch_stein_tri(bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, p->d_d, p->d_e, Q, w,
+                                p->d_cst, info));
   }
   for (size_t b = 0; b < p->buckets.size(); b++) {
     int rc = run_passes_sync(p, (int)b, work_t, Q, w, info, nullptr, st, 0);
@@ -1188,7 +1192,7 @@ int tune_measure(const TuneKey& k, int count, int base_flags, TuneVal* out) {
 }
 
 int autotune_plan(gla_plan_t p, int base_flags) {
-  const int fam = p->prec == GLA_PREC_F64 ? 0 : (p->stein ? 2 : 1);
+  const int fam = p->prec == GLA_PREC_F64 ? 0 : (p->prec == GLA_PREC_F32_REFINED && p->stein ? 2 : 1);
   const char jz = p->prec == GLA_PREC_F32_REFINED ? 'V' : p->jobz;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   for (Bucket& bk : p->buckets) {

@@ -84,7 +84,10 @@ cudaError_t sytrd_enqueue(SytrdPlan* p, void* A, long long lda, void* d, void* e
 int* sytrd_error_word(SytrdPlan* p);
 
 struct DcPlan;
-int dc_plan_create(DcPlan** out, int n, bool f64);
+// bisect_leaves (FP32 only): the leaves go through the per-eigenvalue solver
+// (GLA_FLAG_F32_BISECT) instead of the QL chase; for the FP32 stage of the
+// FP32 + refinement path, whose refinement absorbs its ~1e-4 orthogonality.
+int dc_plan_create(DcPlan** out, int n, bool f64, bool bisect_leaves = false);
 void dc_plan_destroy(DcPlan* p);
 // Z has leading dimension n; info gets one word per leaf.
 int dc_enqueue(DcPlan* p, void* d, const void* e, void* Z, int* leaf_info, cudaStream_t st);
@@ -101,7 +104,7 @@ int backtr_enqueue(BacktrPlan* p, const void* A, long long lda, const void* tau,
 
 // ---- large-path context: workspace for one order n and one working precision
 struct LargeCtx;
-int large_create(LargeCtx** out, int n, bool f64);
+int large_create(LargeCtx** out, int n, bool f64, bool bisect_leaves = false);
 void large_destroy(LargeCtx* c);
 size_t large_workspace_bytes(const LargeCtx* c);
 // Stage times of the last large_syev (ms): tridiagonalisation (with the

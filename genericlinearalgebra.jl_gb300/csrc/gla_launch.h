@@ -46,6 +46,12 @@ cudaError_t launch_apply(int tcode, int nblocks, int nt, size_t smem, cudaStream
 cudaError_t launch_sort_values(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
                                const void* d, void* w, const int* info, const int* scale_exp);
 
+// SymTridiagonal input on the FP32 stage: the per-eigenvalue solver
+// (small_stein.cuh) for every matrix still running (after
+// launch_init_tridiagonal); solved ones are marked done and applied.
+cudaError_t launch_stein_tri(int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs, const int* perm,
+                             const void* d, const void* e, void* Q, void* w, ChaseState* cst, const int* info);
+
 // Capture-safe executes: info = -2 for matrices whose chase is still running.
 cudaError_t launch_mark_unfinished(int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
                                    const ChaseState* cst, int* info);

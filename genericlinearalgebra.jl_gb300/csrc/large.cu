@@ -122,7 +122,7 @@ __global__ void k_large_store(const T* __restrict__ d, const T* __restrict__ Z, 
 
 }  // namespace
 
-int large_create(LargeCtx** out, int n, bool f64) {
+int large_create(LargeCtx** out, int n, bool f64, bool bisect_leaves) {
   *out = nullptr;
   LargeCtx* c = new (std::nothrow) LargeCtx();
   if (!c) return -1000 - (int)cudaErrorMemoryAllocation;
@@ -131,7 +131,7 @@ int large_create(LargeCtx** out, int n, bool f64) {
   const size_t el = f64 ? 8 : 4;
   cudaError_t err = sytrd_plan_create(&c->sy, n, f64);
   int rc = err == cudaSuccess ? 0 : -1000 - (int)err;
-  if (!rc) rc = dc_plan_create(&c->dc, n, f64);
+  if (!rc) rc = dc_plan_create(&c->dc, n, f64, bisect_leaves);
   if (!rc) rc = backtr_plan_create(&c->bt, n, f64);
   auto alloc = [&](void** p, size_t bytes) {
     if (!rc) {

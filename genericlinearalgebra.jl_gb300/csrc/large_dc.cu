@@ -38,6 +38,7 @@
 #include "gla_large.h"
 #include "gla_launch.h"
 #include "gla_small.cuh"
+#include "../../include/glagpu.h"
 
 namespace gla {
 
@@ -780,7 +781,7 @@ int dc_run(DcPlan& p, T* d, const T* e, T* Z, int* info, cudaStream_t st) {
 
 }  // namespace
 
-int dc_plan_create(DcPlan** out, int n, bool f64) {
+int dc_plan_create(DcPlan** out, int n, bool f64, bool bisect_leaves) {
   *out = nullptr;
   DcPlan* p = new DcPlan();
   p->n = n;
@@ -818,7 +819,8 @@ int dc_plan_create(DcPlan** out, int n, bool f64) {
     leaf_a[b] = aoff;
     aoff += (long long)leaf_m[b] * leaf_m[b];
   }
-  int rc = gla_plan_create(&p->leafplan, f64 ? 0 : 1, 'V', 'L', p->nleaf, lsz.data(), 0.0, 0);
+  int rc = gla_plan_create(&p->leafplan, f64 ? GLA_PREC_F64 : GLA_PREC_F32, 'V', 'L', p->nleaf, lsz.data(), 0.0,
+                           (!f64 && bisect_leaves) ? GLA_FLAG_F32_BISECT : 0);
   if (rc) {
     delete p;
     return rc;

@@ -451,7 +451,8 @@ static int solve_clusters(RefineLarge* r, const std::vector<int>& cs, const std:
     // small clusters come first in coff order; copy them into a contiguous
     // arena otherwise
     gla_plan_t p = nullptr;
-    int rc = gla_plan_create(&p, GLA_PREC_F32, 'V', 'L', (int64_t)small_n.size(), small_n.data(), 0.0, 0);
+    int rc = gla_plan_create(&p, GLA_PREC_F32, 'V', 'L', (int64_t)small_n.size(), small_n.data(), 0.0,
+                             GLA_FLAG_F32_BISECT);
     if (rc) return rc;
     long long aoff = 0, woff = 0;
     float* arena = r->Glo;   // free at this point (Gram blocks consumed)
@@ -490,7 +491,7 @@ static int solve_clusters(RefineLarge* r, const std::vector<int>& cs, const std:
     if (it != r->big.end()) {
       lc = it->second;
     } else {
-      int rc = large_create(&lc, cc[k], false);
+      int rc = large_create(&lc, cc[k], false, true);
       if (rc) return rc;
       r->big[cc[k]] = lc;
     }

@@ -183,6 +183,79 @@ GLA_DEV bool mgs_cluster(int n, float* Y, int ldy, int c0, int c1) {
   return ok;
 }
 
+// The whole solver for one matrix, run by every thread of the CTA (blockDim
+// >= n): dd, ee the diagonal and off-diagonal, e2s, lams (n floats each),
+// Ys (n x ldy), misc (n + 8 ints) and fscr (96 floats) shared scratch.
+// Returns (uniformly) true with the ascending eigenvalues in lams and the
+// orthonormal eigenvectors in the columns of Ys, or false when the matrix is
+// left to the QL chase.
+GLA_DEV bool stein_solve(int n, const float* __restrict__ dd, const float* __restrict__ ee, float* __restrict__ e2s,
+                         float* __restrict__ lams, float* __restrict__ Ys, int ldy, int* __restrict__ misc,
+                         float* __restrict__ fscr) {
+  const int tid = threadIdx.x, NT = blockDim.x;
+  // Gershgorin interval, ||T|| bound, pivmin (LAPACK dstebz's safeguards)
+  float glo = 3.0e38f, ghi = -3.0e38f, e2max = 0.f;
+  for (int i = tid; i < n; i += NT) {
+    const float ai = (i > 0 ? fabsf(ee[i - 1]) : 0.f) + (i + 1 < n ? fabsf(ee[i]) : 0.f);
+    glo = fminf(glo, dd[i] - ai);
+    ghi = fmaxf(ghi, dd[i] + ai);
+    const float e2 = (i + 1 < n) ? ee[i] * ee[i] : 0.f;
+    e2s[i] = e2;
+    e2max = fmaxf(e2max, e2);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+    ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+    e2max = fmaxf(e2max, __shfl_xor_sync(0xffffffffu, e2max, o));
+  }
+  if ((tid & 31) == 0) {
+    fscr[tid >> 5] = glo;
+    fscr[32 + (tid >> 5)] = ghi;
+    fscr[64 + (tid >> 5)] = e2max;
+  }
+  if (tid == 0) misc[0] = 0;
+  __syncthreads();
+  for (int w = 0; w < (NT >> 5); w++) {
+    glo = fminf(glo, fscr[w]);
+    ghi = fmaxf(ghi, fscr[32 + w]);
+    e2max = fmaxf(e2max, fscr[64 + w]);
+  }
+  const float tnorm = fmaxf(fabsf(glo), fabsf(ghi));
+  const float pivmin = 0x1p-100f * fmaxf(1.f, e2max);
+  const float widen = 2.f * (float)n * prec<float>::eps * tnorm + 2.f * pivmin;
+  glo -= widen;
+  ghi += widen;
+  const float atol = 2.f * prec<float>::eps * tnorm + 4.f * pivmin;
+  if (tid < n) lams[tid] = eig_bisect(n, dd, e2s, tid, glo, ghi, atol, pivmin);
+  __syncthreads();
+  // strict: a zero gap is tight even when ||T|| = 0
+  if (tid + 1 < n && !(lams[tid + 1] - lams[tid] > kTightGap * tnorm)) misc[0] = 1;
+  __syncthreads();
+  if (misc[0] != 0) return false;
+  if (tid < n && !twisted_vector(n, dd, ee, e2s, lams[tid], pivmin, Ys, ldy, tid)) misc[0] = 1;
+  if (tid == 0) {  // clusters of two or more eigenvalues within kLooseGap ||T||
+    int nc = 0, s0 = 0;
+    for (int k = 1; k <= n; k++) {
+      if (k == n || lams[k] - lams[k - 1] > kLooseGap * tnorm) {
+        if (k - s0 >= 2) {
+          misc[2 + 2 * nc] = s0;
+          misc[3 + 2 * nc] = k;
+          nc++;
+        }
+        s0 = k;
+      }
+    }
+    misc[1] = nc;
+  }
+  __syncthreads();
+  const int nc = misc[1];
+  for (int c = tid >> 5; c < nc; c += NT >> 5)
+    if (!mgs_cluster(n, Ys, ldy, misc[2 + 2 * c], misc[3 + 2 * c]) && (tid & 31) == 0) misc[0] = 1;
+  __syncthreads();
+  return misc[0] == 0;
+}
+
 // Shared-memory words the solver needs beyond the tridiagonalisation's own
 // arrays: Y (n x ldy floats), e^2 and the eigenvalues (n floats each), and
 // n + 8 ints (flags, cluster count, cluster bounds).

@@ -16,6 +16,8 @@
 //   rank-2 update: flat index over the trailing lower triangle,
 //   Q formation: dorg2l-style backward accumulation in place of the
 //   reflectors (H_k applied only to the already-formed trailing block).
+#include <algorithm>
+
 #include "gla_launch.h"
 #include "gla_small.cuh"
 #include "small_stein.cuh"
@@ -360,73 +362,8 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
     float* e2s = Ys + (size_t)n * ldy;
     float* lams = e2s + n;
     int* misc = reinterpret_cast<int*>(lams + n);  // [0] give up, [1] clusters, [2 + 2c], [3 + 2c] bounds
-    const float* dd = uu;
-    const float* ee = ww;
-    // Gershgorin interval, ||T|| bound, pivmin (LAPACK dstebz's safeguards)
-    float glo = 3.0e38f, ghi = -3.0e38f, e2max = 0.f;
-    for (int i = tid; i < n; i += NT) {
-      const float ai = (i > 0 ? fabsf(ee[i - 1]) : 0.f) + (i + 1 < n ? fabsf(ee[i]) : 0.f);
-      glo = fminf(glo, dd[i] - ai);
-      ghi = fmaxf(ghi, dd[i] + ai);
-      const float e2 = (i + 1 < n) ? ee[i] * ee[i] : 0.f;
-      e2s[i] = e2;
-      e2max = fmaxf(e2max, e2);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      glo = fminf(glo, __shfl_xor_sync(0xffffffffu, glo, o));
-      ghi = fmaxf(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
-      e2max = fmaxf(e2max, __shfl_xor_sync(0xffffffffu, e2max, o));
-    }
-    // red (32 8-byte slots) holds the per-warp minima and maxima, redm the e^2 maxima
-    float* fred = reinterpret_cast<float*>(red);
-    float* fred2 = reinterpret_cast<float*>(redm);
-    if ((tid & 31) == 0) {
-      fred[tid >> 5] = glo;
-      fred[32 + (tid >> 5)] = ghi;
-      fred2[tid >> 5] = e2max;
-    }
-    if (tid == 0) misc[0] = 0;
-    __syncthreads();
-    for (int w = 0; w < (NT >> 5); w++) {
-      glo = fminf(glo, fred[w]);
-      ghi = fmaxf(ghi, fred[32 + w]);
-      e2max = fmaxf(e2max, fred2[w]);
-    }
-    const float tnorm = fmaxf(fabsf(glo), fabsf(ghi));
-    const float pivmin = 0x1p-100f * fmaxf(1.f, e2max);
-    const float widen = 2.f * (float)n * prec<float>::eps * tnorm + 2.f * pivmin;
-    glo -= widen;
-    ghi += widen;
-    const float atol = 2.f * prec<float>::eps * tnorm + 4.f * pivmin;
-    if (tid < n) lams[tid] = eig_bisect(n, dd, e2s, tid, glo, ghi, atol, pivmin);
-    __syncthreads();
-    // strict: a zero gap is tight even when ||T|| = 0
-    if (tid + 1 < n && !(lams[tid + 1] - lams[tid] > kTightGap * tnorm)) misc[0] = 1;
-    __syncthreads();
-    if (misc[0] == 0) {
-      if (tid < n && !twisted_vector(n, dd, ee, e2s, lams[tid], pivmin, Ys, ldy, tid)) misc[0] = 1;
-      if (tid == 0) {  // clusters of two or more eigenvalues within kLooseGap ||T||
-        int nc = 0, s0 = 0;
-        for (int k = 1; k <= n; k++) {
-          if (k == n || lams[k] - lams[k - 1] > kLooseGap * tnorm) {
-            if (k - s0 >= 2) {
-              misc[2 + 2 * nc] = s0;
-              misc[3 + 2 * nc] = k;
-              nc++;
-            }
-            s0 = k;
-          }
-        }
-        misc[1] = nc;
-      }
-      __syncthreads();
-      const int nc = misc[1];
-      for (int c = tid >> 5; c < nc; c += NT >> 5)
-        if (!mgs_cluster(n, Ys, ldy, misc[2 + 2 * c], misc[3 + 2 * c]) && (tid & 31) == 0) misc[0] = 1;
-      __syncthreads();
-    }
-    if (misc[0] == 0) {
+    // red and redm (64 8-byte slots) are free here: the solver's reduction scratch
+    if (stein_solve(n, uu, ww, e2s, lams, Ys, ldy, misc, reinterpret_cast<float*>(redm))) {
       small_gemm_qy(n, S, ld, Ys, ldy, Qg);
       for (int k = tid; k < n; k += NT) wout[dsc.w_off + k] = sexp ? ldexpf(lams[k], sexp) : lams[k];
       if (tid == 0) {
@@ -448,6 +385,62 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
 }
 
 
+size_t stein_tri_smem_bytes(int n) { return 512 + 4 * (2 * (size_t)n + stein_extra_words(n)); }
+
+// Tridiagonal input on the FP32 stage (the leaves of the divide and conquer
+// of the FP32 + refinement path): the per-eigenvalue solver of
+// small_stein.cuh on (d, e) as the chase would take them, one CTA per
+// matrix (blockDim >= n). A solved matrix gets its ascending eigenvalues in
+// wout and its eigenvectors in Q, and is marked done for the chase and the
+// rotation replay; the others keep Q = I and their "running" chase state.
+__global__ void __launch_bounds__(128) k_stein_tri(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
+                                                   const float* __restrict__ dg_all, const float* __restrict__ eg_all,
+                                                   float* __restrict__ Qout, float* __restrict__ wout,
+                                                   ChaseState* __restrict__ cst, const int* __restrict__ info) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int mid = perm[blockIdx.x];
+  const SmallDesc dsc = descs[mid];
+  const int n = dsc.n, tid = threadIdx.x;
+  if (n < 1 || info[mid] != 0 || cst[mid].status != kChaseRunning) return;
+  float* fscr = reinterpret_cast<float*>(smem_raw);  // 128 floats
+  float* dd = reinterpret_cast<float*>(smem_raw + 512);
+  float* ee = dd + n;
+  const int ldy = stein_ldy(n);
+  float* Ys = ee + n;
+  float* e2s = Ys + (size_t)n * ldy;
+  float* lams = e2s + n;
+  int* misc = reinterpret_cast<int*>(lams + n);
+  for (int i = tid; i < n; i += blockDim.x) {
+    dd[i] = dg_all[dsc.w_off + i];
+    ee[i] = (i + 1 < n) ? eg_all[dsc.w_off + i] : 0.f;
+  }
+  __syncthreads();
+  if (!stein_solve(n, dd, ee, e2s, lams, Ys, ldy, misc, fscr)) return;
+  float* Qg = Qout + dsc.a_off;
+  for (int j = 0; j < n; j++)
+    for (int i = tid; i < n; i += blockDim.x) Qg[(size_t)j * n + i] = Ys[(size_t)i * ldy + j];
+  for (int k = tid; k < n; k += blockDim.x) wout[dsc.w_off + k] = lams[k];
+  if (tid == 0) {
+    ChaseState st;
+    st.bs = n;
+    st.nsweeps = 0;
+    st.nrot = 0;
+    st.nhdr = 0;
+    st.status = kChaseDone;
+    st.applied = 1;
+    cst[mid] = st;
+  }
+}
+
+cudaError_t launch_stein_tri(int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs, const int* perm,
+                             const void* d, const void* e, void* Q, void* w, ChaseState* cst, const int* info) {
+  if (nblocks <= 0) return cudaSuccess;
+  const int nt = std::max(32, (nmax + 31) / 32 * 32);
+  k_stein_tri<<<nblocks, nt, stein_tri_smem_bytes(nmax), st>>>(descs, perm, (const float*)d, (const float*)e,
+                                                               (float*)Q, (float*)w, cst, info);
+  return cudaGetLastError();
+}
+
 template <class T, class Tin, bool Q, bool ST = false> static void set_tri_attr() {
   cudaFuncSetAttribute(k_tridiag<T, Tin, Q, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tridiag_smem_bytes(kSmallMaxN, 256, sizeof(T), ST));
@@ -461,6 +454,9 @@ cudaError_t tridiag_kernels_init() {
   set_tri_attr<float, double, true>();
   set_tri_attr<float, double, false>();
   set_tri_attr<float, double, true, true>();
+  set_tri_attr<float, float, true, true>();
+  cudaFuncSetAttribute(k_stein_tri, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)stein_tri_smem_bytes(kSmallMaxN));
   return cudaGetLastError();
 }
 
@@ -475,7 +471,8 @@ cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t sm
     if (wantq) GLA_TRI(double, double, true, false);
     else GLA_TRI(double, double, false, false);
   } else if (tcode == kF32) {
-    if (wantq) GLA_TRI(float, float, true, false);
+    if (wantq && stein) GLA_TRI(float, float, true, true);
+    else if (wantq) GLA_TRI(float, float, true, false);
     else GLA_TRI(float, float, false, false);
   } else {
     if (wantq && stein) GLA_TRI(float, double, true, true);

@@ -104,11 +104,12 @@ class Plan:
     Arena layout: matrix b is column-major n_b x n_b at offset sum(n_c^2, c<b);
     its eigenvalues at sum(n_c, c<b). precision: "f64", "f32", "f32_refined".
     refine_ql: for "f32_refined", run the FP32 stage with the QL chase instead
-    of the per-eigenvalue solver (GLA_FLAG_REFINE_QL).
+    of the per-eigenvalue solver (GLA_FLAG_REFINE_QL). bisect: for "f32", use
+    that per-eigenvalue solver instead of the QL chase (GLA_FLAG_F32_BISECT).
     """
 
     def __init__(self, ns, precision="f64", jobz="V", uplo="L", tol=None, alg="QL", small_log=False,
-                 timing=False, graph=False, autotune=False, refine_ql=False):
+                 timing=False, graph=False, autotune=False, refine_ql=False, bisect=False):
         L = _lib.load()
         ns = np.ascontiguousarray(np.asarray(ns, dtype=np.int64))
         if (ns < 0).any() or (ns > GLA_MAX_N).any():
@@ -120,7 +121,8 @@ class Plan:
         self.dtype = np.float32 if precision == "f32" else np.float64
         flags = (GLA_ALG_QR if alg == "QR" else GLA_ALG_QL) | (_lib.GLA_FLAG_SMALL_LOG if small_log else 0) | \
             (_lib.GLA_FLAG_TIMING if timing else 0) | (_lib.GLA_FLAG_GRAPH if graph else 0) | \
-            (_lib.GLA_FLAG_AUTOTUNE if autotune else 0) | (_lib.GLA_FLAG_REFINE_QL if refine_ql else 0)
+            (_lib.GLA_FLAG_AUTOTUNE if autotune else 0) | (_lib.GLA_FLAG_REFINE_QL if refine_ql else 0) | \
+            (_lib.GLA_FLAG_F32_BISECT if bisect else 0)
         self.graph = graph
         h = C.c_void_p()
         _lib.check(L.gla_plan_create(C.byref(h), PRECISIONS[precision], jobz.encode(), uplo.encode(), len(ns),

@@ -25,6 +25,7 @@ GLA_FLAG_TIMING = 8
 GLA_FLAG_GRAPH = 16
 GLA_FLAG_AUTOTUNE = 32
 GLA_FLAG_REFINE_QL = 64
+GLA_FLAG_F32_BISECT = 128
 PHASES = ("tridiag", "chase", "apply", "refine")
 COUNTERS = ("rotations", "sweeps", "row_rotations", "refine_n3", "passes")
 

@@ -75,6 +75,14 @@ extern "C" {
  * the QL chase only for matrices whose eigenvalues come within 1e-6 ||T||
  * of each other). Both feed the same refinement. */
 #define GLA_FLAG_REFINE_QL 64
+/* Flag bit (GLA_PREC_F32, orders <= 128): solve with that per-eigenvalue
+ * solver instead of the QL chase (matrices with eigenvalues within
+ * 1e-6 ||T|| of each other still take the chase). Eigenvalues as accurate
+ * as the chase's; eigenvectors orthogonal to about 1e-4 (eps(Float32)
+ * ||T|| over the smallest gap outside its Gram-Schmidt clusters) instead of
+ * n eps(Float32). The FP32 + refinement path uses it for its internal FP32
+ * solves (cluster matrices, divide-and-conquer leaves). */
+#define GLA_FLAG_F32_BISECT 128
 
 /* Phases reported by gla_plan_phase_times. */
 #define GLA_PHASE_TRIDIAG 0 /* symtri! + Array(Q)          */

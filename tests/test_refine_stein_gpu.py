@@ -123,3 +123,36 @@ def test_prescribed_gapped_and_scaled(G):
     assert (info == 0).all()
     for A, lam, w, V in zip(mats, lams, ws, Vs):
         check(A, w, V, wo=lam)
+
+
+def test_f32_plans_with_the_bisection_flag(G):
+    # GLA_FLAG_F32_BISECT on plain FP32 plans (the refined path's internal FP32
+    # solves): eigenvalues as accurate as the QL chase's (8 n eps32 ||A||),
+    # residual <= 32 n eps32, orthogonality <= 1e-3 (pairs just outside the
+    # Gram-Schmidt bound of 1e-3 ||T|| are orthogonal to eps32 ||T|| / gap,
+    # about 1e-4; the refinement absorbs it); hard matrices go to the chase
+    eps32 = 2.0 ** -23
+    rng = np.random.default_rng(44)
+    sizes = list(rng.integers(1, 129, size=60))
+    mats = [goe(int(n), 7300 + i) for i, n in enumerate(sizes)] + hard_matrices()
+    plan = G.Plan([m.shape[0] for m in mats], precision="f32", bisect=True)
+    w = np.empty(max(plan.w_elems, 1), np.float32)
+    V = np.empty(max(plan.a_elems, 1), np.float32)
+    info = np.zeros(len(mats), dtype=np.int32)
+    plan.execute_host(plan.pack(mats), w, V, info)
+    ws, Vs = plan.unpack(w, V)
+    st = plan.stats()
+    plan.close()
+    assert (info == 0).all()
+    assert st["rotations"] > 0  # the hard matrices
+    for A, wg, Vg in zip(mats, ws, Vs):
+        n = A.shape[0]
+        A32 = A.astype(np.float32).astype(np.float64)
+        wo = O.syev(A32, "V")[0]
+        nA = max(np.linalg.norm(A32, 2), 1e-30)
+        wg = wg.astype(np.float64)
+        Vg = Vg.astype(np.float64)
+        assert np.all(np.diff(wg) >= 0)
+        assert np.abs(wg - wo).max() <= 8 * n * eps32 * nA
+        assert residual(A32, Vg, wg) <= 32 * n * eps32
+        assert orth(Vg) <= 1e-3
