@@ -123,6 +123,7 @@ struct gla_plan_s {
   void* d_w32 = nullptr;
   RefineWork rw;          // refinement scratch
   void* d_vtmp = nullptr; // V target when the caller passes none
+  void* d_qtmp = nullptr; // stein: Q of every matrix (float arena) while its tridiagonal is solved
   // host-execute buffers
   void* h_A = nullptr;
   void* h_w = nullptr;
@@ -305,6 +306,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   const size_t o_x32 = carve(refined ? 4 * aoff : 0);
   const size_t o_w32 = carve(refined ? 4 * woff : 0);
   const size_t o_vtmp = carve((jobz == 'N' && refined) ? 8 * aoff : 0);
+  const size_t o_qtmp = carve(p->stein ? 4 * aoff : 0);
   size_t refine_bytes = refined ? refine_workspace_bytes(aoff, woff, batch) : 0;
   const size_t o_ref = carve(refine_bytes);
   p->ws_bytes = off;
@@ -327,6 +329,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->d_x32 = refined ? (void*)(w + o_x32) : nullptr;
   p->d_w32 = refined ? (void*)(w + o_w32) : nullptr;
   p->d_vtmp = (jobz == 'N' && refined) ? (void*)(w + o_vtmp) : nullptr;
+  p->d_qtmp = p->stein ? (void*)(w + o_qtmp) : nullptr;
   if (refined) refine_carve(&p->rw, w + o_ref, aoff, woff, batch);
   if (batch) err = cudaMemcpy(p->d_desc, desc.data(), sizeof(SmallDesc) * batch, cudaMemcpyHostToDevice);
   if (err == cudaSuccess && !perm_bucket.empty())
@@ -589,7 +592,7 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
     p->mark(b, GLA_PHASE_TRIDIAG, 0, s);
     GLA_CUDA(launch_tridiag(tc, wantq, bk.count, bk.nt_tri, tridiag_smem_bytes(bk.nmax, bk.nt_tri, el, p->stein), s,
                             p->d_desc, p->d_perm_bucket + bk.start, A, lower, p->d_d, p->d_e, Q, info, p->d_cst,
-                            p->d_scale, p->stein, wq));
+                            p->d_scale, p->stein, wq, p->d_qtmp));
     p->mark(b, GLA_PHASE_TRIDIAG, 1, s);
     if (wantq) {
       const int npass = p->graph ? kGraphPasses : kAsyncPasses;

@@ -26,13 +26,14 @@ size_t apply_smem_bytes(int n, int elem);
 // Raise the dynamic shared-memory limit of every kernel instantiation once.
 cudaError_t small_kernels_init();
 
-// stein (kF32FromF64 with Q only): the CTA also solves the tridiagonal
+// stein (FP32 work type with Q only): the CTA also solves the tridiagonal
 // (bisection + twisted factorisation) and writes X = Q Y and the eigenvalues
-// (to w) for every matrix it does not leave to the QL chase.
+// (to w) for every matrix it does not leave to the QL chase; qtmp: a float
+// scratch arena of the plan's a_elems entries.
 cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
                            const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
                            void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein = false,
-                           void* w = nullptr);
+                           void* w = nullptr, void* qtmp = nullptr);
 
 cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,

@@ -64,18 +64,17 @@ GLA_DEV void block_sum_max(T v, unsigned long long m, T* red, unsigned long long
 // (stride ld across the lanes of a warp) spread over all shared-memory banks.
 GLA_DEV int stage_ld(int n) { return (n + 1) | 1; }
 
-size_t tridiag_smem_bytes(int n, int nt, int elem, bool stein) {
+size_t tridiag_smem_bytes(int n, int nt, int elem, bool) {
   // redm[32] u64 | red[32] (8-byte slots) | S[n*ld] | vv,uu,ww,taus [n] | part[8*nt]
-  // [| the FP32 tridiagonal solver's arrays (stein, float only)]
+  // (the FP32 tridiagonal solver reuses S and part once Q is in global memory)
   const size_t ld = (size_t)((n + 1) | 1);
-  return 512 + (size_t)elem * ((size_t)n * ld + 4 * (size_t)n + 8 * (size_t)nt) +
-         (stein ? 4 * stein_extra_words(n) : 0);
+  return 512 + (size_t)elem * ((size_t)n * ld + 4 * (size_t)n + 8 * (size_t)nt);
 }
 
-// X = Q Y (n x n, Q column-major in S with leading dimension ld, Y row-major
-// in Ys with leading dimension ldy), stored column-major to Xg. Thread
-// tiles of 8 x 8 outputs with rows and columns strided by ceil(n/8), so that
-// the threads of a warp read consecutive (or identical) shared words.
+// X = Q Y (n x n, Q column-major with leading dimension ld, Y row-major in
+// Ys with leading dimension ldy), stored column-major to Xg. Thread tiles of
+// 8 x 8 outputs with rows and columns strided by ceil(n/8), so that the
+// threads of a warp read consecutive (or identical) words.
 GLA_DEV void small_gemm_qy(int n, const float* __restrict__ S, int ld, const float* __restrict__ Ys, int ldy,
                            float* __restrict__ Xg) {
   const int nt8 = (n + 7) >> 3;
@@ -113,16 +112,18 @@ GLA_DEV void small_gemm_qy(int n, const float* __restrict__ S, int ld, const flo
   }
 }
 
-// STEIN (float only, FP32 + refinement path): after forming Q, solve the
-// tridiagonal in the same CTA (small_stein.cuh) and write X = Q Y and the
-// ascending eigenvalues (times 2^scale) to wout, marking the matrix done for
-// the chase; a matrix the solver leaves to the QL chase gets Q as usual.
+// STEIN (float only): after forming Q, solve the tridiagonal in the same CTA
+// (small_stein.cuh) and write X = Q Y and the ascending eigenvalues (times
+// 2^scale) to wout, marking the matrix done for the chase; a matrix the
+// solver leaves to the QL chase gets Q as usual. Q goes to qtmp (an n x n
+// float scratch per matrix, arena layout) first, so that the solver's
+// arrays reuse the shared memory of the reduction.
 template <class T, class Tin, bool WANTQ, bool STEIN>
 __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                  const Tin* __restrict__ A, int lower, T* __restrict__ dout,
                                                  T* __restrict__ eout, T* __restrict__ Qout, int* __restrict__ info,
                                                  ChaseState* __restrict__ cst, int* __restrict__ scale_exp,
-                                                 T* __restrict__ wout) {
+                                                 T* __restrict__ wout, T* __restrict__ qtmp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int mid = perm[blockIdx.x];
   const SmallDesc dsc = descs[mid];
@@ -357,14 +358,20 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
   __syncthreads();
   T* Qg = Qout + dsc.a_off;
   if constexpr (STEIN) {
-    const int ldy = stein_ldy(n);
-    float* Ys = part + 8 * NT;
-    float* e2s = Ys + (size_t)n * ldy;
+    float* Qt = qtmp + dsc.a_off;
+    for (int j = 0; j < n; j++)
+      for (int i = tid; i < n; i += NT) Qt[(size_t)j * n + i] = S[(size_t)j * ld + i];
+    __syncthreads();
+    // Y over S (leading dimension ld), e^2, eigenvalues and flags over part
+    // (8 NT >= 3 n + 8 words), d and e stay in uu and ww
+    float* Ys = S;
+    float* e2s = part;
     float* lams = e2s + n;
     int* misc = reinterpret_cast<int*>(lams + n);  // [0] give up, [1] clusters, [2 + 2c], [3 + 2c] bounds
     // red and redm (64 8-byte slots) are free here: the solver's reduction scratch
-    if (stein_solve(n, uu, ww, e2s, lams, Ys, ldy, misc, reinterpret_cast<float*>(redm))) {
-      small_gemm_qy(n, S, ld, Ys, ldy, Qg);
+    const bool solved = stein_solve(n, uu, ww, e2s, lams, Ys, ld, misc, reinterpret_cast<float*>(redm));
+    if (solved) {
+      small_gemm_qy(n, Qt, n, Ys, ld, Qg);
       for (int k = tid; k < n; k += NT) wout[dsc.w_off + k] = sexp ? ldexpf(lams[k], sexp) : lams[k];
       if (tid == 0) {
         ChaseState st;
@@ -378,7 +385,10 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
       }
       return;
     }
-    // left to the QL chase: Q below, the chase state stays "running"
+    // left to the QL chase: Q, the chase state stays "running"
+    for (int j = 0; j < n; j++)
+      for (int i = tid; i < n; i += NT) Qg[(size_t)j * n + i] = Qt[(size_t)j * n + i];
+    return;
   }
   for (int j = 0; j < n; j++)
     for (int i = tid; i < n; i += NT) Qg[(size_t)j * n + i] = S[(size_t)j * ld + i];
@@ -462,11 +472,12 @@ cudaError_t tridiag_kernels_init() {
 
 cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
                            const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
-                           void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein, void* w) {
+                           void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein, void* w,
+                           void* qtmp) {
   if (nblocks <= 0) return cudaSuccess;
 #define GLA_TRI(T, Tin, WQ, ST)                                                                                 \
   k_tridiag<T, Tin, WQ, ST><<<nblocks, nt, smem, st>>>(descs, perm, (const Tin*)A, lower, (T*)d, (T*)e, (T*)Q, \
-                                                       info, cst, scale_exp, (T*)w)
+                                                       info, cst, scale_exp, (T*)w, (T*)qtmp)
   if (tcode == kF64) {
     if (wantq) GLA_TRI(double, double, true, false);
     else GLA_TRI(double, double, false, false);

@@ -113,15 +113,19 @@ def test_lapack_side_baseline_child():
     assert out["kind"] == "lapack" and out["value"] > 0 and out["cores"] >= 1
 
 
-def test_chase_roofline_figures():
-    # the launch list's top kernel of the batched step is reported with its
-    # algorithmic work (16 operations per applied rotation) over its time
+def test_roofline_figures():
+    # the launch list's top kernels of the batched refined step are reported
+    # with their algorithmic work over their time
     import bench
-    r = bench.chase_roofline({"rotations": 1_000_000}, 2.0, 35.0, "FP32")
-    assert r["kernel"] == "k_chase" and r["bound"] == "latency" and r["unit"] == "T FP32 ops/s"
-    assert abs(r["achieved"] - 16e6 / 2e-3 / 1e12) < 1e-15
-    assert abs(r["frac"] - r["achieved"] / 35.0) < 1e-18 and r["traffic"] is None
-    assert bench.chase_roofline({"rotations": 5}, 0.0, None, "FP64")["frac"] is None
+    r = bench.refine_roofline(7.0, 35.0, 4096)
+    assert r["kernel"] == "k_refine" and r["unit"] == "T FP32 ops/s"
+    assert abs(r["frac"] - 0.2) < 1e-12
+    assert abs(r["traffic"] - 4 * bench.REFINE_DRAM_BYTES_PER_1024) < 1.0
+    assert bench.refine_roofline(7.0, None, 4096)["frac"] is None
+    import numpy as np
+    t = bench.tridiag_roofline(np.array([128, 64]), 2.0, 35.0)
+    flops = (4 / 3 + 4 / 3 + 2) * (128 ** 3 + 64 ** 3)
+    assert abs(t["achieved"] - flops / 2e-3 / 1e12) < 1e-12 and t["peak"] == 70.0
 
 
 def test_launch_counts():
