@@ -78,7 +78,8 @@ cudaError_t large_adjoint(int n, const double* w, const double* V, long long ldv
 
 // ---- stage plans (one order, one working precision)
 struct SytrdPlan;
-cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64);
+// tc (FP32 only): trailing updates on the tensor cores (3xTF32, tc_gemm.cuh).
+cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64, bool tc = false);
 void sytrd_plan_destroy(SytrdPlan* p);
 cudaError_t sytrd_enqueue(SytrdPlan* p, void* A, long long lda, void* d, void* e, void* tau, cudaStream_t st);
 int* sytrd_error_word(SytrdPlan* p);
@@ -96,15 +97,24 @@ int dc_leaf_count(const DcPlan* p);
 size_t dc_plan_bytes(const DcPlan* p);
 
 struct BacktrPlan;
-int backtr_plan_create(BacktrPlan** out, int n, bool f64);
+// tc (FP32 only): both GEMMs of every block on the tensor cores (3xTF32).
+int backtr_plan_create(BacktrPlan** out, int n, bool f64, bool tc = false);
 void backtr_plan_destroy(BacktrPlan* p);
+// Error word the back-transformation's tensor-core GEMMs set when a bounded
+// wait runs out (the large context passes its reduction's word).
+void backtr_set_error_word(BacktrPlan* p, int* err);
 // Z := Q Z, or Q' Z when trans, for Z of ncol columns (-1: n).
 int backtr_enqueue(BacktrPlan* p, const void* A, long long lda, const void* tau, void* Z, long long ldz,
                    cudaStream_t st, int ncol = -1, bool trans = false);
 
 // ---- large-path context: workspace for one order n and one working precision
 struct LargeCtx;
-int large_create(LargeCtx** out, int n, bool f64, bool bisect_leaves = false);
+// refine_stage (FP32 only): the context solves the FP32 stage of the FP32 +
+// refinement path, whose refinement absorbs errors of ~1e-4: its
+// divide-and-conquer leaves go through the per-eigenvalue solver and its
+// trailing updates and back-transformation through the 3xTF32 tensor-core
+// GEMM. Plain FP32 solves keep the QL leaves and the FP32 SIMT GEMMs.
+int large_create(LargeCtx** out, int n, bool f64, bool refine_stage = false);
 void large_destroy(LargeCtx* c);
 size_t large_workspace_bytes(const LargeCtx* c);
 // Stage times of the last large_syev (ms): tridiagonalisation (with the

@@ -122,17 +122,18 @@ __global__ void k_large_store(const T* __restrict__ d, const T* __restrict__ Z, 
 
 }  // namespace
 
-int large_create(LargeCtx** out, int n, bool f64, bool bisect_leaves) {
+int large_create(LargeCtx** out, int n, bool f64, bool refine_stage) {
   *out = nullptr;
   LargeCtx* c = new (std::nothrow) LargeCtx();
   if (!c) return -1000 - (int)cudaErrorMemoryAllocation;
   c->n = n;
   c->f64 = f64;
   const size_t el = f64 ? 8 : 4;
-  cudaError_t err = sytrd_plan_create(&c->sy, n, f64);
+  cudaError_t err = sytrd_plan_create(&c->sy, n, f64, !f64 && refine_stage);
   int rc = err == cudaSuccess ? 0 : -1000 - (int)err;
-  if (!rc) rc = dc_plan_create(&c->dc, n, f64, bisect_leaves);
-  if (!rc) rc = backtr_plan_create(&c->bt, n, f64);
+  if (!rc) rc = dc_plan_create(&c->dc, n, f64, refine_stage);
+  if (!rc) rc = backtr_plan_create(&c->bt, n, f64, !f64 && refine_stage);
+  if (!rc) backtr_set_error_word(c->bt, sytrd_error_word(c->sy));
   auto alloc = [&](void** p, size_t bytes) {
     if (!rc) {
       cudaError_t e2 = cudaMalloc(p, std::max<size_t>(bytes, 16));

@@ -14,14 +14,17 @@
 
 #include "gla_common.cuh"
 #include "gla_large.h"
+#include "tc_gemm.cuh"
 
 namespace gla {
 
 constexpr int kBT = kBacktrNB;
 
 // Y (n x n): column j is reflector j with its unit element and zeros above.
+// Y (and, when Yt is given, its transpose: the K-major operand of the
+// tensor-core Z -= Y W2) from the reflectors stored below the subdiagonal.
 template <class T>
-__global__ void k_form_y(const T* __restrict__ A, long long lda, T* __restrict__ Y, int n) {
+__global__ void k_form_y(const T* __restrict__ A, long long lda, T* __restrict__ Y, int n, T* __restrict__ Yt) {
   const int j = blockIdx.y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     T v;
@@ -32,6 +35,7 @@ __global__ void k_form_y(const T* __restrict__ A, long long lda, T* __restrict__
     else
       v = A[i + (long long)j * lda];
     Y[i + (long long)j * n] = v;
+    if (Yt) Yt[j + (long long)i * n] = v;
   }
 }
 
@@ -119,7 +123,7 @@ __global__ void __launch_bounds__(256) k_tw(const T* __restrict__ Wp, int splits
       for (int q = 0; q <= i; q++) s = fma(Ts[q][i], ws[q][c], s);
     else
       for (int q = i; q < kb; q++) s = fma(Ts[i][q], ws[q][c], s);
-    W2[i + (long long)(c0 + c) * kb] = s;
+    W2[i + (long long)(c0 + c) * kBT] = s;
   }
 }
 
@@ -131,10 +135,14 @@ struct BacktrPlan {
   void* Y = nullptr;
   void* Tm = nullptr;
   void* Wp = nullptr;
-  void* W2 = nullptr;
+  void* W2 = nullptr;   // T W, kBT x n (leading dimension kBT)
+  float* Yt = nullptr;  // FP32 with tensor cores: Y transposed
+  int* err = nullptr;   // error word of the tensor-core GEMMs (set by backtr_set_error_word)
 };
 
-int backtr_plan_create(BacktrPlan** out, int n, bool f64) {
+void backtr_set_error_word(BacktrPlan* p, int* err) { p->err = err; }
+
+int backtr_plan_create(BacktrPlan** out, int n, bool f64, bool tc) {
   *out = nullptr;
   BacktrPlan* p = new BacktrPlan();
   p->n = n;
@@ -152,6 +160,7 @@ int backtr_plan_create(BacktrPlan** out, int n, bool f64) {
   alloc(&p->Tm, el * (size_t)p->nblk * kBT * kBT);
   alloc(&p->Wp, el * (size_t)p->splits * kBT * n);
   alloc(&p->W2, el * (size_t)kBT * n);
+  if (!f64 && tc && n % 4 == 0 && tc::tc_available()) alloc((void**)&p->Yt, sizeof(float) * (size_t)n * n);
   if (err == cudaSuccess)
     err = f64 ? cudaFuncSetAttribute((const void*)k_larft<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)larft_smem_bytes<double>())
@@ -171,6 +180,7 @@ void backtr_plan_destroy(BacktrPlan* p) {
   cudaFree(p->Tm);
   cudaFree(p->Wp);
   cudaFree(p->W2);
+  cudaFree(p->Yt);
   delete p;
 }
 
@@ -184,7 +194,13 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Zall, 
   const int n = p.n;
   if (n < 2 || ncol <= 0) return 0;
   T* Y = (T*)p.Y;
-  k_form_y<T><<<dim3((n + 255) / 256, n), 256, 0, st>>>(A, lda, Y, n);
+  // FP32 with tensor cores: both GEMMs of a block on tcgen05 (3xTF32) when
+  // the tensor maps of Y, Y' and Z can be built (16-byte-aligned columns)
+  CUtensorMap mY, mYt;
+  const bool tc = sizeof(T) == 4 && p.Yt && p.err && (ldz % 4) == 0 && ((uintptr_t)Zall & 15) == 0 &&
+                  tc::tc_make_map(&mY, (const float*)Y, n, n, n, tc::kBM) &&
+                  tc::tc_make_map(&mYt, p.Yt, n, n, n, tc::kBM);
+  k_form_y<T><<<dim3((n + 255) / 256, n), 256, 0, st>>>(A, lda, Y, n, tc ? (T*)p.Yt : (T*)nullptr);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return -1000 - (int)err;
   k_larft<T><<<p.nblk, 256, larft_smem_bytes<T>(), st>>>(Y, tau, (T*)p.Tm, n);
@@ -194,6 +210,8 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Zall, 
   for (int c0 = 0; c0 < ncol; c0 += n) {
   const int nc = std::min(n, ncol - c0);
   T* Z = Zall + (long long)c0 * ldz;
+  CUtensorMap mZ;
+  const bool tcz = tc && tc::tc_make_map(&mZ, (const float*)Z, n, nc, ldz, tc::kBN);
   for (int bi = 0; bi < p.nblk; bi++) {
     const int b = trans ? bi : p.nblk - 1 - bi;
     const int j0 = b * kBT, kb = std::min(kBT, n - 1 - j0);
@@ -202,6 +220,54 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Zall, 
     // column segments aligned for vector access
     const int r0 = (j0 + 1) & ~(16 / (int)sizeof(T) - 1);
     const int mrows = n - r0;
+    if (tcz) {
+      // W = Y_b' Z[r0:, :]: A operand rows = columns j0.. of Y (K = rows of
+      // Y), B operand = columns of Z; split K as the SIMT path does
+      int splits = std::max(1, std::min(p.splits, mrows / (4 * tc::kBK)));
+      const int ks = ((mrows + splits - 1) / splits + tc::kBK - 1) / tc::kBK * tc::kBK;
+      splits = (mrows + ks - 1) / ks;
+      tc::TcArgs g{};
+      g.M = kb;
+      g.N = nc;
+      g.nseg = 1;
+      g.K[0] = mrows;
+      g.a_x[0] = r0;
+      g.b_x[0] = r0;
+      g.a_y = j0;
+      g.b_y = 0;
+      g.ksplit = splits > 1 ? ks : 0;
+      g.split_stride = (long long)kb * n;
+      g.D = (float*)p.Wp;
+      g.ldd = kb;
+      g.alpha = 1.f;
+      g.beta = 0.f;
+      g.err = p.err;
+      if ((err = tc::tc_gemm_launch(mY, mZ, g, splits, st)) != cudaSuccess) return -1000 - (int)err;
+      k_tw<T><<<(nc + 15) / 16, 256, 0, st>>>((const T*)p.Wp, splits, (long long)kb * n,
+                                              (const T*)p.Tm + (long long)b * kBT * kBT, (T*)p.W2, kb, nc,
+                                              trans ? 1 : 0);
+      if ((err = cudaGetLastError()) != cudaSuccess) return -1000 - (int)err;
+      // Z[r0:, :] -= Y_b W2: A operand rows = rows r0.. of Y (K-major through
+      // Y'), B operand = W2 (K = the block's kb reflectors)
+      CUtensorMap mW2;
+      if (!tc::tc_make_map(&mW2, (const float*)p.W2, kb, nc, kBT, tc::kBN)) return -1000 - (int)cudaErrorInvalidValue;
+      tc::TcArgs h{};
+      h.M = mrows;
+      h.N = nc;
+      h.nseg = 1;
+      h.K[0] = kb;
+      h.a_x[0] = j0;
+      h.b_x[0] = 0;
+      h.a_y = r0;
+      h.b_y = 0;
+      h.D = (float*)Z + r0;
+      h.ldd = ldz;
+      h.alpha = -1.f;
+      h.beta = 1.f;
+      h.err = p.err;
+      if ((err = tc::tc_gemm_launch(mYt, mW2, h, 1, st)) != cudaSuccess) return -1000 - (int)err;
+      continue;
+    }
     // W = Y_b' Z[r0:, :]
     GemmDesc g{};
     g.m = kb;
@@ -232,7 +298,7 @@ int backtr_run(BacktrPlan& p, const T* A, long long lda, const T* tau, T* Zall, 
     h.A = Y + r0 + (long long)j0 * n;
     h.lda = n;
     h.B = p.W2;
-    h.ldb = kb;
+    h.ldb = kBT;
     h.C = Z + r0;
     h.ldc = ldz;
     h.alpha = -1.0;

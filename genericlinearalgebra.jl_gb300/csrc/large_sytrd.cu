@@ -31,6 +31,7 @@
 
 #include "gla_common.cuh"
 #include "gla_large.h"
+#include "tc_gemm.cuh"
 
 namespace gla {
 
@@ -419,16 +420,70 @@ struct SytrdPlan {
   void* qfp = nullptr;
   void* dots = nullptr;
   void* VW = nullptr;     // [V | W] panel buffer, n x 2 kSytrdNB
+  float* VWt = nullptr;   // FP32: [V | W] transposed (2 kSytrdNB x n), the tensor-core update's K-major operand
   int* bkidx = nullptr;   // SYR2K k remaps: [2 nb] for nbp = kSytrdNB, then for the last panel
   unsigned* bar = nullptr;
   int* err = nullptr;
   bool f64 = true;
 };
 
+// [V | W] of a panel with nbp reflectors (V at VW, W at VW + nbp n, rows
+// t.. of interest) into VWt: row kk < 32 = V column kk, row 32 + kk = W
+// column kk (zero for kk >= nbp), column i = row i.
+__global__ void k_vw_transpose(const float* __restrict__ VW, int n, int nbp, int t, float* __restrict__ VWt) {
+  __shared__ float tile[32][65];
+  const int i0 = t + blockIdx.x * 32;
+  for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
+    const int ii = idx % 32, kk = idx / 32;
+    const int i = i0 + ii;
+    const int c = kk < 32 ? kk : kk - 32;
+    float v = 0.f;
+    if (i < n && c < nbp) v = VW[i + (long long)(kk < 32 ? c : nbp + c) * n];
+    tile[ii][kk] = v;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 32 * 64; idx += blockDim.x) {
+    const int kk = idx % 64, ii = idx / 64;
+    const int i = i0 + ii;
+    if (i < n) VWt[kk + (long long)i * 64] = tile[ii][kk];
+  }
+}
+
 }  // namespace gla
 
 namespace {
 using namespace gla;
+
+// The trailing update A[t:, t:] -= V W' + W V' (lower tiles) as two K
+// segments of the 3xTF32 tensor-core GEMM: A operand rows = V / W rows
+// (K-major through VWt), B operand columns = W / V rows. False when the
+// shapes do not allow the tensor maps (the SIMT GEMM then runs).
+bool sytrd_update_tc(SytrdPlan& sp, float* A, long long lda, int n, int t, int nbp, cudaStream_t st,
+                     cudaError_t* err) {
+  *err = cudaSuccess;
+  if (sp.VWt == nullptr || kSytrdNB != 32) return false;
+  CUtensorMap m;
+  if (!tc::tc_make_map(&m, sp.VWt, 64, n, 64, tc::kBM)) return false;
+  k_vw_transpose<<<(n - t + 31) / 32, 256, 0, st>>>((const float*)sp.VW, n, nbp, t, sp.VWt);
+  if ((*err = cudaGetLastError()) != cudaSuccess) return true;
+  tc::TcArgs g{};
+  g.M = g.N = n - t;
+  g.nseg = 2;
+  g.K[0] = g.K[1] = 32;
+  g.a_x[0] = 0;   // V
+  g.b_x[0] = 32;  // W
+  g.a_x[1] = 32;  // W
+  g.b_x[1] = 0;   // V
+  g.a_y = g.b_y = t;
+  g.D = A + t + (long long)t * lda;
+  g.ldd = lda;
+  g.alpha = -1.f;
+  g.beta = 1.f;
+  g.lower = 1;
+  g.err = sp.err;
+  *err = tc::tc_gemm_launch(m, m, g, 1, st);
+  return true;
+}
 
 template <class T>
 cudaError_t sytrd_run(SytrdPlan& sp, T* A, long long lda, T* d, T* e, T* tau, cudaStream_t st) {
@@ -470,6 +525,10 @@ cudaError_t sytrd_run(SytrdPlan& sp, T* A, long long lda, T* d, T* e, T* tau, cu
     if (err != cudaSuccess) return err;
     const int t = k0 + nbp;
     if (t < n - 1) {  // trailing update A[t:, t:] -= V W' + W V' (lower tiles)
+      if (sizeof(T) == 4 && sytrd_update_tc(sp, (float*)A, lda, n, t, nbp, st, &err)) {
+        if (err != cudaSuccess) return err;
+        continue;
+      }
       GemmDesc g{};
       g.m = n - t;
       g.n = n - t;
@@ -494,7 +553,7 @@ cudaError_t sytrd_run(SytrdPlan& sp, T* A, long long lda, T* d, T* e, T* tau, cu
 
 namespace gla {
 
-cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64) {
+cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64, bool tc) {
   *out = nullptr;
   SytrdPlan* sp = new SytrdPlan();
   sp->n = n;
@@ -543,6 +602,7 @@ cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64) {
     err = cudaMemcpy(sp->ustart, ustart.data(), sizeof(int) * ustart.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMemcpy(sp->bkidx, bk.data(), sizeof(int) * bk.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMemset(sp->VW, 0, el * (size_t)n * 2 * kSytrdNB);
+  if (err == cudaSuccess && !f64 && tc && tc::tc_available()) alloc((void**)&sp->VWt, sizeof(float) * 64 * (size_t)n);
   if (err != cudaSuccess) {
     sytrd_plan_destroy(sp);
     return err;
@@ -560,6 +620,7 @@ void sytrd_plan_destroy(SytrdPlan* sp) {
   cudaFree(sp->qfp);
   cudaFree(sp->dots);
   cudaFree(sp->VW);
+  cudaFree(sp->VWt);
   cudaFree(sp->bkidx);
   cudaFree(sp->bar);
   cudaFree(sp->err);

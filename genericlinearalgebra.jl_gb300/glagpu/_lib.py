@@ -73,6 +73,7 @@ SIGNATURES = {
     "gla_dstev": ([_ch, _i64, _vp, _vp, _vp, _i64, _int, C.POINTER(_int), _vp], _int),
     "gla_dsyev_static": ([_ch, _ch, _i64, _vp, _i64, _vp, C.POINTER(_int), _vp], _int),
     "gla_release_workspaces": ([], _int),
+    "gla_sgemm_3xtf32": ([_i64, _i64, _i64, C.c_float, _vp, _i64, _vp, _i64, C.c_float, _vp, _i64, _vp], _int),
 }
 
 _lib = None

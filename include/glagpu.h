@@ -209,6 +209,21 @@ int gla_dsyev(char jobz, char uplo, int64_t n, double* A, int64_t lda, double* w
 int gla_ssyev(char jobz, char uplo, int64_t n, float* A, int64_t lda, float* w, int* info, void* stream);
 
 /*
+ * FP32 GEMM on the tcgen05 tensor cores in split TF32 (3xTF32), the product
+ * the FP32 large-matrix path uses for its rank-2k trailing updates and its
+ * eigenvector back-transformation: C = alpha A B + beta C with A (m x k)
+ * given transposed, At (k x m, column-major, element (i, l) of A at
+ * At[l + i ldat]), B (k x n, column-major) and C (m x n, column-major).
+ * Operands are loaded by TMA: At and B 16-byte aligned, ldat and ldb
+ * multiples of 4 (else the argument's index is returned). Error about
+ * 2^-21 relative to sum |a||b| per entry. Asynchronous on the stream; a
+ * bounded wait that ran out inside the kernel is reported by the next call
+ * (status -1000 - cudaErrorLaunchTimeout). No counterpart in the reference.
+ */
+int gla_sgemm_3xtf32(int64_t m, int64_t n, int64_t k, float alpha, const float* At, int64_t ldat, const float* B,
+                     int64_t ldb, float beta, float* C, int64_t ldc, void* stream);
+
+/*
  * Frees the device workspaces that the single-call entry points keep for the
  * life of the process, one per distinct order or size: gla_dsyev, gla_ssyev,
  * gla_dstev, gla_gemm_df, gla_zheev, gla_qheev, gla_dsytrd and gla_dormtr.
