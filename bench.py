@@ -39,8 +39,8 @@ for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
         sys.path.insert(0, _p)
 
 METRIC = "eigh/s (batch n≤128) & n=4096 time at 1e-13 resid: FP32+refine vs FP64 GPU"
-# DRAM bytes (read + write) of the eight k_refine launches of one step of the
-# 1024-matrix workload (ncu dram__bytes_read.sum + dram__bytes_write.sum)
+# DRAM bytes (read + write) of the refinement in one step of the 1024-matrix
+# workload (ncu dram__bytes_read.sum + dram__bytes_write.sum)
 REFINE_DRAM_BYTES_PER_1024 = 281.7e6
 BATCH = 4096
 NLO, NHI = 8, 128
@@ -73,45 +73,35 @@ GRAPH_PASSES = 4
 
 
 def launches_per_step(n_buckets, passes, refined, graph):
-    """Kernels one batched execute launches: per size bucket the
-    tridiagonalisation, a chase and a rotation replay per pass, the
-    refinement (refined paths) and, in a graph plan, the kernel that marks
-    matrices left unfinished by the fixed passes."""
-    return n_buckets * (1 + 2 * passes + (1 if refined else 0) + (1 if graph else 0))
+    """Kernels one batched execute launches. FP32 + refinement: the one
+    persistent solve-and-refine kernel, then over all matrices at once a
+    chase and a rotation replay per pass, the refinement (both finish only
+    the matrices the persistent kernel leaves to the QL chase) and, in a
+    graph plan, the kernel that marks matrices left unfinished. Other paths:
+    per size bucket the tridiagonalisation, a chase and a rotation replay per
+    pass, and the mark in a graph plan."""
+    if refined:
+        return 1 + 2 * passes + 1 + (1 if graph else 0)
+    return n_buckets * (1 + 2 * passes + (1 if graph else 0))
 
 
 def refine_roofline(achieved, peak_ops, batch):
-    """k_refine, the largest share of the batched refined step's ncu launch
-    list: double-float Ogita-Aishima products on the FP32 pipe. achieved =
-    FP32 operations per second, counted as 13 instructions per double-float
-    multiply-add (TwoProduct 2, TwoSum 6, 2 adds, QuickTwoSum 3) and ~3 n^3
-    multiply-adds per iteration (A X, X'(AX), X'X as symmetric halves, X E),
-    over the refinement's phase time (CUDA events on each size bucket's
-    stream); peak = the FP32 FMA rate of cuBLAS SGEMM measured in this run.
-    traffic: DRAM bytes of one step's k_refine launches from an ncu capture
-    of the 1024-matrix case (same order distribution) scaled by the matrix
-    count; the algorithmic bytes are ~20 sum(n^2) = 0.48 GB per step, the
-    rest is the per-matrix double-float scratch (56 n^2 bytes) that no
-    longer fits in L2 at this batch size."""
-    return {"kernel": "k_refine", "bound": "fp32", "achieved": achieved, "peak": peak_ops, "unit": "T FP32 ops/s",
+    """k_solve_refine, the persistent kernel that runs (almost) the whole
+    batched refined step: the FP32 tridiagonalisation and tridiagonal solve,
+    then the double-float Ogita-Aishima refinement, both on the FP32 pipe.
+    achieved = FP32-pipe operations per second over the kernel's time (CUDA
+    events on the execute's stream; see run_ours); peak = the FP32 FMA rate
+    of cuBLAS SGEMM measured in this run. traffic: DRAM bytes of one step
+    of the 1024-matrix case (same order distribution), from an ncu capture,
+    scaled by the matrix count; the algorithmic bytes are ~20 sum(n^2) =
+    0.48 GB per step, the rest is the per-matrix double-float scratch of
+    the refinement (56 n^2 bytes) that does not stay in L2."""
+    return {"kernel": "k_solve_refine", "bound": "fp32", "achieved": achieved, "peak": peak_ops,
+            "unit": "T FP32 ops/s",
             "frac": (achieved / peak_ops) if peak_ops else None,
             "traffic": REFINE_DRAM_BYTES_PER_1024 * batch / 1024 if REFINE_DRAM_BYTES_PER_1024 else None,
             "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, FMA rate (FP32 pipe); "
                            "MEASURED_PEAKS.json has only HBM and bf16 peaks"}
-
-
-def tridiag_roofline(ns, tri_ms, peak_ops):
-    """k_tridiag with the in-kernel FP32 tridiagonal solver (the second share
-    of the launch list): (4/3 + 4/3 + 2) n^3 flops per matrix (reduction, Q
-    formation, X = Q Y; the O(n^2) bisection and vectors not counted), over
-    the tridiagonalisation phase time; peak = twice the FP32 FMA rate.
-    Latency-bound (one CTA per matrix, n dependent reflector steps, 2.1
-    barrier stalls per issue), so the fraction is small by construction."""
-    flops = (4.0 / 3.0 + 4.0 / 3.0 + 2.0) * float((ns.astype(np.float64) ** 3).sum())
-    achieved = flops / (tri_ms * 1e-3) / 1e12 if tri_ms > 0 else 0.0
-    return {"kernel": "k_tridiag (with the FP32 tridiagonal solver)", "bound": "latency", "achieved": achieved,
-            "peak": 2.0 * peak_ops if peak_ops else None, "unit": "TFLOP/s FP32",
-            "frac": achieved / (2.0 * peak_ops) if peak_ops else None, "traffic": None}
 
 
 def replica_seed(rank):
@@ -410,18 +400,18 @@ def run_ours(args):
         ph = H["phase_ms_per_step"]
         c = H["counters"]
         ns3 = float((ns.astype(np.float64) ** 3).sum())
-        # Rooflines of the batched step's two largest kernels in its ncu launch
-        # list: k_chase (the larger share; latency-bound) and k_refine. The
-        # refinement's double-float arithmetic runs on the FP32 pipe: achieved
-        # = FP32 operations per second, counted as
-        # 13 instructions per double-float multiply-add (TwoProduct 2, TwoSum 6,
-        # 2 adds, QuickTwoSum 3) and ~3 n^3 multiply-adds per iteration (A X,
-        # X'(AX), X'X as symmetric halves, X E); peak = the FP32 FMA rate of
-        # cuBLAS SGEMM measured in this run (TFLOP/s / 2).
+        # Roofline of the refined step's dominant kernel, the persistent
+        # k_solve_refine (its time is the plan's "tridiag" phase): FP32-pipe
+        # operations per second, counted as 13 instructions per double-float
+        # multiply-add of the refinement (TwoProduct 2, TwoSum 6, 2 adds,
+        # QuickTwoSum 3) times ~3 n^3 multiply-adds per iteration (A X,
+        # X'(AX), X'X as symmetric halves, X E), plus the FP32 multiply-adds
+        # of the reduction, Q and X = Q Y ((4/3 + 4/3 + 2) n^3 / 2); peak = the
+        # FP32 FMA rate of cuBLAS SGEMM measured in this run (TFLOP/s / 2).
         sg = measured_sgemm_tflops(torch)
-        refine_ms = ph.get("refine", 0.0)
-        ops = 13.0 * 3.0 * c["refine_n3"]
-        achieved = ops / (refine_ms * 1e-3) / 1e12 if refine_ms > 0 else 0.0
+        fused_ms = ph.get("tridiag", 0.0)
+        ops = 13.0 * 3.0 * c["refine_n3"] + (4.0 / 3.0 + 4.0 / 3.0 + 2.0) / 2.0 * ns3
+        achieved = ops / (fused_ms * 1e-3) / 1e12 if fused_ms > 0 else 0.0
         peak_ops = sg / 2.0
         cpu = cpu_baseline(ns, mats)
         lapack = lapack_baseline(ns, mats)
@@ -443,7 +433,6 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}",
                        "timing": "CUDA-graph replay of the whole batched solve (plan with GLA_FLAG_GRAPH)"},
             "roofline": refine_roofline(achieved, peak_ops, len(ns)),
-            "roofline_tridiag": tridiag_roofline(ns, ph.get("tridiag", 0.0), peak_ops),
             "roofline_large": large_roofline(large, measured_peaks_file()),
             "fp64_dgemm_tflops_measured": peak,
             "cpu_baseline": cpu,
@@ -495,7 +484,8 @@ def summary(line):
                     "refined_max_err": max([v for v in acc.values() if v is not None], default=None),
                     "refined_meets_1e13": r.get("refined_meets_1e13")}
     c1 = line.get("c1_single_n64") or {}
-    out["c1_n64"] = {"gpu_us": c1.get("gpu_us_per_solve"), "cpu_1core_us": c1.get("cpu_oracle_us_per_solve_1core")}
+    out["c1_n64"] = {"gpu_us": c1.get("gpu_us_per_solve"), "cpu_1core_us": c1.get("cpu_oracle_us_per_solve_1core"),
+                     "refined_route_us": g(c1, "refined_route", "us_per_solve")}
     c4 = line.get("c4_forward_adjoint") or {}
     if c4:
         out["c4_graph_speedup"] = (g(c4, "f32_refined", "graph_matrices_per_s") or 0) / max(
@@ -581,8 +571,11 @@ def run_c4(torch, glagpu, dev, reps=3):
 
 def run_c1(torch, glagpu, dev, reps=200):
     """Single matrix: eigen!(Hermitian(A)) FP64, n = 64 GOE (seed 1), through
-    gla_dsyev (device pointers; it synchronizes to return info). Latency per
-    solve on the GPU beside one host core running the oracle port."""
+    gla_dsyev (device pointers; it synchronizes to return info: the
+    reference's algorithm in FP64, whose QL chase is one serial FP64 chain)
+    and through a one-matrix FP32 + refinement plan (FP64-accurate results).
+    Latency per solve on the GPU beside one host core running the oracle
+    port, and the error of both against the oracle and the 256-bit values."""
     import ctypes
     import glagpu._lib as L
     from helpers import goe, orth, residual
@@ -615,10 +608,42 @@ def run_c1(torch, glagpu, dev, reps=200):
         O.syev(A0)
         k += 1
     cpu_us = (time.perf_counter() - t0) / k * 1e6
-    return {"n": n, "gpu_us_per_solve": gpu_us, "cpu_oracle_us_per_solve_1core": cpu_us,
-            "timing": "host wall clock per gla_dsyev call (copy-in of A, solve, info read), mean of %d" % reps,
-            "accuracy": {"residual": residual(A0, V, wh), "orthogonality": orth(V),
-                         "eig_err_vs_oracle": float(np.abs(wh - wo).max())}, "info": int(info.value)}
+    # the same matrix through the FP32 + refinement route (FP64-accurate
+    # results): a one-matrix plan, device buffers, info read back each call
+    plan = glagpu.Plan([n], precision="f32_refined")
+    wr = torch.empty(n, dtype=torch.float64, device=dev)
+    Vr = torch.empty(n * n, dtype=torch.float64, device=dev)
+    infor = torch.zeros(1, dtype=torch.int32, device=dev)
+    for _ in range(5):
+        plan.execute(Ad, wr, Vr, infor)
+        int(infor.item())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        plan.execute(Ad, wr, Vr, infor)
+        int(infor.item())
+    ref_us = (time.perf_counter() - t0) / reps * 1e6
+    Vh = Vr.cpu().numpy().reshape(n, n, order="F")
+    wrh = wr.cpu().numpy()
+    plan.close()
+    out = {"n": n, "gpu_us_per_solve": gpu_us, "cpu_oracle_us_per_solve_1core": cpu_us,
+           "timing": "host wall clock per gla_dsyev call (copy-in of A, solve, info read), mean of %d" % reps,
+           "accuracy": {"residual": residual(A0, V, wh), "orthogonality": orth(V),
+                        "eig_err_vs_oracle": float(np.abs(wh - wo).max())}, "info": int(info.value),
+           "refined_route": {"us_per_solve": ref_us, "info": int(infor.item()),
+                             "timing": "host wall clock per one-matrix FP32 + refinement plan execute "
+                                       "(device buffers, info read back), mean of %d" % reps,
+                             "accuracy": {"residual": residual(A0, Vh, wrh), "orthogonality": orth(Vh),
+                                          "eig_err_vs_oracle": float(np.abs(wrh - wo).max())}}}
+    try:  # the 256-bit eigenvalues of this exact input (tests/golden/golden_large.json)
+        from helpers import golden_large
+        A256, w256, _, _ = golden_large(n)
+        if np.array_equal(A256, A0):
+            out["eig_err_vs_256bit"] = float(np.abs(wh - w256).max())
+            out["refined_route"]["eig_err_vs_256bit"] = float(np.abs(wrh - w256).max())
+    except Exception:
+        pass
+    return out
 
 
 def c5_workload():

@@ -149,6 +149,11 @@ struct gla_plan_s {
   bool timing = false;
   bool graph = false;  // capture-safe execute (no host synchronisation)
   bool stein = false;  // FP32 stage by bisection + twisted factorisation (small_stein.cuh)
+  // F32_REFINED with that solver: the orders <= 128 are solved and refined by
+  // one persistent launch (k_solve_refine) instead of per-bucket pipelines
+  bool persistent = false;
+  int persist_grid = 0;
+  int* d_next = nullptr;  // its work counter
   cudaEvent_t tev[kMaxBuckets][GLA_NUM_PHASES][2] = {};
   bool tused[kMaxBuckets][GLA_NUM_PHASES] = {};
   void mark(int b, int phase, int end, cudaStream_t st) {
@@ -226,6 +231,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->graph = (flags & GLA_FLAG_GRAPH) != 0;
   p->stein = (precision == GLA_PREC_F32_REFINED && !(flags & GLA_FLAG_REFINE_QL)) ||
              (precision == GLA_PREC_F32 && (flags & GLA_FLAG_F32_BISECT));
+  p->persistent = p->stein && precision == GLA_PREC_F32_REFINED;
   p->n.assign(n, n + batch);
 
   // ---- descriptors and offsets
@@ -307,6 +313,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   const size_t o_w32 = carve(refined ? 4 * woff : 0);
   const size_t o_vtmp = carve((jobz == 'N' && refined) ? 8 * aoff : 0);
   const size_t o_qtmp = carve(p->stein ? 4 * aoff : 0);
+  const size_t o_next = carve(sizeof(int));
   size_t refine_bytes = refined ? refine_workspace_bytes(aoff, woff, batch) : 0;
   const size_t o_ref = carve(refine_bytes);
   p->ws_bytes = off;
@@ -330,6 +337,13 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->d_w32 = refined ? (void*)(w + o_w32) : nullptr;
   p->d_vtmp = (jobz == 'N' && refined) ? (void*)(w + o_vtmp) : nullptr;
   p->d_qtmp = p->stein ? (void*)(w + o_qtmp) : nullptr;
+  p->d_next = (int*)(w + o_next);
+  if (p->persistent) {  // two CTAs per SM (registers and shared memory allow two)
+    int dev = 0, nsm = 0;
+    if (err == cudaSuccess) err = cudaGetDevice(&dev);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    p->persist_grid = std::max(1, std::min(2 * nsm, p->nwork));
+  }
   if (refined) refine_carve(&p->rw, w + o_ref, aoff, woff, batch);
   if (batch) err = cudaMemcpy(p->d_desc, desc.data(), sizeof(SmallDesc) * batch, cudaMemcpyHostToDevice);
   if (err == cudaSuccess && !perm_bucket.empty())
@@ -504,7 +518,8 @@ namespace {
 int enqueue_refine(gla_plan_t p, int b, const void* A, int lower, void* Vout, void* w, int* info, cudaStream_t st) {
   const Bucket& bk = p->buckets[b];
   GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
-                         lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats));
+                         lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats,
+                         p->d_cst));
   return 0;
 }
 
@@ -560,6 +575,60 @@ int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cuda
   return 0;
 }
 
+// The orders <= 128 of an FP32 + refinement plan with the in-kernel FP32
+// solver: one persistent launch solves and refines every matrix it can
+// (largest first, from a work counter); the QL chase, rotation replay and
+// refinement kernels, launched once over all those matrices, finish the
+// few it leaves (they skip the rest). With no host check in capture-safe
+// plans; otherwise a full rotation log is finished by further host-checked
+// passes.
+int execute_persistent(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st) {
+  const int lower = p->uplo == 'L';
+  const int n = p->nwork;
+  GLA_CUDA(cudaMemsetAsync(p->d_next, 0, sizeof(int), st));
+  p->mark(0, GLA_PHASE_TRIDIAG, 0, st);
+  GLA_CUDA(launch_solve_refine(&p->rw, n, p->nmax, p->persist_grid, st, p->d_desc, p->d_perm_bucket, p->d_next,
+                               (const double*)A, lower, (float*)p->d_d, (float*)p->d_e, (float*)p->d_x32, info,
+                               p->d_cst, p->d_scale, (float*)p->d_w32, (float*)p->d_qtmp, (double*)Vout, (double*)w,
+                               p->d_stats));
+  p->mark(0, GLA_PHASE_TRIDIAG, 1, st);
+  const int npass = p->graph ? kGraphPasses : kAsyncPasses;
+  auto pass = [&]() -> int {
+    GLA_CUDA(cudaMemsetAsync(p->d_pending, 0, sizeof(int), st));
+    GLA_CUDA(launch_chase(kF32, p->algo, n, chase_smem_bytes(p->nmax, 4), st, p->d_desc, p->d_perm_bucket, p->d_d,
+                          p->d_e, p->d_cst, p->d_rot, p->d_hdr, info, p->tol, kMaxSweepsPerN, p->d_pending,
+                          p->d_stats));
+    GLA_CUDA(launch_apply(kF32, n, kSmallMaxN, apply_smem_bytes(p->nmax, 4), st, p->d_desc, p->d_perm_bucket,
+                          p->d_x32, p->d_d, p->d_w32, p->d_cst, p->d_rot, p->d_hdr, info, p->d_scale));
+    return 0;
+  };
+  p->mark(0, GLA_PHASE_CHASE, 0, st);
+  for (int k = 0; k < npass; k++) {
+    int rc = pass();
+    if (rc) return rc;
+  }
+  p->mark(0, GLA_PHASE_CHASE, 1, st);
+  int passes = npass;
+  if (p->graph) {
+    GLA_CUDA(launch_mark_unfinished(n, st, p->d_desc, p->d_perm_bucket, p->d_cst, info));
+  } else {
+    for (;;) {  // a rotation log that filled up in every pass so far
+      GLA_CUDA(cudaMemcpyAsync(p->pin_pending, p->d_pending, sizeof(int), cudaMemcpyDeviceToHost, st));
+      GLA_CUDA(cudaStreamSynchronize(st));
+      if (p->pin_pending[0] == 0 || passes >= kMaxPasses) break;
+      int rc = pass();
+      if (rc) return rc;
+      passes++;
+    }
+  }
+  p->last_passes = passes;
+  p->mark(0, GLA_PHASE_REFINE, 0, st);
+  GLA_CUDA(launch_refine(&p->rw, n, p->nmax, st, p->d_desc, p->d_perm_bucket, (const double*)A, lower,
+                         (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats, p->d_cst));
+  p->mark(0, GLA_PHASE_REFINE, 1, st);
+  return 0;
+}
+
 // Every size bucket runs its whole pipeline on its own stream (buckets are
 // independent), forked from and joined back into the caller's stream, so
 // the long chases of the largest matrices overlap with the other buckets.
@@ -583,6 +652,7 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
   void* wq = refined ? p->d_w32 : w;
   const int* scale = refined ? p->d_scale : nullptr;
   void* Vout = p->jobz == 'V' ? V : p->d_vtmp;
+  if (p->persistent) return execute_persistent(p, A, w, Vout, info, st);
   const int nb = (int)p->buckets.size();
   GLA_CUDA(cudaEventRecord(p->fork, st));
   for (int b = 0; b < nb; b++) {

@@ -28,8 +28,21 @@ struct RefineWork {
 size_t refine_workspace_bytes(int64_t a_elems, int64_t w_elems, int64_t batch);
 void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t w_elems, int64_t batch);
 cudaError_t refine_kernels_init();
+// ChaseState.applied of a matrix that k_solve_refine has solved and refined.
+constexpr int kRefinedInKernel = 2;
+
+// One CTA per matrix (perm[0..nblocks)); with cst, matrices already refined
+// by the persistent kernel are skipped.
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
-                          int* info, const int* scale_exp, unsigned long long* stats);
+                          int* info, const int* scale_exp, unsigned long long* stats,
+                          const ChaseState* cst = nullptr);
+
+// The persistent FP32 + refinement solve of count matrices (order: largest
+// first) on grid CTAs; *next must be zero on entry.
+cudaError_t launch_solve_refine(const RefineWork* rw, int count, int nmax, int grid, cudaStream_t st,
+                                const SmallDesc* descs, const int* order, int* next, const double* A, int lower,
+                                float* d, float* e, float* X32, int* info, ChaseState* cst, int* scale_exp,
+                                float* w32, float* qtmp, double* V, double* w, unsigned long long* stats);
 
 }  // namespace gla

@@ -28,7 +28,9 @@
 // iterate that the next iteration removes quadratically; from the second
 // iteration on |E| <= 1e-8 and the error is below 1e-15.
 #include "df64.cuh"
+#include "gla_launch.h"
 #include "gla_refine.h"
+#include "small_tridiag.cuh"
 #include "tile_gemm.cuh"
 
 namespace gla {
@@ -122,12 +124,11 @@ GLA_DEV void jacobi_warp(int k, float* C, float* Z) {
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
-                                                const double* __restrict__ A, int lower,
-                                                const float* __restrict__ X32, double* __restrict__ Vout,
-                                                double* __restrict__ wout, int* __restrict__ info,
-                                                const int* __restrict__ scale_exp, RefineWork rw,
-                                                unsigned long long* __restrict__ stats) {
+// The refinement of matrix mid by the whole CTA (kRT threads).
+GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const double* __restrict__ A, int lower,
+                         const float* __restrict__ X32, double* __restrict__ Vout, double* __restrict__ wout,
+                         int* __restrict__ info, const int* __restrict__ scale_exp, const RefineWork& rw,
+                         unsigned long long* __restrict__ stats) {
   __shared__ df64 As[16 * kTP];
   __shared__ df64 Bs2[16 * kTP];
   __shared__ double lam[kSmallMaxN];
@@ -138,7 +139,6 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
   __shared__ int ncl_s, flag_s, big_s;
   __shared__ double gmin_s, lmax_s;
   float* Bsf = reinterpret_cast<float*>(Bs2);
-  const int mid = perm[blockIdx.x];
   const SmallDesc dsc = descs[mid];
   const int n = dsc.n, tid = threadIdx.x;
   const size_t ao = dsc.a_off;
@@ -444,15 +444,76 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
     }
 }
 
-cudaError_t refine_kernels_init() { return cudaSuccess; }
+// One CTA per matrix; a matrix the persistent kernel below already refined
+// (ChaseState.applied == kRefinedInKernel) is skipped.
+__global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
+                                                const double* __restrict__ A, int lower,
+                                                const float* __restrict__ X32, double* __restrict__ Vout,
+                                                double* __restrict__ wout, int* __restrict__ info,
+                                                const int* __restrict__ scale_exp, RefineWork rw,
+                                                unsigned long long* __restrict__ stats,
+                                                const ChaseState* __restrict__ cst) {
+  const int mid = perm[blockIdx.x];
+  if (cst && cst[mid].applied == kRefinedInKernel) return;
+  refine_body(mid, descs, A, lower, X32, Vout, wout, info, scale_exp, rw, stats);
+}
+
+// The whole FP32 + refinement solve of a batch in one persistent launch:
+// every CTA takes the next matrix (largest orders first, from an atomic
+// counter), tridiagonalises it and solves the tridiagonal in FP32
+// (tridiag_body with the per-eigenvalue solver), then refines the pair to
+// FP64 accuracy (refine_body), and takes the next. A matrix the FP32 solver
+// leaves to the QL chase (or with non-finite input) is left to the chase,
+// rotation-replay and refinement kernels that follow (they skip the rest).
+__global__ void __launch_bounds__(kRT, 2)
+    k_solve_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ order, int count,
+                   int* __restrict__ next, const double* __restrict__ A, int lower, float* __restrict__ d,
+                   float* __restrict__ e, float* __restrict__ X32, int* __restrict__ info,
+                   ChaseState* __restrict__ cst, int* __restrict__ scale_exp, float* __restrict__ w32,
+                   float* __restrict__ qtmp, double* __restrict__ Vout, double* __restrict__ wout, RefineWork rw,
+                   unsigned long long* __restrict__ stats) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_idx;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_idx = atomicAdd(next, 1);
+    __syncthreads();
+    const int idx = s_idx;
+    if (idx >= count) return;
+    const int mid = order[idx];
+    tridiag_body<float, double, true, true>(mid, smem_raw, descs, A, lower, d, e, X32, info, cst, scale_exp, w32,
+                                            qtmp);
+    __syncthreads();
+    if (cst[mid].applied == 1) {  // solved in FP32 (small_stein.cuh)
+      refine_body(mid, descs, A, lower, X32, Vout, wout, info, scale_exp, rw, stats);
+      __syncthreads();
+      if (threadIdx.x == 0) cst[mid].applied = kRefinedInKernel;
+    }
+  }
+}
+
+cudaError_t refine_kernels_init() {
+  return cudaFuncSetAttribute(k_solve_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tridiag_smem_bytes(kSmallMaxN, kRT, 4));
+}
 
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
-                          int* info, const int* scale_exp, unsigned long long* stats) {
+                          int* info, const int* scale_exp, unsigned long long* stats, const ChaseState* cst) {
   if (nblocks <= 0) return cudaSuccess;
   (void)nmax;
-  k_refine<<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw,
-                                                          stats);
+  k_refine<<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw, stats, cst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solve_refine(const RefineWork* rw, int count, int nmax, int grid, cudaStream_t st,
+                                const SmallDesc* descs, const int* order, int* next, const double* A, int lower,
+                                float* d, float* e, float* X32, int* info, ChaseState* cst, int* scale_exp,
+                                float* w32, float* qtmp, double* V, double* w, unsigned long long* stats) {
+  if (count <= 0) return cudaSuccess;
+  k_solve_refine<<<grid, kRT, tridiag_smem_bytes(nmax, kRT, 4), st>>>(descs, order, count, next, A, lower, d, e, X32,
+                                                                      info, cst, scale_exp, w32, qtmp, V, w, *rw,
+                                                                      stats);
   return cudaGetLastError();
 }
 

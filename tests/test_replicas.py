@@ -118,20 +118,18 @@ def test_roofline_figures():
     # with their algorithmic work over their time
     import bench
     r = bench.refine_roofline(7.0, 35.0, 4096)
-    assert r["kernel"] == "k_refine" and r["unit"] == "T FP32 ops/s"
+    assert r["kernel"] == "k_solve_refine" and r["unit"] == "T FP32 ops/s"
     assert abs(r["frac"] - 0.2) < 1e-12
     assert abs(r["traffic"] - 4 * bench.REFINE_DRAM_BYTES_PER_1024) < 1.0
     assert bench.refine_roofline(7.0, None, 4096)["frac"] is None
-    import numpy as np
-    t = bench.tridiag_roofline(np.array([128, 64]), 2.0, 35.0)
-    flops = (4 / 3 + 4 / 3 + 2) * (128 ** 3 + 64 ** 3)
-    assert abs(t["achieved"] - flops / 2e-3 / 1e12) < 1e-12 and t["peak"] == 70.0
 
 
 def test_launch_counts():
-    # per size bucket: tridiagonalisation, (chase, replay) per pass, the
-    # refinement, and in a graph plan the unfinished-matrix mark
+    # refined: one persistent kernel, (chase, replay) per pass and one
+    # refinement over all matrices, the mark in a graph plan; other paths per
+    # size bucket: tridiagonalisation, (chase, replay) per pass, the mark
     import bench
-    assert bench.launches_per_step(8, 2, True, False) == 8 * 6
-    assert bench.launches_per_step(8, bench.GRAPH_PASSES, True, True) == 8 * 11
+    assert bench.launches_per_step(8, 2, True, False) == 6
+    assert bench.launches_per_step(8, bench.GRAPH_PASSES, True, True) == 11
     assert bench.launches_per_step(8, bench.GRAPH_PASSES, False, True) == 8 * 10
+    assert bench.launches_per_step(8, 2, False, False) == 8 * 5
