@@ -445,7 +445,7 @@ namespace {
 // One chase pass (+ rotation replay, and the sort once a matrix is done) of
 // bucket b on stream st. V holds Q (or the previous pass's rotated Q).
 int enqueue_pass(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info, const int* scale,
-                 cudaStream_t st, bool timed = false) {
+                 cudaStream_t st, bool timed = false, bool rows2 = false) {
   const Bucket& bk = p->buckets[b];
   const int work_t = tcode == kF64 ? kF64 : kF32;
   const int el = tcode == kF64 ? 8 : 4;
@@ -459,7 +459,8 @@ int enqueue_pass(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info,
     p->mark(b, GLA_PHASE_APPLY, 0, st);
   }
   GLA_CUDA(launch_apply(work_t, bk.count, bk.nt, apply_smem_bytes(bk.nmax, el), st, p->d_desc,
-                        p->d_perm_bucket + bk.start, V, p->d_d, wout, p->d_cst, p->d_rot, p->d_hdr, info, scale));
+                        p->d_perm_bucket + bk.start, V, p->d_d, wout, p->d_cst, p->d_rot, p->d_hdr, info, scale,
+                        rows2));
   if (timed) p->mark(b, GLA_PHASE_APPLY, 1, st);
   return 0;
 }
@@ -467,7 +468,7 @@ int enqueue_pass(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info,
 // Chase passes until bucket b has no matrix left with a full rotation log
 // (host-checked; used by the single-matrix drivers and as the fallback).
 int run_passes_sync(gla_plan_t p, int b, int tcode, void* V, void* wout, int* info, const int* scale,
-                    cudaStream_t st, int done_passes) {
+                    cudaStream_t st, int done_passes, bool rows2 = false) {
   int passes = done_passes;
   for (;;) {
     if (passes > 0) {
@@ -475,7 +476,7 @@ int run_passes_sync(gla_plan_t p, int b, int tcode, void* V, void* wout, int* in
       GLA_CUDA(cudaStreamSynchronize(st));
       if (p->pin_pending[b] == 0 || passes >= kMaxPasses) break;
     }
-    int rc = enqueue_pass(p, b, tcode, V, wout, info, scale, st);
+    int rc = enqueue_pass(p, b, tcode, V, wout, info, scale, st, false, rows2);
     if (rc) return rc;
     passes++;
   }
@@ -763,6 +764,59 @@ int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* 
   int bad = 0;
   for (int64_t b = 0; b < p->batch; b++) bad += info_host[b] != 0;
   return bad;
+}
+
+int gla_plan_execute_eigen2(gla_plan_t p, const void* A, void* w, void* V2, int* info, void* stream) {
+  if (!p) return -1;
+  if (!A && p->a_elems) return -2;
+  if (!w && p->w_elems) return -3;
+  if (!V2 && p->w_elems) return -4;
+  if (!info && p->batch) return -5;
+  if (p->jobz != 'V' || p->prec == GLA_PREC_F32_REFINED || !p->large_idx.empty()) return GLA_ERR_UNSUPPORTED;
+  cudaStream_t st = (cudaStream_t)stream;
+  p->last_stream = st;
+  p->last_passes = 0;
+  for (int b = 0; b < kMaxBuckets; b++)
+    for (int ph = 0; ph < GLA_NUM_PHASES; ph++) p->tused[b][ph] = false;
+  GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
+  if (p->batch) GLA_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * p->batch, st));
+  if (p->nwork == 0) return 0;
+  const int tc = p->tcode(), el = (int)p->elem();
+  const int nb = (int)p->buckets.size();
+  GLA_CUDA(cudaEventRecord(p->fork, st));
+  for (int b = 0; b < nb; b++) {
+    const Bucket& bk = p->buckets[b];
+    cudaStream_t s = bk.stream;
+    GLA_CUDA(cudaStreamWaitEvent(s, p->fork, 0));
+    p->mark(b, GLA_PHASE_TRIDIAG, 0, s);
+    GLA_CUDA(launch_tridiag(tc, false, bk.count, bk.nt_tri, tridiag_smem_bytes(bk.nmax, bk.nt_tri, el), s, p->d_desc,
+                            p->d_perm_bucket + bk.start, A, p->uplo == 'L', p->d_d, p->d_e, nullptr, info, p->d_cst,
+                            p->d_scale, false, nullptr, nullptr, V2));
+    p->mark(b, GLA_PHASE_TRIDIAG, 1, s);
+    const int npass = p->graph ? kGraphPasses : kAsyncPasses;
+    for (int k = 0; k < npass; k++) {
+      int rc = enqueue_pass(p, b, tc, V2, w, info, nullptr, s, k == 0, true);
+      if (rc) return rc;
+    }
+    if (p->graph)
+      GLA_CUDA(launch_mark_unfinished(bk.count, s, p->d_desc, p->d_perm_bucket + bk.start, p->d_cst, info));
+    else
+      GLA_CUDA(cudaMemcpyAsync(p->pin_pending + b, p->d_pending + b, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GLA_CUDA(cudaEventRecord(bk.join, s));
+    GLA_CUDA(cudaStreamWaitEvent(st, bk.join, 0));
+  }
+  if (p->graph) {
+    p->last_passes = kGraphPasses;
+    return 0;
+  }
+  GLA_CUDA(cudaStreamSynchronize(st));
+  p->last_passes = kAsyncPasses;
+  for (int b = 0; b < nb; b++) {
+    if (p->pin_pending[b] == 0) continue;
+    int rc = run_passes_sync(p, b, tc, V2, w, info, nullptr, st, kAsyncPasses, true);
+    if (rc) return rc;
+  }
+  return 0;
 }
 
 int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const double* wbar, const double* Vbar,

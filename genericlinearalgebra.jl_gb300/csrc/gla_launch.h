@@ -29,20 +29,23 @@ cudaError_t small_kernels_init();
 // stein (FP32 work type with Q only): the CTA also solves the tridiagonal
 // (bisection + twisted factorisation) and writes X = Q Y and the eigenvalues
 // (to w) for every matrix it does not leave to the QL chase; qtmp: a float
-// scratch arena of the plan's a_elems entries.
+// scratch arena of the plan's a_elems entries. rows2 (wantq false): rows 1
+// and n of Q instead (2 x n column-major per matrix, at twice its w offset),
+// for eigen2.
 cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
                            const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
                            void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein = false,
-                           void* w = nullptr, void* qtmp = nullptr);
+                           void* w = nullptr, void* qtmp = nullptr, void* rows2 = nullptr);
 
 cudaError_t launch_chase(int tcode, int algo, int count, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* d, void* e, ChaseState* cst, void* rot, unsigned* hdr, int* info,
                          double tol, int max_sweeps_per_n, int* pending, unsigned long long* stats,
                          int lanes_per_warp = 0);
 
+// rows2: V holds rows 1 and n only (eigen2; 2 x n at twice the w offset).
 cudaError_t launch_apply(int tcode, int nblocks, int nt, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* V, const void* d, void* w, ChaseState* cst, const void* rot,
-                         const unsigned* hdr, const int* info, const int* scale_exp);
+                         const unsigned* hdr, const int* info, const int* scale_exp, bool rows2 = false);
 
 cudaError_t launch_sort_values(int tcode, int nblocks, cudaStream_t st, const SmallDesc* descs, const int* perm,
                                const void* d, void* w, const int* info, const int* scale_exp);

@@ -36,17 +36,16 @@
 #include <stdint.h>
 
 #include "df64.cuh"
+#include "oz_prims.cuh"
 
 namespace gla {
 namespace oz {
 
 constexpr int kBM = 128;        // C tile rows (MMA M)
-constexpr int kKS = 32;         // k per pipeline stage (two K = 16 MMAs per slice pair)
 constexpr int kGroupK = 256;    // k per TMEM drain (exactness bound)
 constexpr int kMaxSlices = 7;
 constexpr int kDrainWarps = 8;  // two per TMEM lane quarter
 constexpr int kThreads = 64 + 32 * kDrainWarps;
-constexpr long long kWaitLimit = 1ll << 26;
 
 // Bytes of one tiled slab block: rows x kKS k, bf16.
 __host__ __device__ constexpr int block_bytes(int rows) { return rows * kKS * 2; }
@@ -84,14 +83,6 @@ struct OzCfg {
 using CfgDF = OzCfg<7, 64, true>;
 using CfgF32 = OzCfg<4, 128, false>;
 
-// Byte offset of element (r, kk) inside a tiled slab block (8-row x 8-k core
-// matrices of 128 contiguous bytes; K-neighbours 128 B apart = LBO, row
-// groups kSBO = 512 B apart = SBO).
-constexpr int kSBO = kKS * 16;
-__host__ __device__ __forceinline__ int tile_off(int r, int kk) {
-  return (r >> 3) * kSBO + (kk >> 3) * 128 + (r & 7) * 16 + (kk & 7) * 2;
-}
-
 // Sliced operand: slice s, row block b (height H rows), k slab q at
 // base + ((b * nks + q) * S + s) * block_bytes(H): the slices of one slab are
 // adjacent, so one bulk copy moves all of them.
@@ -101,69 +92,6 @@ struct Sliced {
   unsigned* mbits;  // per row: bits of max |hi| (slicing scratch)
   int rows, nblk, nks, H, S;  // S: slices per value once sliced, 0 before
 };
-
-GLA_DEV uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-GLA_DEV uint64_t make_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)((128u >> 4) & 0x3FFF) << 16;  // LBO: K-neighbour core matrices
-  d |= (uint64_t)(((uint32_t)kSBO >> 4) & 0x3FFF) << 32;  // SBO: next 8-row group
-  d |= (uint64_t)1 << 46;                        // descriptor version (tcgen05)
-  return d;                                      // base offset 0, no swizzle
-}
-
-
-GLA_DEV void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
-}
-GLA_DEV bool mbar_try(uint64_t* b, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-      : "=r"(done)
-      : "r"(smem_u32(b)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-// Bounded wait; false when it ran out or another thread flagged an error.
-GLA_DEV bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* err) {
-  for (long long it = 0; it < kWaitLimit; it++) {
-    if (mbar_try(b, parity)) return true;
-    if ((it & 1023) == 1023 && *err) return false;
-  }
-  atomicExch((int*)err, 1);
-  return false;
-}
-GLA_DEV void mbar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-GLA_DEV void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-GLA_DEV void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-GLA_DEV void mma_f16(uint32_t tmem_d, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
-          tmem_d),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
-}
-GLA_DEV void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-GLA_DEV void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
 
 struct GemmArgs {
   Sliced A, B;           // A: rows = M (H = 128); B: rows = N (H = BN)
@@ -215,11 +143,6 @@ __global__ void __launch_bounds__(256) k_oz_rowmax_rows(const float* __restrict_
   float m = 0.f;
   for (int k = k0; k < k1; k++) m = fmaxf(m, fabsf(hi[c + (long long)k * ld]));
   if (m > 0.f) atomicMax(&mbits[c], __float_as_uint(m));
-}
-
-GLA_DEV int slice_exp(unsigned mb) {
-  const float m = __uint_as_float(mb);
-  return m > 0.f ? ilogbf(m) + 1 : 0;
 }
 
 // ROWS = false: operand row c is source column c (element (c, k) at

@@ -30,7 +30,10 @@ size_t apply_smem_bytes(int n, int elem) {
 // wout/Vout_final: sorted outputs written only once the chase is done; for
 // the reduced-precision run they are the FP32 workspace copies.
 // scale_exp: eigenvalues are multiplied by 2^scale_exp on output (may be null).
-template <class T>
+// ROWS2 (eigen2!): V holds only rows 1 and n of the eigenvector matrix,
+// 2 x n column-major at twice the matrix's w offset; the same replay and sort
+// on those two rows.
+template <class T, bool ROWS2>
 __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                T* __restrict__ V, const T* __restrict__ dg_all,
                                                T* __restrict__ wout, ChaseState* __restrict__ cst,
@@ -43,24 +46,26 @@ __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ des
   if (st.applied) return;
   const bool done = st.status == kChaseDone;
   if (!done && st.nhdr == 0) return;  // nothing logged for this matrix in this pass
-  const int n = dsc.n, ld = n + 1;
+  const int n = dsc.n;
+  const int nr = ROWS2 ? 2 : n;   // rows held
+  const int ld = ROWS2 ? 2 : n + 1;
   const int tid = threadIdx.x, NT = blockDim.x;
   T* S = reinterpret_cast<T*>(smem_raw);
   T* buf = S + (size_t)n * ld;
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(buf + 2 * kRotChunk);
   int* rank = reinterpret_cast<int*>(keys + n);
-  T* Vg = V + dsc.a_off;
+  T* Vg = V + (ROWS2 ? 2 * dsc.w_off : dsc.a_off);  // column-major, leading dimension nr
 
   if (info[mid] == -1) {  // non-finite input: NaN outputs
     const T nanv = (T)NAN;
-    for (int idx = tid; idx < n * n; idx += NT) Vg[idx] = nanv;
+    for (int idx = tid; idx < nr * n; idx += NT) Vg[idx] = nanv;
     for (int i = tid; i < n; i += NT) wout[dsc.w_off + i] = nanv;
     if (tid == 0) cst[mid].applied = 1;
     return;
   }
 
   for (int j = 0; j < n; j++)
-    for (int i = tid; i < n; i += NT) S[(size_t)j * ld + i] = Vg[(size_t)j * n + i];
+    for (int i = tid; i < nr; i += NT) S[(size_t)j * ld + i] = Vg[(size_t)j * nr + i];
   __syncthreads();
 
   // ---- replay this pass's rotations: whole sweeps per staged chunk
@@ -69,7 +74,7 @@ __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ des
   const int nhdr = st.nhdr;
   for (int h = tid; h < nhdr; h += NT) hs[h] = hdr[dsc.hdr_off + h];
   const int r = tid;
-  const bool row = r < n;
+  const bool row = r < nr;
   T* Sr = S + r;
   int h = 0, q0 = 0;
   while (h < nhdr) {
@@ -107,7 +112,7 @@ __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ des
 
   if (!done) {  // partial pass: write the rotated Q back for the next pass
     for (int j = 0; j < n; j++)
-      for (int i = tid; i < n; i += NT) Vg[(size_t)j * n + i] = S[(size_t)j * ld + i];
+      for (int i = tid; i < nr; i += NT) Vg[(size_t)j * nr + i] = S[(size_t)j * ld + i];
     return;
   }
 
@@ -131,7 +136,7 @@ __global__ void __launch_bounds__(128) k_apply(const SmallDesc* __restrict__ des
   __syncthreads();
   for (int j = 0; j < n; j++) {
     const int dst = rank[j];
-    for (int i = tid; i < n; i += NT) Vg[(size_t)dst * n + i] = S[(size_t)j * ld + i];
+    for (int i = tid; i < nr; i += NT) Vg[(size_t)dst * nr + i] = S[(size_t)j * ld + i];
   }
   if (tid == 0) cst[mid].applied = 1;
 }
@@ -199,23 +204,32 @@ __global__ void k_init_tridiagonal(const SmallDesc* __restrict__ descs, const in
 }
 
 cudaError_t apply_kernels_init() {
-  cudaFuncSetAttribute(k_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_apply<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)apply_smem_bytes(kSmallMaxN, 8));
-  cudaFuncSetAttribute(k_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_apply<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)apply_smem_bytes(kSmallMaxN, 4));
+  cudaFuncSetAttribute(k_apply<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)apply_smem_bytes(kSmallMaxN, 8));
+  cudaFuncSetAttribute(k_apply<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)apply_smem_bytes(kSmallMaxN, 4));
   return cudaGetLastError();
 }
 
 cudaError_t launch_apply(int tcode, int nblocks, int nt, size_t smem, cudaStream_t st, const SmallDesc* descs,
                          const int* perm, void* V, const void* d, void* w, ChaseState* cst, const void* rot,
-                         const unsigned* hdr, const int* info, const int* scale_exp) {
+                         const unsigned* hdr, const int* info, const int* scale_exp, bool rows2) {
   if (nblocks <= 0) return cudaSuccess;
-  if (tcode == kF64)
-    k_apply<double><<<nblocks, nt, smem, st>>>(descs, perm, (double*)V, (const double*)d, (double*)w, cst,
-                                               (const double*)rot, hdr, info, scale_exp);
-  else
-    k_apply<float><<<nblocks, nt, smem, st>>>(descs, perm, (float*)V, (const float*)d, (float*)w, cst,
-                                              (const float*)rot, hdr, info, scale_exp);
+#define GLA_AP(T, R2)                                                                                         \
+  k_apply<T, R2><<<nblocks, nt, smem, st>>>(descs, perm, (T*)V, (const T*)d, (T*)w, cst, (const T*)rot, hdr, \
+                                            info, scale_exp)
+  if (tcode == kF64) {
+    if (rows2) GLA_AP(double, true);
+    else GLA_AP(double, false);
+  } else {
+    if (rows2) GLA_AP(float, true);
+    else GLA_AP(float, false);
+  }
+#undef GLA_AP
   return cudaGetLastError();
 }
 

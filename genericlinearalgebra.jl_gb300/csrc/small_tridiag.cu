@@ -37,10 +37,11 @@ __global__ void __launch_bounds__(256) k_tridiag(const SmallDesc* __restrict__ d
                                                  const Tin* __restrict__ A, int lower, T* __restrict__ dout,
                                                  T* __restrict__ eout, T* __restrict__ Qout, int* __restrict__ info,
                                                  ChaseState* __restrict__ cst, int* __restrict__ scale_exp,
-                                                 T* __restrict__ wout, T* __restrict__ qtmp) {
+                                                 T* __restrict__ wout, T* __restrict__ qtmp,
+                                                 T* __restrict__ rows2) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   tridiag_body<T, Tin, WANTQ, STEIN>(perm[blockIdx.x], smem_raw, descs, A, lower, dout, eout, Qout, info, cst,
-                                     scale_exp, wout, qtmp);
+                                     scale_exp, wout, qtmp, rows2);
 }
 
 size_t stein_tri_smem_bytes(int n) { return 512 + 4 * (2 * (size_t)n + stein_extra_words(n)); }
@@ -121,11 +122,11 @@ cudaError_t tridiag_kernels_init() {
 cudaError_t launch_tridiag(int tcode, bool wantq, int nblocks, int nt, size_t smem, cudaStream_t st,
                            const SmallDesc* descs, const int* perm, const void* A, int lower, void* d, void* e,
                            void* Q, int* info, ChaseState* cst, int* scale_exp, bool stein, void* w,
-                           void* qtmp) {
+                           void* qtmp, void* rows2) {
   if (nblocks <= 0) return cudaSuccess;
 #define GLA_TRI(T, Tin, WQ, ST)                                                                                 \
   k_tridiag<T, Tin, WQ, ST><<<nblocks, nt, smem, st>>>(descs, perm, (const Tin*)A, lower, (T*)d, (T*)e, (T*)Q, \
-                                                       info, cst, scale_exp, (T*)w, (T*)qtmp)
+                                                       info, cst, scale_exp, (T*)w, (T*)qtmp, (T*)rows2)
   if (tcode == kF64) {
     if (wantq) GLA_TRI(double, double, true, false);
     else GLA_TRI(double, double, false, false);

@@ -98,7 +98,8 @@ template <class T, class Tin, bool WANTQ, bool STEIN>
 GLA_DEV void tridiag_body(int mid, unsigned char* smem_raw, const SmallDesc* __restrict__ descs,
                           const Tin* __restrict__ A, int lower, T* __restrict__ dout, T* __restrict__ eout,
                           T* __restrict__ Qout, int* __restrict__ info, ChaseState* __restrict__ cst,
-                          int* __restrict__ scale_exp, T* __restrict__ wout, T* __restrict__ qtmp) {
+                          int* __restrict__ scale_exp, T* __restrict__ wout, T* __restrict__ qtmp,
+                          T* __restrict__ rows2 = nullptr) {
   const SmallDesc dsc = descs[mid];
   const int n = dsc.n;
   const int ld = stage_ld(n);
@@ -279,6 +280,33 @@ GLA_DEV void tridiag_body(int mid, unsigned char* smem_raw, const SmallDesc* __r
       uu[i] = di;
       ww[i] = ei;
     }
+  }
+  if (!WANTQ && rows2) {
+    // eigen2! (src/eigenSelfAdjoint.jl:633-644): only rows 1 and n of Q,
+    // [e_1'; e_n'] Q = rmul!(V, Q) (:62-80), in place of Array(Q): row 1 is
+    // e_1' (Q = diag(1, Qt)); row n is e_n' H_0 H_1 ... H_{n-3}, one
+    // reflector at a time (H_k on indices k+1.., v = [1; column k below its
+    // subdiagonal], tau_k). Stored 2 x n column-major at 2 w_off.
+    __syncthreads();
+    T* r = vv;  // the row being formed (n entries); uu holds the dot-product partials
+    for (int i = tid; i < n; i += NT) r[i] = (i == n - 1) ? T(1) : T(0);
+    __syncthreads();
+    for (int k = 0; k + 2 < n; k++) {
+      const T tau = taus[k];
+      if (tau == T(0)) continue;  // uniform: taus is shared
+      T part = T(0);
+      for (int i = k + 1 + tid; i < n; i += NT) part = fma(r[i], (i == k + 1) ? T(1) : S[(size_t)k * ld + i], part);
+      const T dot = block_sum(part, red);
+      const T f = tau * dot;
+      for (int i = k + 1 + tid; i < n; i += NT) r[i] = fma(-f, (i == k + 1) ? T(1) : S[(size_t)k * ld + i], r[i]);
+      __syncthreads();
+    }
+    T* R2 = rows2 + 2 * dsc.w_off;
+    for (int i = tid; i < n; i += NT) {
+      R2[2 * i] = (i == 0) ? T(1) : T(0);
+      R2[2 * i + 1] = r[i];
+    }
+    return;
   }
   if (!WANTQ) return;
   __syncthreads();

@@ -177,6 +177,15 @@ class Plan:
                                           C.c_void_p(info.data_ptr()), _stream_ptr(stream))
         return _lib.check(rc, "gla_plan_execute")
 
+    def execute_eigen2(self, A, w, V2, info, stream=None):
+        """eigen2 over the batch (gla_plan_execute_eigen2): eigenvalues and
+        rows 1 and n of each eigenvector matrix, 2 x n_b column-major at
+        twice the eigenvalue offset (V2 holds 2 w_elems). Device tensors."""
+        rc = _lib.load().gla_plan_execute_eigen2(self._h, C.c_void_p(A.data_ptr()), C.c_void_p(w.data_ptr()),
+                                                 C.c_void_p(V2.data_ptr()), C.c_void_p(info.data_ptr()),
+                                                 _stream_ptr(stream))
+        return _lib.check(rc, "gla_plan_execute_eigen2")
+
     def capture(self, A, w, V, info):
         """Capture execute(A, w, V, info) into a torch.cuda.CUDAGraph (plan made
         with graph=True). Replaying it re-solves whatever A holds at replay."""
@@ -656,9 +665,31 @@ def _tridiag_subset(T, irange, vl, vu, abstol):
 def eigen2(A, uplo="L", tol=None, precision="f64", alg="QL"):
     """eigen2 (src/eigenSelfAdjoint.jl:633-668): ascending eigenvalues and the
     FIRST and LAST rows of the eigenvector matrix (a 2 x n array; for n = 1
-    both rows are the single entry). The rows are those of eigen(A) on the
-    same input: the reference accumulates only these two rows of the
-    rotations, the device path forms the full matrix and keeps two rows."""
+    both rows are the single entry). Dense real input of order <= 128 in
+    FP64 or FP32 takes the reference's cheap form (gla_plan_execute_eigen2:
+    rows 1 and n of Q from the reflectors, the rotations replayed on two
+    rows); its rows agree with eigen(A)'s to rounding. Other input (a
+    SymTridiagonal, whose rows equal eigen's exactly, larger orders, the
+    refined precision) keeps two rows of eigen(A)."""
+    dense = not isinstance(A, (SymTridiagonal, QuaternionMatrix)) and not _is_complex(A)
+    if dense and precision in ("f64", "f32") and A.shape[0] == A.shape[1] and 1 <= A.shape[0] <= GLA_MAX_SMALL_N:
+        torch = _torch()
+        on_dev = _is_torch(A)
+        n = int(A.shape[0])
+        plan = Plan([n], precision=precision, jobz="V", uplo=uplo, tol=tol, alg=alg)
+        try:
+            dt = torch.float32 if precision == "f32" else torch.float64
+            dev = A.device if on_dev else torch.device("cuda")
+            Ad = plan.pack([A], device=dev).to(dt)
+            w = torch.empty(n, dtype=dt, device=dev)
+            V2 = torch.empty(2 * n, dtype=dt, device=dev)
+            info = torch.zeros(1, dtype=torch.int32, device=dev)
+            plan.execute_eigen2(Ad, w, V2, info)
+            _raise_for_info(info.cpu().numpy())
+        finally:
+            plan.close()
+        vecs = V2.reshape(n, 2).t()  # column-major 2 x n
+        return Eigen(w, vecs.clone()) if on_dev else Eigen(w.cpu().numpy(), vecs.cpu().numpy().copy())
     r = eigen(A, uplo=uplo, tol=tol, precision=precision, alg=alg)
     vals, vecs = r
     n = vecs.shape[0]

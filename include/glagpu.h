@@ -144,6 +144,18 @@ int gla_plan_arena_sizes(gla_plan_t plan, int64_t* a_elems, int64_t* w_elems);
 int gla_plan_execute(gla_plan_t plan, const void* A, void* w, void* V, int* info, void* stream);
 
 /*
+ * eigen2 (src/eigenSelfAdjoint.jl:633-644): the ascending eigenvalues and
+ * only rows 1 and n of the eigenvector matrix, the reference's cheap form:
+ * rows 1 and n of Q are formed from the reflectors (rmul!(V, Q) on a 2 x n V,
+ * :62-80) instead of Q itself, and the QL (or QR) rotations are replayed on
+ * those two rows only. V2: per matrix a 2 x n column-major block at twice
+ * its eigenvalue offset (2 sum_{c<b} n_c). Plans with jobz 'V' and
+ * precision GLA_PREC_F64 or GLA_PREC_F32 whose orders are all <= 128;
+ * others return GLA_ERR_UNSUPPORTED. Synchronization as gla_plan_execute.
+ */
+int gla_plan_execute_eigen2(gla_plan_t plan, const void* A, void* w, void* V2, int* info, void* stream);
+
+/*
  * Same, from and to HOST buffers: copies A in, runs, copies w, V and info
  * out, and synchronizes `stream` before returning. Uses plan-owned device
  * buffers (allocated on first use). Pinned host memory is fastest.
