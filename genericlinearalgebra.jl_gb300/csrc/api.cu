@@ -122,6 +122,7 @@ struct gla_plan_s {
   void* d_x32 = nullptr;  // FP32 eigenvectors (refined runs, or 'N' refined)
   void* d_w32 = nullptr;
   RefineWork rw;          // refinement scratch
+  bool refine_tc = true;  // the refinement's double-float products on the tensor cores
   void* d_vtmp = nullptr; // V target when the caller passes none
   void* d_qtmp = nullptr; // stein: Q of every matrix (float arena) while its tridiagonal is solved
   // host-execute buffers
@@ -214,7 +215,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     if (any_large && (flags & GLA_FLAG_GRAPH)) return -8;
   }
   if ((flags & ~(3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_TIMING | GLA_FLAG_GRAPH | GLA_FLAG_AUTOTUNE |
-                 GLA_FLAG_REFINE_QL | GLA_FLAG_F32_BISECT)) != 0 ||
+                 GLA_FLAG_REFINE_QL | GLA_FLAG_F32_BISECT | GLA_FLAG_REFINE_SIMT)) != 0 ||
       (flags & 3) > GLA_ALG_QR)
     return -8;
   GLA_CUDA(ensure_init());
@@ -232,6 +233,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->stein = (precision == GLA_PREC_F32_REFINED && !(flags & GLA_FLAG_REFINE_QL)) ||
              (precision == GLA_PREC_F32 && (flags & GLA_FLAG_F32_BISECT));
   p->persistent = p->stein && precision == GLA_PREC_F32_REFINED;
+  p->refine_tc = !(flags & GLA_FLAG_REFINE_SIMT);
   p->n.assign(n, n + batch);
 
   // ---- descriptors and offsets
@@ -387,7 +389,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     return -1000 - (int)err;
   }
   if (flags & GLA_FLAG_AUTOTUNE) {
-    int rc = autotune_plan(p, flags & (3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_REFINE_QL));
+    int rc = autotune_plan(p, flags & (3 | GLA_FLAG_SMALL_LOG | GLA_FLAG_REFINE_QL | GLA_FLAG_REFINE_SIMT));
     if (rc) {
       gla_plan_destroy(p);
       return rc;
@@ -520,7 +522,7 @@ int enqueue_refine(gla_plan_t p, int b, const void* A, int lower, void* Vout, vo
   const Bucket& bk = p->buckets[b];
   GLA_CUDA(launch_refine(&p->rw, bk.count, bk.nmax, st, p->d_desc, p->d_perm_bucket + bk.start, (const double*)A,
                          lower, (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats,
-                         p->d_cst));
+                         p->d_cst, p->refine_tc));
   return 0;
 }
 
@@ -591,7 +593,7 @@ int execute_persistent(gla_plan_t p, const void* A, void* w, void* Vout, int* in
   GLA_CUDA(launch_solve_refine(&p->rw, n, p->nmax, p->persist_grid, st, p->d_desc, p->d_perm_bucket, p->d_next,
                                (const double*)A, lower, (float*)p->d_d, (float*)p->d_e, (float*)p->d_x32, info,
                                p->d_cst, p->d_scale, (float*)p->d_w32, (float*)p->d_qtmp, (double*)Vout, (double*)w,
-                               p->d_stats));
+                               p->d_stats, p->refine_tc));
   p->mark(0, GLA_PHASE_TRIDIAG, 1, st);
   const int npass = p->graph ? kGraphPasses : kAsyncPasses;
   auto pass = [&]() -> int {
@@ -625,7 +627,8 @@ int execute_persistent(gla_plan_t p, const void* A, void* w, void* Vout, int* in
   p->last_passes = passes;
   p->mark(0, GLA_PHASE_REFINE, 0, st);
   GLA_CUDA(launch_refine(&p->rw, n, p->nmax, st, p->d_desc, p->d_perm_bucket, (const double*)A, lower,
-                         (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats, p->d_cst));
+                         (const float*)p->d_x32, (double*)Vout, (double*)w, info, p->d_scale, p->d_stats, p->d_cst,
+                         p->refine_tc));
   p->mark(0, GLA_PHASE_REFINE, 1, st);
   return 0;
 }
@@ -653,6 +656,7 @@ int plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, cudaS
   void* wq = refined ? p->d_w32 : w;
   const int* scale = refined ? p->d_scale : nullptr;
   void* Vout = p->jobz == 'V' ? V : p->d_vtmp;
+  if (refined) GLA_CUDA(cudaMemsetAsync(p->rw.err, 0, sizeof(int), st));
   if (p->persistent) return execute_persistent(p, A, w, Vout, info, st);
   const int nb = (int)p->buckets.size();
   GLA_CUDA(cudaEventRecord(p->fork, st));

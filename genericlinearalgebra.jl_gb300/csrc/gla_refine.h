@@ -23,6 +23,7 @@ struct RefineWork {
   float* E = nullptr;  // correction E
   float* J = nullptr;  // Jacobi scratch of cluster rotations (2 * a_elems)
   float* T = nullptr;  // FP32 product X E (a_elems)
+  int* err = nullptr;  // tensor-core wait error word (zeroed by each execute)
 };
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t w_elems, int64_t batch);
@@ -32,17 +33,19 @@ cudaError_t refine_kernels_init();
 constexpr int kRefinedInKernel = 2;
 
 // One CTA per matrix (perm[0..nblocks)); with cst, matrices already refined
-// by the persistent kernel are skipped.
+// by the persistent kernel are skipped. tc: the double-float products on the
+// tensor cores (tc_small.cuh), else on the FP32 pipe.
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
                           int* info, const int* scale_exp, unsigned long long* stats,
-                          const ChaseState* cst = nullptr);
+                          const ChaseState* cst = nullptr, bool tc = true);
 
 // The persistent FP32 + refinement solve of count matrices (order: largest
 // first) on grid CTAs; *next must be zero on entry.
 cudaError_t launch_solve_refine(const RefineWork* rw, int count, int nmax, int grid, cudaStream_t st,
                                 const SmallDesc* descs, const int* order, int* next, const double* A, int lower,
                                 float* d, float* e, float* X32, int* info, ChaseState* cst, int* scale_exp,
-                                float* w32, float* qtmp, double* V, double* w, unsigned long long* stats);
+                                float* w32, float* qtmp, double* V, double* w, unsigned long long* stats,
+                                bool tc = true);
 
 }  // namespace gla

@@ -18,9 +18,11 @@
 // FP32 after shifting by the cluster mean (its accuracy only needs to be
 // relative to the cluster's spread; the next iteration restores the rest).
 //
-// Arithmetic: the products X'X, AX, X'(AX) and X E are evaluated in
-// double-float arithmetic (df64.cuh) on the FP32 pipe, ~2^-47 relative per
-// operation; lam and the gaps in FP64.
+// Arithmetic: the products AX, X'(AX) and X'X are evaluated to double-float
+// accuracy, ~2^-47 relative, on the tcgen05 tensor cores (tc_small.cuh: the
+// Ozaki scheme with seven bf16 slices per operand) or, with
+// GLA_FLAG_REFINE_SIMT, in double-float arithmetic (df64.cuh) on the FP32
+// pipe; X E in FP32 (below); lam and the gaps in FP64.
 //
 // The first iteration exploits that X0 (the FP32 eigenvectors) holds exact
 // floats. The update X <- X + X E is evaluated in FP32: its rounding error
@@ -31,6 +33,7 @@
 #include "gla_launch.h"
 #include "gla_refine.h"
 #include "small_tridiag.cuh"
+#include "tc_small.cuh"
 #include "tile_gemm.cuh"
 
 namespace gla {
@@ -54,6 +57,7 @@ void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t)
   rw->E = reinterpret_cast<float*>(p + 7 * a_elems);
   rw->J = rw->E + a_elems;
   rw->T = rw->J + 2 * a_elems;
+  rw->err = reinterpret_cast<int*>(rw->T + a_elems);  // in the 4096-byte tail
 }
 
 GLA_DEV float block_sum_f(float v, float* red) {
@@ -124,11 +128,22 @@ GLA_DEV void jacobi_warp(int k, float* C, float* Z) {
   __syncwarp();
 }
 
-// The refinement of matrix mid by the whole CTA (kRT threads).
+// (i, j) = (idx mod n, idx div n) for idx < n^2 <= 2^14 by a float
+// reciprocal: the quotient (idx + 1/2)/n stays >= 1/(2n) away from integers,
+// far beyond the float rounding of the product.
+GLA_DEV void split_idx(int idx, int n, float inv_n, int& i, int& j) {
+  j = (int)(((float)idx + 0.5f) * inv_n);
+  i = idx - j * n;
+}
+
+// The refinement of matrix mid by the whole CTA (kRT threads). TC: the three
+// double-float products on the tensor cores through tcx (set up by the
+// kernel), else on the FP32 pipe.
+template <bool TC>
 GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const double* __restrict__ A, int lower,
                          const float* __restrict__ X32, double* __restrict__ Vout, double* __restrict__ wout,
                          int* __restrict__ info, const int* __restrict__ scale_exp, const RefineWork& rw,
-                         unsigned long long* __restrict__ stats) {
+                         unsigned long long* __restrict__ stats, tcs::Ctx* tcx) {
   __shared__ df64 As[16 * kTP];
   __shared__ df64 Bs2[16 * kTP];
   __shared__ double lam[kSmallMaxN];
@@ -137,10 +152,14 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
   __shared__ unsigned long long keys[kSmallMaxN];
   __shared__ int rank[kSmallMaxN], ord[kSmallMaxN], cstart[kSmallMaxN + 1], cid[kSmallMaxN];
   __shared__ int ncl_s, flag_s, big_s;
+  __shared__ unsigned brk_mask[kRT / 32];
+  __shared__ double gred[kRT / 32];
   __shared__ double gmin_s, lmax_s;
+  __shared__ int expA[TC ? kSmallMaxN : 1], expX[TC ? kSmallMaxN : 1], expY[TC ? kSmallMaxN : 1];
   float* Bsf = reinterpret_cast<float*>(Bs2);
   const SmallDesc dsc = descs[mid];
   const int n = dsc.n, tid = threadIdx.x;
+  const float inv_n = 1.f / (float)n;
   const size_t ao = dsc.a_off;
   const double* Ag = A + ao;
   double* V = Vout ? Vout + ao : nullptr;
@@ -165,13 +184,15 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
   float* Asf = reinterpret_cast<float*>(As);
   float an2 = 0.f;
   for (int idx = tid; idx < n * n; idx += kRT) {
-    const int i = idx % n, k = idx / n;
+    int i, k;
+    split_idx(idx, n, inv_n, i, k);
     const double a = (lower ? (i >= k) : (i <= k)) ? Ag[idx] : Ag[(size_t)i * n + k];
     const df64 ad = df_from(ldexp(a, -se));
     A2[idx] = ad;
     an2 = fmaf(ad.hi, ad.hi, an2);
   }
   const float anorm = sqrtf(block_sum_f(an2, red));
+  if (TC) tcs::col_exps(n, A2, expA);  // A is symmetric: its row exponents
   const df64 zero = df_make(0.f, 0.f);
   auto zinit = [&](int, int) { return zero; };
   df64* cS = S0;
@@ -179,7 +200,41 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
   bool converged = false;
   float emax_prev = 1e30f;
   for (int it = 0; it < kMaxRefineIters; it++) {
-    if (it == 0) {
+    if (TC) {
+      // Y = A X; S = X'Y and R = I - X'X (upper triangles, mirrored); on the
+      // first iteration X is X0, the FP32 eigenvectors (exact floats)
+      df64* Sd = it == 0 ? S0 : S;
+      df64* Rd = it == 0 ? R0 : R;
+      const df64* Xc = X;
+      auto xk = [&](int k, int j) { return it == 0 ? df_make(X0[(size_t)j * n + k], 0.f) : Xc[(size_t)j * n + k]; };
+      auto xt = [&](int i, int k) { return it == 0 ? df_make(X0[(size_t)i * n + k], 0.f) : Xc[(size_t)i * n + k]; };
+      if (it == 0)
+        tcs::col_exps(n, X0, expX);
+      else
+        tcs::col_exps(n, Xc, expX);
+      tcs::gemm(
+          *tcx, n, expA, expX, [&](int i, int k) { return A2[(size_t)k * n + i]; }, xk,
+          [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, false);
+      tcs::col_exps(n, Y, expY);
+      tcs::gemm(
+          *tcx, n, expX, expY, xt, [&](int k, int j) { return Y[(size_t)j * n + k]; },
+          [&](int i, int j, df64 v) {
+            Sd[(size_t)j * n + i] = v;
+            Sd[(size_t)i * n + j] = v;
+          },
+          true);
+      tcs::gemm(
+          *tcx, n, expX, expX, xt, xk,
+          [&](int i, int j, df64 v) {
+            const df64 r = df_add(df_make(i == j ? 1.f : 0.f, 0.f), df_neg(v));
+            Rd[(size_t)j * n + i] = r;
+            Rd[(size_t)i * n + j] = r;
+          },
+          true);
+      if (!tcs::ok(*tcx)) break;  // a tensor-core wait ran out: reported as not converged
+      cS = Sd;
+      cR = Rd;
+    } else if (it == 0) {
       // ---- first iteration on the FP32 eigenvectors X0 (exact floats)
       tile_gemm_df<float>(
           n, [&](int i, int k) { return A2[(size_t)k * n + i]; }, [&](int k, int j) { return X0[(size_t)j * n + k]; },
@@ -239,7 +294,8 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
     __syncthreads();
     float sd2 = 0.f, r2 = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
-      const int i = idx % n, j = idx / n;
+      int i, j;
+      split_idx(idx, n, inv_n, i, j);
       const float sv = (i == j) ? (float)(df_to(cS[idx]) - lam[i]) : cS[idx].hi;
       sd2 = fmaf(sv, sv, sd2);
       r2 = fmaf(cR[idx].hi, cR[idx].hi, r2);
@@ -254,27 +310,50 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
       ord[rk] = i;
     }
     __syncthreads();
-    if (tid == 0) {
-      int nc = 0, big = 0;
+    // clusters: runs of the sorted lam with consecutive gaps <= delta.
+    // Sorted position r > 0 starts a new cluster when its gap exceeds delta;
+    // its cluster id is the number of such starts at positions 1 .. r
+    // (warp ballots), and gmin the smallest gap between clusters.
+    {
+      const int lane = tid & 31, wid = tid >> 5;
+      double g = 1e300;
+      bool b = false;
+      if (tid >= 1 && tid < n) {
+        const double gg = lam[ord[tid]] - lam[ord[tid - 1]];
+        b = (float)gg > delta;
+        if (b) g = gg;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, b);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) g = fmin(g, __shfl_xor_sync(0xffffffffu, g, o));
+      if (lane == 0) {
+        brk_mask[wid] = m;
+        gred[wid] = g;
+      }
+      __syncthreads();
+      int before = 0, nb = 0;
       double gmin = 1e300;
-      lmax_s = fmax(fabs(lam[ord[0]]), fabs(lam[ord[n - 1]]));  // ||A||_2 of the scaled matrix
-      cstart[0] = 0;
-      for (int r = 1; r < n; r++) {
-        const double g = lam[ord[r]] - lam[ord[r - 1]];
-        if ((float)g > delta) {
-          cstart[++nc] = r;
-          gmin = fmin(gmin, g);
-        }
+      for (int w = 0; w < kRT / 32; w++) {
+        const int pc = __popc(brk_mask[w]);
+        if (w < wid) before += pc;
+        nb += pc;
+        gmin = fmin(gmin, gred[w]);
       }
-      cstart[++nc] = n;
-      for (int c = 0; c < nc; c++) {
-        big |= (cstart[c + 1] - cstart[c]) >= 2;
-        for (int r = cstart[c]; r < cstart[c + 1]; r++) cid[ord[r]] = c;
+      if (tid < n) {
+        const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+        const int c = before + __popc(m & upto);
+        cid[ord[tid]] = c;
+        if (b) cstart[c] = tid;
       }
-      ncl_s = nc;
-      flag_s = 0;
-      gmin_s = gmin;
-      big_s = big;
+      if (tid == 0) {
+        cstart[0] = 0;
+        cstart[nb + 1] = n;
+        ncl_s = nb + 1;
+        flag_s = 0;
+        gmin_s = gmin;
+        big_s = nb + 1 < n;  // some cluster holds two or more
+        lmax_s = fmax(fabs(lam[ord[0]]), fabs(lam[ord[n - 1]]));  // ||A||_2 of the scaled matrix
+      }
     }
     __syncthreads();
     // E: the Newton-type correction between clusters; inside a cluster (its
@@ -289,7 +368,8 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
     const float tfloor = (float)(1e-14 * lmax_s);
     float emax = 0.f, rmax = 0.f;
     for (int idx = tid; idx < n * n; idx += kRT) {
-      const int i = idx % n, j = idx / n;
+      int i, j;
+      split_idx(idx, n, inv_n, i, j);
       const float rhalf = 0.5f * (cR[idx].hi + cR[idx].lo);
       rmax = fmaxf(rmax, fabsf(rhalf));
       float e = rhalf;
@@ -444,8 +524,13 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
     }
 }
 
+// Dynamic shared memory of the refinement kernels: the tensor-core slabs,
+// or, in the persistent kernel, the tridiagonalisation's layout if larger.
+size_t refine_smem_bytes(bool tc) { return tc ? (size_t)tcs::kSmem : 0; }
+
 // One CTA per matrix; a matrix the persistent kernel below already refined
 // (ChaseState.applied == kRefinedInKernel) is skipped.
+template <bool TC>
 __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ perm,
                                                 const double* __restrict__ A, int lower,
                                                 const float* __restrict__ X32, double* __restrict__ Vout,
@@ -453,9 +538,14 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
                                                 const int* __restrict__ scale_exp, RefineWork rw,
                                                 unsigned long long* __restrict__ stats,
                                                 const ChaseState* __restrict__ cst) {
+  extern __shared__ __align__(128) unsigned char rsm[];
+  __shared__ tcs::Shared tsh;
   const int mid = perm[blockIdx.x];
-  if (cst && cst[mid].applied == kRefinedInKernel) return;
-  refine_body(mid, descs, A, lower, X32, Vout, wout, info, scale_exp, rw, stats);
+  if (cst && cst[mid].applied == kRefinedInKernel) return;  // (uniform) before any TMEM is taken
+  tcs::Ctx tcx;
+  if (TC) tcs::setup(tcx, &tsh, rsm, rw.err);
+  refine_body<TC>(mid, descs, A, lower, X32, Vout, wout, info, scale_exp, rw, stats, &tcx);
+  if (TC) tcs::teardown(tcx);
 }
 
 // The whole FP32 + refinement solve of a batch in one persistent launch:
@@ -465,6 +555,8 @@ __global__ void __launch_bounds__(kRT) k_refine(const SmallDesc* __restrict__ de
 // FP64 accuracy (refine_body), and takes the next. A matrix the FP32 solver
 // leaves to the QL chase (or with non-finite input) is left to the chase,
 // rotation-replay and refinement kernels that follow (they skip the rest).
+// The CTA holds its TMEM (256 columns; two CTAs per SM) for its lifetime.
+template <bool TC>
 __global__ void __launch_bounds__(kRT, 2)
     k_solve_refine(const SmallDesc* __restrict__ descs, const int* __restrict__ order, int count,
                    int* __restrict__ next, const double* __restrict__ A, int lower, float* __restrict__ d,
@@ -472,48 +564,71 @@ __global__ void __launch_bounds__(kRT, 2)
                    ChaseState* __restrict__ cst, int* __restrict__ scale_exp, float* __restrict__ w32,
                    float* __restrict__ qtmp, double* __restrict__ Vout, double* __restrict__ wout, RefineWork rw,
                    unsigned long long* __restrict__ stats) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ int s_idx;
+  __shared__ tcs::Shared tsh;
+  tcs::Ctx tcx;
+  if (TC) tcs::setup(tcx, &tsh, smem_raw, rw.err);
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_idx = atomicAdd(next, 1);
     __syncthreads();
     const int idx = s_idx;
-    if (idx >= count) return;
+    if (idx >= count) break;
     const int mid = order[idx];
     tridiag_body<float, double, true, true>(mid, smem_raw, descs, A, lower, d, e, X32, info, cst, scale_exp, w32,
                                             qtmp);
     __syncthreads();
     if (cst[mid].applied == 1) {  // solved in FP32 (small_stein.cuh)
-      refine_body(mid, descs, A, lower, X32, Vout, wout, info, scale_exp, rw, stats);
+      refine_body<TC>(mid, descs, A, lower, X32, Vout, wout, info, scale_exp, rw, stats, &tcx);
       __syncthreads();
       if (threadIdx.x == 0) cst[mid].applied = kRefinedInKernel;
     }
   }
+  if (TC) tcs::teardown(tcx);
 }
 
+namespace {
+size_t solve_refine_smem(int nmax, bool tc) {
+  return std::max(tridiag_smem_bytes(nmax, kRT, 4), refine_smem_bytes(tc));
+}
+}  // namespace
+
 cudaError_t refine_kernels_init() {
-  return cudaFuncSetAttribute(k_solve_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tridiag_smem_bytes(kSmallMaxN, kRT, 4));
+  cudaFuncSetAttribute(k_solve_refine<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)solve_refine_smem(kSmallMaxN, false));
+  cudaFuncSetAttribute(k_solve_refine<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)solve_refine_smem(kSmallMaxN, true));
+  cudaFuncSetAttribute(k_refine<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)refine_smem_bytes(true));
+  return cudaGetLastError();
 }
 
 cudaError_t launch_refine(const RefineWork* rw, int nblocks, int nmax, cudaStream_t st, const SmallDesc* descs,
                           const int* perm, const double* A, int lower, const float* X32, double* V, double* w,
-                          int* info, const int* scale_exp, unsigned long long* stats, const ChaseState* cst) {
+                          int* info, const int* scale_exp, unsigned long long* stats, const ChaseState* cst,
+                          bool tc) {
   if (nblocks <= 0) return cudaSuccess;
   (void)nmax;
-  k_refine<<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw, stats, cst);
+  if (tc)
+    k_refine<true><<<nblocks, kRT, refine_smem_bytes(true), st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp,
+                                                                  *rw, stats, cst);
+  else
+    k_refine<false><<<nblocks, kRT, 0, st>>>(descs, perm, A, lower, X32, V, w, info, scale_exp, *rw, stats, cst);
   return cudaGetLastError();
 }
 
 cudaError_t launch_solve_refine(const RefineWork* rw, int count, int nmax, int grid, cudaStream_t st,
                                 const SmallDesc* descs, const int* order, int* next, const double* A, int lower,
                                 float* d, float* e, float* X32, int* info, ChaseState* cst, int* scale_exp,
-                                float* w32, float* qtmp, double* V, double* w, unsigned long long* stats) {
+                                float* w32, float* qtmp, double* V, double* w, unsigned long long* stats, bool tc) {
   if (count <= 0) return cudaSuccess;
-  k_solve_refine<<<grid, kRT, tridiag_smem_bytes(nmax, kRT, 4), st>>>(descs, order, count, next, A, lower, d, e, X32,
-                                                                      info, cst, scale_exp, w32, qtmp, V, w, *rw,
-                                                                      stats);
+  const size_t smem = solve_refine_smem(nmax, tc);
+  if (tc)
+    k_solve_refine<true><<<grid, kRT, smem, st>>>(descs, order, count, next, A, lower, d, e, X32, info, cst,
+                                                  scale_exp, w32, qtmp, V, w, *rw, stats);
+  else
+    k_solve_refine<false><<<grid, kRT, smem, st>>>(descs, order, count, next, A, lower, d, e, X32, info, cst,
+                                                   scale_exp, w32, qtmp, V, w, *rw, stats);
   return cudaGetLastError();
 }
 

@@ -115,16 +115,20 @@ GLA_DEV void tridiag_body(int mid, unsigned char* smem_raw, const SmallDesc* __r
 
   const Tin* Ag = A + dsc.a_off;
   // ---- load the referenced triangle (mirroring 'U' into 'L'), check finiteness
+  // (flat over the n^2 entries, so that every thread has several
+  // independent loads in flight; column j = idx / n by a float reciprocal,
+  // exact for idx < 2^14: the quotient's fraction stays >= 1/(2n) from 1)
   int bad = 0;
   unsigned long long amax = 0;
-  for (int j = 0; j < n; j++) {
-    for (int i = tid; i < n; i += NT) {
-      if (lower ? (i >= j) : (i <= j)) {
-        Tin v = Ag[(size_t)j * n + i];
-        bad |= !isfinite(v);
-        unsigned long long b = AbsBits<Tin>::get(v);
-        amax = b > amax ? b : amax;
-      }
+  const float inv_n = 1.f / (float)n;
+#pragma unroll 4
+  for (int idx = tid; idx < n * n; idx += NT) {
+    const int j = (int)(((float)idx + 0.5f) * inv_n), i = idx - j * n;
+    if (lower ? (i >= j) : (i <= j)) {
+      Tin v = Ag[idx];
+      bad |= !isfinite(v);
+      unsigned long long b = AbsBits<Tin>::get(v);
+      amax = b > amax ? b : amax;
     }
   }
   bad = __syncthreads_or(bad);
@@ -162,14 +166,14 @@ GLA_DEV void tridiag_body(int mid, unsigned char* smem_raw, const SmallDesc* __r
     }
     if (tid == 0) scale_exp[mid] = sexp;
   }
-  for (int j = 0; j < n; j++) {
-    for (int i = tid; i < n; i += NT) {
-      if (lower ? (i >= j) : (i <= j)) {
-        Tin v = Ag[(size_t)j * n + i];
-        T t = (sizeof(Tin) != sizeof(T)) ? (T)ldexp((double)v, -sexp) : (T)v;
-        if (lower) S[j * ld + i] = t;
-        else S[i * ld + j] = t;
-      }
+#pragma unroll 4
+  for (int idx = tid; idx < n * n; idx += NT) {
+    const int j = (int)(((float)idx + 0.5f) * inv_n), i = idx - j * n;
+    if (lower ? (i >= j) : (i <= j)) {
+      Tin v = Ag[idx];
+      T t = (sizeof(Tin) != sizeof(T)) ? (T)ldexp((double)v, -sexp) : (T)v;
+      if (lower) S[j * ld + i] = t;
+      else S[i * ld + j] = t;
     }
   }
   __syncthreads();

@@ -106,10 +106,13 @@ class Plan:
     refine_ql: for "f32_refined", run the FP32 stage with the QL chase instead
     of the per-eigenvalue solver (GLA_FLAG_REFINE_QL). bisect: for "f32", use
     that per-eigenvalue solver instead of the QL chase (GLA_FLAG_F32_BISECT).
+    refine_simt: for "f32_refined", the refinement's double-float products on
+    the FP32 pipe instead of the tensor cores (GLA_FLAG_REFINE_SIMT).
     """
 
     def __init__(self, ns, precision="f64", jobz="V", uplo="L", tol=None, alg="QL", small_log=False,
-                 timing=False, graph=False, autotune=False, refine_ql=False, bisect=False):
+                 timing=False, graph=False, autotune=False, refine_ql=False, bisect=False,
+                 refine_simt=False):
         L = _lib.load()
         ns = np.ascontiguousarray(np.asarray(ns, dtype=np.int64))
         if (ns < 0).any() or (ns > GLA_MAX_N).any():
@@ -122,7 +125,7 @@ class Plan:
         flags = (GLA_ALG_QR if alg == "QR" else GLA_ALG_QL) | (_lib.GLA_FLAG_SMALL_LOG if small_log else 0) | \
             (_lib.GLA_FLAG_TIMING if timing else 0) | (_lib.GLA_FLAG_GRAPH if graph else 0) | \
             (_lib.GLA_FLAG_AUTOTUNE if autotune else 0) | (_lib.GLA_FLAG_REFINE_QL if refine_ql else 0) | \
-            (_lib.GLA_FLAG_F32_BISECT if bisect else 0)
+            (_lib.GLA_FLAG_F32_BISECT if bisect else 0) | (_lib.GLA_FLAG_REFINE_SIMT if refine_simt else 0)
         self.graph = graph
         h = C.c_void_p()
         _lib.check(L.gla_plan_create(C.byref(h), PRECISIONS[precision], jobz.encode(), uplo.encode(), len(ns),

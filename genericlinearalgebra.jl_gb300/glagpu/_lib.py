@@ -26,6 +26,7 @@ GLA_FLAG_GRAPH = 16
 GLA_FLAG_AUTOTUNE = 32
 GLA_FLAG_REFINE_QL = 64
 GLA_FLAG_F32_BISECT = 128
+GLA_FLAG_REFINE_SIMT = 256
 PHASES = ("tridiag", "chase", "apply", "refine")
 COUNTERS = ("rotations", "sweeps", "row_rotations", "refine_n3", "passes")
 

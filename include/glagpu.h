@@ -83,6 +83,12 @@ extern "C" {
  * n eps(Float32). The FP32 + refinement path uses it for its internal FP32
  * solves (cluster matrices, divide-and-conquer leaves). */
 #define GLA_FLAG_F32_BISECT 128
+/* Flag bit (GLA_PREC_F32_REFINED, orders <= 128): evaluate the refinement's
+ * double-float products (A X, X'(A X), X'X) on the FP32 pipe in double-float
+ * arithmetic instead of the default tcgen05 tensor-core Ozaki products (seven
+ * bf16 slices per operand, exact integer accumulation). Both are ~2^-47
+ * relative; results agree within the refinement's 1e-13 bounds. */
+#define GLA_FLAG_REFINE_SIMT 256
 
 /* Phases reported by gla_plan_phase_times. */
 #define GLA_PHASE_TRIDIAG 0 /* symtri! + Array(Q)          */
