@@ -194,16 +194,17 @@ struct SlabRegs {
 GLA_DEV int cm_row(int cm, int lane) { return ((cm >> 2) << 3) + (lane >> 2); }
 GLA_DEV int cm_k(int cm, int lane) { return ((cm & 3) << 3) + ((lane & 3) << 1); }
 
+// rows: the rows of P this pass needs (the rest are zero slices).
 template <class LP, class LQ>
-GLA_DEV void slab_load(SlabRegs& g, int n, int k0, int j0, const LP& lp, const LQ& lq) {
+GLA_DEV void slab_load(SlabRegs& g, int n, int rows, int k0, int j0, const LP& lp, const LQ& lq) {
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const df64 zero = df_make(0.f, 0.f);
 #pragma unroll
   for (int t = 0; t < kPPairs; t++) {
     const int cm = wid + 8 * t;
     const int r = cm_row(cm, lane), k = k0 + cm_k(cm, lane);
-    g.p[t][0] = (r < n && k < n) ? lp(r, k) : zero;
-    g.p[t][1] = (r < n && k + 1 < n) ? lp(r, k + 1) : zero;
+    g.p[t][0] = (r < rows && k < n) ? lp(r, k) : zero;
+    g.p[t][1] = (r < rows && k + 1 < n) ? lp(r, k + 1) : zero;
   }
 #pragma unroll
   for (int t = 0; t < kQPairs; t++) {
@@ -214,7 +215,7 @@ GLA_DEV void slab_load(SlabRegs& g, int n, int k0, int j0, const LP& lp, const L
   }
 }
 
-GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int j0, const int* ea, const int* eb) {
+GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int rows, int j0, const int* ea, const int* eb) {
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* sa = c.slabs;
   unsigned char* sb = c.slabs + kS * kABlk;
@@ -223,9 +224,9 @@ GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int j0, const in
     const int cm = wid + 8 * t;
     const int r = cm_row(cm, lane), kk = cm_k(cm, lane);
     unsigned char* dst = sa + oz::tile_off(r, kk);
-    if (r < n) {
+    if (r < rows) {
       slice7x2(g.p[t][0], g.p[t][1], ea[r], dst, kABlk);
-    } else {  // padding rows of the M = 128 operand
+    } else {  // rows of the M = 128 operand not needed (or beyond n)
 #pragma unroll
       for (int q = 0; q < kS; q++) *reinterpret_cast<uint32_t*>(dst + q * kABlk) = 0u;
     }
@@ -258,11 +259,13 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
   const int nks = (n + kKS - 1) / kKS;
   SlabRegs g;
   for (int j0 = 0; j0 < n; j0 += kNT) {
-    slab_load(g, n, 0, j0, lp, lq);
+    // stored rows: all, or (upper) i <= j < j0 + 32
+    const int rows = upper ? min(n, j0 + kNT) : n;
+    slab_load(g, n, rows, 0, j0, lp, lq);
     for (int q = 0; q < nks; q++) {
       // the MMAs of the previous slab read the buffers: wait for them
       if (q > 0 && !wait_mma(c)) return false;
-      slab_slice(g, c, n, j0, ea, eb);
+      slab_slice(g, c, n, rows, j0, ea, eb);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();
       if (tid == 0) {
@@ -283,7 +286,7 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
         oz::mma_commit(&c.sh->bar);
       }
       // the next slab's loads overlap these MMAs
-      if (q + 1 < nks) slab_load(g, n, (q + 1) * kKS, j0, lp, lq);
+      if (q + 1 < nks) slab_load(g, n, rows, (q + 1) * kKS, j0, lp, lq);
     }
     if (!wait_mma(c)) return false;
     asm volatile("tcgen05.fence::after_thread_sync;");
