@@ -41,7 +41,7 @@ for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
 METRIC = "eigh/s (batch n≤128) & n=4096 time at 1e-13 resid: FP32+refine vs FP64 GPU"
 # DRAM bytes (read + write) of the refinement in one step of the 1024-matrix
 # workload (ncu dram__bytes_read.sum + dram__bytes_write.sum)
-REFINE_DRAM_BYTES_PER_1024 = 281.7e6
+REFINE_DRAM_BYTES_PER_1024 = 685.5e6
 BATCH = 4096
 NLO, NHI = 8, 128
 SEED = 2
@@ -85,23 +85,27 @@ def launches_per_step(n_buckets, passes, refined, graph):
     return n_buckets * (1 + 2 * passes + (1 if graph else 0))
 
 
-def refine_roofline(achieved, peak_ops, batch):
+def refine_roofline(achieved, peak, batch, fp32):
     """k_solve_refine, the persistent kernel that runs (almost) the whole
-    batched refined step: the FP32 tridiagonalisation and tridiagonal solve,
-    then the double-float Ogita-Aishima refinement, both on the FP32 pipe.
-    achieved = FP32-pipe operations per second over the kernel's time (CUDA
-    events on the execute's stream; see run_ours); peak = the FP32 FMA rate
-    of cuBLAS SGEMM measured in this run. traffic: DRAM bytes of one step
-    of the 1024-matrix case (same order distribution), from an ncu capture,
-    scaled by the matrix count; the algorithmic bytes are ~20 sum(n^2) =
-    0.48 GB per step, the rest is the per-matrix double-float scratch of
-    the refinement (56 n^2 bytes) that does not stay in L2."""
-    return {"kernel": "k_solve_refine", "bound": "fp32", "achieved": achieved, "peak": peak_ops,
-            "unit": "T FP32 ops/s",
-            "frac": (achieved / peak_ops) if peak_ops else None,
+    batched refined step. Its tensor-core work: the refinement's three
+    double-float products per iteration (A X, X'(A X), X'X), each 28 bf16
+    slice products of 2 n^3 (the Ozaki scheme, seven slices per operand),
+    i.e. 168 n^3 bf16 flops per matrix and iteration (the plan's refine_n3
+    counter sums n^3 over matrices and iterations). achieved = those flops
+    over the kernel's time (CUDA events on the execute's stream, the plan's
+    "tridiag" phase); peak = MEASURED_PEAKS.json bf16 (burst). The kernel is
+    latency-bound (per-column barriers of the FP32 reduction, the slicing),
+    so the fraction is small by construction; fp32 gives its FP32-pipe work
+    (reduction, Q, X = QY, X E) against the SGEMM FMA rate of this run.
+    traffic: DRAM bytes of one launch over the first 1024 workload matrices
+    (same order distribution), from an ncu capture, scaled by the matrix
+    count; the algorithmic bytes are ~20 sum(n^2) = 0.48 GB per step, the
+    rest is the per-matrix double-float scratch of the refinement (56 n^2
+    bytes) that does not stay in L2."""
+    return {"kernel": "k_solve_refine", "bound": "tensor", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
             "traffic": REFINE_DRAM_BYTES_PER_1024 * batch / 1024 if REFINE_DRAM_BYTES_PER_1024 else None,
-            "peak_source": "measured in this run: cuBLAS SGEMM 8192^3, FMA rate (FP32 pipe); "
-                           "MEASURED_PEAKS.json has only HBM and bf16 peaks"}
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)", "fp32_pipe": fp32}
 
 
 def replica_seed(rank):
@@ -401,18 +405,21 @@ def run_ours(args):
         c = H["counters"]
         ns3 = float((ns.astype(np.float64) ** 3).sum())
         # Roofline of the refined step's dominant kernel, the persistent
-        # k_solve_refine (its time is the plan's "tridiag" phase): FP32-pipe
-        # operations per second, counted as 13 instructions per double-float
-        # multiply-add of the refinement (TwoProduct 2, TwoSum 6, 2 adds,
-        # QuickTwoSum 3) times ~3 n^3 multiply-adds per iteration (A X,
-        # X'(AX), X'X as symmetric halves, X E), plus the FP32 multiply-adds
-        # of the reduction, Q and X = Q Y ((4/3 + 4/3 + 2) n^3 / 2); peak = the
-        # FP32 FMA rate of cuBLAS SGEMM measured in this run (TFLOP/s / 2).
+        # k_solve_refine (its time is the plan's "tridiag" phase): bf16
+        # tensor flops of the refinement's sliced products (refine_roofline),
+        # and beside them its FP32-pipe flops: the reduction, Q and X = QY
+        # ((4/3 + 4/3 + 2) n^3) and X E (2 n^3 per iteration) against the
+        # SGEMM rate measured in this run.
         sg = measured_sgemm_tflops(torch)
         fused_ms = ph.get("tridiag", 0.0)
-        ops = 13.0 * 3.0 * c["refine_n3"] + (4.0 / 3.0 + 4.0 / 3.0 + 2.0) / 2.0 * ns3
-        achieved = ops / (fused_ms * 1e-3) / 1e12 if fused_ms > 0 else 0.0
-        peak_ops = sg / 2.0
+        sec = fused_ms * 1e-3
+        tflops = 168.0 * c["refine_n3"] / sec / 1e12 if sec > 0 else 0.0
+        f32_flops = (4.0 / 3.0 + 4.0 / 3.0 + 2.0) * ns3 + 2.0 * c["refine_n3"]
+        f32_ach = f32_flops / sec / 1e12 if sec > 0 else 0.0
+        mp = measured_peaks_file()
+        bf16_peak = (mp or {}).get("bf16_tflops")
+        fp32 = {"achieved": f32_ach, "peak": sg, "unit": "TFLOP/s", "frac": (f32_ach / sg) if sg else None,
+                "peak_source": "measured in this run: cuBLAS SGEMM 8192^3"}
         cpu = cpu_baseline(ns, mats)
         lapack = lapack_baseline(ns, mats)
         line = {
@@ -426,13 +433,14 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32 solve + double-float (f32 pair) refinement" if hp == "f32_refined" else "f64",
+            "dtype": ("f32 solve + refinement with double-float (f32 pair) accuracy: bf16-slice tensor-core "
+                      "products (Ozaki), f32 SIMT elsewhere") if hp == "f32_refined" else "f64",
             "data": "synthetic (seeded GOE)",
             "config": {"workload": f"batched eigen!(Hermitian): {len(ns)} GOE matrices, n~U[{NLO},{NHI}], seed {SEED}",
                        "path": hp, "batch": len(ns), "sum_n": int(ns.sum()), "sum_n3": ns3,
                        "l2": "inputs larger than L2 (191 MB FP64 arena)", "parallelism": f"replicas x{ws}",
                        "timing": "CUDA-graph replay of the whole batched solve (plan with GLA_FLAG_GRAPH)"},
-            "roofline": refine_roofline(achieved, peak_ops, len(ns)),
+            "roofline": refine_roofline(tflops, bf16_peak, len(ns), fp32),
             "roofline_large": large_roofline(large, measured_peaks_file()),
             "fp64_dgemm_tflops_measured": peak,
             "cpu_baseline": cpu,

@@ -734,6 +734,33 @@ int gla_plan_execute(gla_plan_t p, const void* A, void* w, void* V, int* info, v
   return plan_execute(p, A, w, V, info, (cudaStream_t)stream);
 }
 
+}  // extern "C"
+
+namespace {
+// Device staging of the _host entry points: all four buffers, or none (a
+// later call retries). V also holds the 2 x n row blocks of eigen2.
+int ensure_staging(gla_plan_t p) {
+  if (p->h_info) return 0;
+  const size_t ioe = p->io_elem();
+  const size_t abytes = ioe * std::max<int64_t>(p->a_elems, 1), wbytes = ioe * std::max<int64_t>(p->w_elems, 1);
+  cudaError_t e = cudaMalloc(&p->h_A, abytes);
+  if (e == cudaSuccess) e = cudaMalloc(&p->h_w, wbytes);
+  if (e == cudaSuccess) e = cudaMalloc(&p->h_V, p->jobz == 'V' ? std::max(abytes, 2 * wbytes) : 16);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p->h_info, sizeof(int) * std::max<int64_t>(p->batch, 1));
+  if (e != cudaSuccess) {
+    cudaFree(p->h_A);
+    cudaFree(p->h_w);
+    cudaFree(p->h_V);
+    p->h_A = p->h_w = p->h_V = nullptr;
+    p->h_info = nullptr;
+    return -1000 - (int)e;
+  }
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
 int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host,
                           void* stream) {
   if (!p) return -1;
@@ -743,21 +770,7 @@ int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* 
   if (!info_host && p->batch) return -5;
   cudaStream_t st = (cudaStream_t)stream;
   const size_t ioe = p->io_elem();
-  const size_t abytes = ioe * std::max<int64_t>(p->a_elems, 1), wbytes = ioe * std::max<int64_t>(p->w_elems, 1);
-  if (!p->h_info) {  // all four staging buffers, or none (a later call retries)
-    cudaError_t e = cudaMalloc(&p->h_A, abytes);
-    if (e == cudaSuccess) e = cudaMalloc(&p->h_w, wbytes);
-    if (e == cudaSuccess) e = cudaMalloc(&p->h_V, p->jobz == 'V' ? abytes : 16);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&p->h_info, sizeof(int) * std::max<int64_t>(p->batch, 1));
-    if (e != cudaSuccess) {
-      cudaFree(p->h_A);
-      cudaFree(p->h_w);
-      cudaFree(p->h_V);
-      p->h_A = p->h_w = p->h_V = nullptr;
-      p->h_info = nullptr;
-      return -1000 - (int)e;
-    }
-  }
+  if (int rs = ensure_staging(p)) return rs;
   GLA_CUDA(cudaMemcpyAsync(p->h_A, A_host, ioe * p->a_elems, cudaMemcpyHostToDevice, st));
   int rc = plan_execute(p, p->h_A, p->h_w, p->h_V, p->h_info, st);
   if (rc) return rc;
@@ -821,6 +834,29 @@ int gla_plan_execute_eigen2(gla_plan_t p, const void* A, void* w, void* V2, int*
     if (rc) return rc;
   }
   return 0;
+}
+
+int gla_plan_execute_eigen2_host(gla_plan_t p, const void* A_host, void* w_host, void* V2_host, int* info_host,
+                                 void* stream) {
+  if (!p) return -1;
+  if (!A_host && p->a_elems) return -2;
+  if (!w_host && p->w_elems) return -3;
+  if (!V2_host && p->w_elems) return -4;
+  if (!info_host && p->batch) return -5;
+  if (p->jobz != 'V' || p->prec == GLA_PREC_F32_REFINED || !p->large_idx.empty()) return GLA_ERR_UNSUPPORTED;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t ioe = p->io_elem();
+  if (int rs = ensure_staging(p)) return rs;
+  GLA_CUDA(cudaMemcpyAsync(p->h_A, A_host, ioe * p->a_elems, cudaMemcpyHostToDevice, st));
+  int rc = gla_plan_execute_eigen2(p, p->h_A, p->h_w, p->h_V, p->h_info, st);
+  if (rc) return rc;
+  GLA_CUDA(cudaMemcpyAsync(w_host, p->h_w, ioe * p->w_elems, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaMemcpyAsync(V2_host, p->h_V, 2 * ioe * p->w_elems, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaMemcpyAsync(info_host, p->h_info, sizeof(int) * p->batch, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaStreamSynchronize(st));
+  int bad = 0;
+  for (int64_t b = 0; b < p->batch; b++) bad += info_host[b] != 0;
+  return bad;
 }
 
 int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const double* wbar, const double* Vbar,

@@ -189,6 +189,14 @@ class Plan:
                                                  _stream_ptr(stream))
         return _lib.check(rc, "gla_plan_execute_eigen2")
 
+    def execute_eigen2_host(self, A, w, V2, info, stream=None):
+        """execute_eigen2 from and to numpy arenas (gla_plan_execute_eigen2_host);
+        synchronizes. Returns the number of matrices with nonzero info."""
+        rc = _lib.load().gla_plan_execute_eigen2_host(self._h, C.c_void_p(A.ctypes.data), C.c_void_p(w.ctypes.data),
+                                                      C.c_void_p(V2.ctypes.data), C.c_void_p(info.ctypes.data),
+                                                      _stream_ptr(stream) if stream is not None else None)
+        return _lib.check(rc, "gla_plan_execute_eigen2_host")
+
     def capture(self, A, w, V, info):
         """Capture execute(A, w, V, info) into a torch.cuda.CUDAGraph (plan made
         with graph=True). Replaying it re-solves whatever A holds at replay."""

@@ -65,6 +65,7 @@ SIGNATURES = {
     "gla_plan_execute": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
     "gla_plan_execute_host": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
     "gla_plan_execute_eigen2": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
+    "gla_plan_execute_eigen2_host": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
     "gla_plan_stats": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_int)], _int),
     "gla_plan_phase_times": ([_vp, C.POINTER(C.c_float)], _int),
     "gla_plan_counters": ([_vp, C.POINTER(_i64)], _int),

@@ -294,13 +294,27 @@ eigen(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; kw...) where {T<:
 eigen(S::SymTridiagonal{Float64}; kw...) = eigen!(copy(S); kw...)
 
 # eigen2 (:633-668): ascending eigenvalues and rows 1 and n of the eigenvector
-# matrix (2 x n). The reference accumulates only those two rows of the
-# rotations; the device path forms the whole matrix and keeps two rows, so
-# eigen2(A).vectors == eigen(A).vectors[[1, n], :] exactly, as
-# test/eigenselfadjoint.jl:18-24 checks.
+# matrix (2 x n). Orders <= GLA_MAX_SMALL_N take the reference's cheap form
+# (gla_plan_execute_eigen2_host): rows 1 and n of Q from the reflectors, the
+# rotations replayed on those two rows only; the values equal eigen's and the
+# rows agree with eigen's to rounding (test/eigenselfadjoint.jl:45-51
+# compares them with isapprox). Larger orders keep two rows of the full
+# eigenvector matrix.
 function eigen2(A::Union{Hermitian{T,Matrix{T}},Symmetric{T,Matrix{T}}}; tol = eps(T)) where {T<:Union{Float32,Float64}}
+    n = LinearAlgebra.checksquare(A)
+    if 1 <= n <= GLA_MAX_SMALL_N
+        prec = T === Float32 ? GLA_PREC_F32 : GLA_PREC_F64
+        p = Plan(Int64[n]; precision = prec, jobz = 'V', uplo = uplochar(A), tol = Float64(tol))
+        w = Vector{T}(undef, n)
+        V2 = Vector{T}(undef, 2n)
+        info = zeros(Cint, 1)
+        check(ccall((:gla_plan_execute_eigen2_host, libglagpu), Cint,
+                    (Ptr{Cvoid}, Ptr{T}, Ptr{T}, Ptr{T}, Ptr{Cint}, Ptr{Cvoid}),
+                    p.handle, vec(Matrix{T}(A.data)), w, V2, info, C_NULL))
+        raise_info(info)
+        return LinearAlgebra.Eigen(w, reshape(V2, 2, n))
+    end
     E = eigen!(copy(A); tol)
-    n = size(E.vectors, 1)
     return LinearAlgebra.Eigen(E.values, E.vectors[[1, n], :])
 end
 function eigen2(S::SymTridiagonal{Float64}; tol = eps(Float64))

@@ -160,6 +160,10 @@ int gla_plan_execute(gla_plan_t plan, const void* A, void* w, void* V, int* info
  * others return GLA_ERR_UNSUPPORTED. Synchronization as gla_plan_execute.
  */
 int gla_plan_execute_eigen2(gla_plan_t plan, const void* A, void* w, void* V2, int* info, void* stream);
+/* Same from and to HOST buffers (V2: 2 w_elems entries); synchronizes the
+ * stream and returns the number of matrices with nonzero info. */
+int gla_plan_execute_eigen2_host(gla_plan_t plan, const void* A_host, void* w_host, void* V2_host, int* info_host,
+                                 void* stream);
 
 /*
  * Same, from and to HOST buffers: copies A in, runs, copies w, V and info

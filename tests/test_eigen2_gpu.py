@@ -217,3 +217,26 @@ def test_large_symtridiagonal_device_inputs(G):
     wo, _, _ = O.stev(d, e, "V")
     assert np.abs(r.values.cpu().numpy() - wo).max() <= 8 * n * EPS64 * np.linalg.norm(T, 2)
     assert residual(T, r.vectors.cpu().numpy(), r.values.cpu().numpy()) <= 1e-13
+
+
+def test_eigen2_host_matches_device(G):
+    # gla_plan_execute_eigen2_host (host arenas, the Julia glue's entry) gives
+    # the device entry's bits, including orders 1 and 2 whose 2 x n block is
+    # larger than n^2
+    import torch
+    sizes = [1, 2, 5, 64, 128, 3]
+    mats = [goe(n, 1200 + n) for n in sizes]
+    plan = G.Plan(sizes)
+    Ah = plan.pack(mats)
+    w = np.empty(plan.w_elems)
+    V2 = np.empty(2 * plan.w_elems)
+    info = np.zeros(len(sizes), dtype=np.int32)
+    assert plan.execute_eigen2_host(Ah, w, V2, info) == 0
+    A = plan.pack(mats, device="cuda")
+    wd = torch.empty(plan.w_elems, dtype=torch.float64, device="cuda")
+    V2d = torch.empty(2 * plan.w_elems, dtype=torch.float64, device="cuda")
+    infod = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    plan.execute_eigen2(A, wd, V2d, infod)
+    torch.cuda.synchronize()
+    assert np.array_equal(w, wd.cpu().numpy()) and np.array_equal(V2, V2d.cpu().numpy())
+    assert (info == 0).all()

@@ -117,11 +117,11 @@ def test_roofline_figures():
     # the launch list's top kernels of the batched refined step are reported
     # with their algorithmic work over their time
     import bench
-    r = bench.refine_roofline(7.0, 35.0, 4096)
-    assert r["kernel"] == "k_solve_refine" and r["unit"] == "T FP32 ops/s"
-    assert abs(r["frac"] - 0.2) < 1e-12
+    r = bench.refine_roofline(70.0, 1750.0, 4096, {"frac": 0.1})
+    assert r["kernel"] == "k_solve_refine" and r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+    assert abs(r["frac"] - 0.04) < 1e-12 and r["fp32_pipe"]["frac"] == 0.1
     assert abs(r["traffic"] - 4 * bench.REFINE_DRAM_BYTES_PER_1024) < 1.0
-    assert bench.refine_roofline(7.0, None, 4096)["frac"] is None
+    assert bench.refine_roofline(7.0, None, 4096, None)["frac"] is None
 
 
 def test_launch_counts():
