@@ -253,21 +253,22 @@ GLA_DEV void tridiag_body(int mid, unsigned char* smem_raw, const SmallDesc* __r
       if (tid < m) ww[tid] = xiv * vi - ui;
       __syncthreads();
     }
-    // ---- A~ += v w' - u v'   (== x(xi x)' - x u' - u x' of :484-491), lower triangle
+    // ---- A~ += v w' - u v'   (== x(xi x)' - x u' - u x' of :484-491), lower triangle:
+    // a warp per column (columns dealt in snake order, w, 2 nw - 1 - w, 2 nw + w,
+    // ..., which evens out their lengths), lanes over its rows
     {
-      const int total = m * (m + 1) / 2;
-      int j = 0, cs = 0, ce = m;
-      for (int f = tid; f < total; f += NT) {
-        while (f >= ce) {
-          j++;
-          cs = ce;
-          ce += m - j;
+      const int lane = tid & 31, wid = tid >> 5, nw = NT >> 5;
+      for (int r = 0;; r++) {
+        const int j = r * nw + ((r & 1) ? (nw - 1 - wid) : wid);
+        if (j >= m) break;
+        const T wj = ww[j], vj = vv[j];
+        T* col = At + (size_t)j * ld;
+        for (int i = j + lane; i < m; i += 32) {
+          T a = col[i];
+          a = fma(vv[i], wj, a);
+          a = fma(-uu[i], vj, a);
+          col[i] = a;
         }
-        const int i = j + (f - cs);
-        T a = At[j * ld + i];
-        a = fma(vv[i], ww[j], a);
-        a = fma(-uu[i], vv[j], a);
-        At[j * ld + i] = a;
       }
     }
     __syncthreads();
