@@ -318,8 +318,22 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   const size_t o_next = carve(sizeof(int));
   size_t refine_bytes = refined ? refine_workspace_bytes(aoff, woff, batch) : 0;
   const size_t o_ref = carve(refine_bytes);
+  cudaError_t err = cudaSuccess;
+  if (p->persistent) {  // two CTAs per SM (registers and shared memory allow two)
+    int dev = 0, nsm = 0;
+    err = cudaGetDevice(&dev);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (err != cudaSuccess) {
+      delete p;
+      return -1000 - (int)err;
+    }
+    p->persist_grid = std::max(1, std::min(2 * nsm, p->nwork));
+  }
+  // the tensor-core products' slice scratch, one per persistent CTA (orders above 32 only)
+  const bool pcache = p->persistent && p->refine_tc && p->nmax > 32;
+  const size_t o_pcache = carve(pcache ? (size_t)p->persist_grid * refine_pcache_bytes() : 0);
   p->ws_bytes = off;
-  cudaError_t err = cudaMalloc((void**)&p->ws, p->ws_bytes);
+  err = cudaMalloc((void**)&p->ws, p->ws_bytes);
   if (err != cudaSuccess) {
     delete p;
     return -1000 - (int)err;
@@ -340,13 +354,8 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->d_vtmp = (jobz == 'N' && refined) ? (void*)(w + o_vtmp) : nullptr;
   p->d_qtmp = p->stein ? (void*)(w + o_qtmp) : nullptr;
   p->d_next = (int*)(w + o_next);
-  if (p->persistent) {  // two CTAs per SM (registers and shared memory allow two)
-    int dev = 0, nsm = 0;
-    if (err == cudaSuccess) err = cudaGetDevice(&dev);
-    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    p->persist_grid = std::max(1, std::min(2 * nsm, p->nwork));
-  }
   if (refined) refine_carve(&p->rw, w + o_ref, aoff, woff, batch);
+  if (refined) p->rw.pcache = pcache ? (unsigned char*)(w + o_pcache) : nullptr;
   if (batch) err = cudaMemcpy(p->d_desc, desc.data(), sizeof(SmallDesc) * batch, cudaMemcpyHostToDevice);
   if (err == cudaSuccess && !perm_bucket.empty())
     err = cudaMemcpy(p->d_perm_bucket, perm_bucket.data(), sizeof(int) * perm_bucket.size(), cudaMemcpyHostToDevice);

@@ -24,9 +24,12 @@ struct RefineWork {
   float* J = nullptr;  // Jacobi scratch of cluster rotations (2 * a_elems)
   float* T = nullptr;  // FP32 product X E (a_elems)
   int* err = nullptr;  // tensor-core wait error word (zeroed by each execute)
+  unsigned char* pcache = nullptr;  // persistent kernel: per-CTA slice scratch of the products (or null)
 };
 
 size_t refine_workspace_bytes(int64_t a_elems, int64_t w_elems, int64_t batch);
+// Bytes of one persistent CTA's slice scratch (RefineWork.pcache).
+size_t refine_pcache_bytes();
 void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t w_elems, int64_t batch);
 cudaError_t refine_kernels_init();
 // ChaseState.applied of a matrix that k_solve_refine has solved and refined.

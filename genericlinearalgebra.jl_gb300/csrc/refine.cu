@@ -45,6 +45,8 @@ size_t refine_workspace_bytes(int64_t a_elems, int64_t, int64_t) {
   return (7 * sizeof(df64) + 4 * sizeof(float)) * (size_t)a_elems + 4096;
 }
 
+size_t refine_pcache_bytes() { return (size_t)tcs::kPCacheBytes; }
+
 void refine_carve(RefineWork* rw, char* base, int64_t a_elems, int64_t, int64_t) {
   df64* p = reinterpret_cast<df64*>(base);
   rw->A2 = p;
@@ -568,7 +570,9 @@ __global__ void __launch_bounds__(kRT, 2)
   __shared__ int s_idx;
   __shared__ tcs::Shared tsh;
   tcs::Ctx tcx;
-  if (TC) tcs::setup(tcx, &tsh, smem_raw, rw.err);
+  if (TC)
+    tcs::setup(tcx, &tsh, smem_raw, rw.err,
+               rw.pcache ? rw.pcache + (size_t)blockIdx.x * tcs::kPCacheBytes : nullptr);
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_idx = atomicAdd(next, 1);

@@ -59,33 +59,58 @@ GLA_DEV constexpr uint32_t idesc_n(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
 }
 static_assert(kS * kNT <= kTmemCols, "level accumulators exceed the CTA's TMEM columns");
+// Per-CTA global scratch of P's slices (all slabs of an order-128 operand):
+// pass 0 slices P and stores each slab's slices there with a bulk copy;
+// later passes load them back with a bulk copy instead of slicing again.
+constexpr int kPSlab = kS * kABlk;                 // 56 KB: P's part of a slab
+constexpr int kPCacheBytes = (128 / kKS) * kPSlab;  // 224 KB per CTA
 static_assert(kM <= 128, "one row of C per TMEM lane");
 
 // Per-CTA state in static shared memory.
 struct Shared {
   uint64_t bar;  // MMA completion (one phase per commit)
   uint64_t fin;  // teardown: every MMA of the CTA finished
+  uint64_t ldbar;  // bulk loads of cached P slabs (one phase per load)
   uint32_t tmem;
   int abort;
+  int ld_pending;  // a bulk load whose completion was not seen (abort path)
+  uint32_t ld_parity;
 };
 
 struct Ctx {
   Shared* sh;
   unsigned char* slabs;  // kSmem bytes of dynamic shared memory, 16-byte aligned
+  unsigned char* pcache; // kPCacheBytes of global scratch of this CTA, or null (no P cache)
   int* err;              // error word in global memory
   uint32_t phase;        // parity of the next completion of sh->bar
+  uint32_t ldphase;      // parity of the next completion of sh->ldbar
 };
 
+GLA_DEV void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(oz::smem_u32(ssrc)),
+               "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// the bulk stores of this thread have read their shared-memory source
+GLA_DEV void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// the bulk stores of this thread are complete
+GLA_DEV void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // All threads of the CTA (256); TMEM is held until teardown().
-GLA_DEV void setup(Ctx& c, Shared* sh, unsigned char* slabs, int* err) {
+GLA_DEV void setup(Ctx& c, Shared* sh, unsigned char* slabs, int* err, unsigned char* pcache = nullptr) {
   c.sh = sh;
   c.slabs = slabs;
+  c.pcache = pcache;
   c.err = err;
   c.phase = 0;
+  c.ldphase = 0;
   if (threadIdx.x == 0) {
     oz::mbar_init(&sh->bar, 1);
     oz::mbar_init(&sh->fin, 1);
+    oz::mbar_init(&sh->ldbar, 1);
     sh->abort = 0;
+    sh->ld_pending = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   if (threadIdx.x < 32) {
@@ -101,7 +126,11 @@ GLA_DEV void setup(Ctx& c, Shared* sh, unsigned char* slabs, int* err) {
 // All threads of the CTA, once, before it exits.
 GLA_DEV void teardown(Ctx& c) {
   __syncthreads();
-  if (threadIdx.x == 0) {  // the thread that issued every MMA of this CTA
+  if (threadIdx.x == 0) {  // the thread that issued every MMA and bulk copy of this CTA
+    bulk_wait_all();
+    if (c.sh->ld_pending)  // (abort path) the last bulk load lands before the CTA exits
+      for (long long it = 0; it < oz::kWaitLimit && !oz::mbar_try(&c.sh->ldbar, c.sh->ld_parity); it++) {
+      }
     oz::mma_commit(&c.sh->fin);
     for (long long it = 0; it < oz::kWaitLimit && !oz::mbar_try(&c.sh->fin, 0); it++) {
     }
@@ -215,12 +244,15 @@ GLA_DEV void slab_load(SlabRegs& g, int n, int rows, int k0, int j0, const LP& l
   }
 }
 
-GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int rows, int j0, const int* ea, const int* eb) {
+// doP = false: Q's slab only (P's comes from the cache).
+GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int rows, int j0, const int* ea, const int* eb,
+                        bool doP) {
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* sa = c.slabs;
   unsigned char* sb = c.slabs + kS * kABlk;
 #pragma unroll
   for (int t = 0; t < kPPairs; t++) {
+    if (!doP) break;
     const int cm = wid + 8 * t;
     const int r = cm_row(cm, lane), kk = cm_k(cm, lane);
     unsigned char* dst = sa + oz::tile_off(r, kk);
@@ -257,17 +289,42 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
   const int tid = threadIdx.x;
   if (c.sh->abort) return false;
   const int nks = (n + kKS - 1) / kKS;
+  // the P cache pays from the second pass on (n > 32)
+  const bool cache = c.pcache != nullptr && n > kNT;
   SlabRegs g;
   for (int j0 = 0; j0 < n; j0 += kNT) {
-    // stored rows: all, or (upper) i <= j < j0 + 32
-    const int rows = upper ? min(n, j0 + kNT) : n;
-    slab_load(g, n, rows, 0, j0, lp, lq);
+    const bool from_cache = cache && j0 > 0;
+    // P rows sliced: all; or (upper, no cache) the stored i <= j < j0 + 32
+    const int rows = (upper && !cache) ? min(n, j0 + kNT) : n;
+    slab_load(g, n, from_cache ? 0 : rows, 0, j0, lp, lq);
+    if (from_cache && j0 == kNT && tid == 0) bulk_wait_all();  // pass 0's stores have landed
     for (int q = 0; q < nks; q++) {
-      // the MMAs of the previous slab read the buffers: wait for them
-      if (q > 0 && !wait_mma(c)) return false;
-      slab_slice(g, c, n, rows, j0, ea, eb);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
+      // the MMAs of the previous slab read the buffers (and, in pass 0 with
+      // the cache, its bulk store read P's part): wait for them
+      if (q > 0) {
+        if (cache && !from_cache && tid == 0) bulk_wait_read();
+        if (!wait_mma(c)) return false;
+      }
+      if (from_cache) {
+        if (tid == 0) {
+          c.sh->ld_pending = 1;
+          c.sh->ld_parity = c.ldphase;
+          oz::mbar_expect_tx(&c.sh->ldbar, (uint32_t)kPSlab);
+          oz::bulk_g2s(c.slabs, c.pcache + (size_t)q * kPSlab, (uint32_t)kPSlab, &c.sh->ldbar);
+        }
+        slab_slice(g, c, n, rows, j0, ea, eb, false);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const bool landed = oz::mbar_wait(&c.sh->ldbar, c.ldphase, c.err);
+        c.ldphase ^= 1;
+        if (!landed) c.sh->abort = 1;
+        __syncthreads();
+        if (c.sh->abort) return false;
+        if (tid == 0) c.sh->ld_pending = 0;
+      } else {
+        slab_slice(g, c, n, rows, j0, ea, eb, true);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+      }
       if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint64_t a0 = oz::make_desc(oz::smem_u32(c.slabs));
@@ -284,9 +341,10 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
                         b0 + (uint64_t)((ks * 256) >> 4), idesc_n(kNT * (kS + 1 - s)), acc);
           }
         oz::mma_commit(&c.sh->bar);
+        if (cache && !from_cache) bulk_s2g(c.pcache + (size_t)q * kPSlab, c.slabs, (uint32_t)kPSlab);
       }
       // the next slab's loads overlap these MMAs
-      if (q + 1 < nks) slab_load(g, n, rows, (q + 1) * kKS, j0, lp, lq);
+      if (q + 1 < nks) slab_load(g, n, from_cache ? 0 : rows, (q + 1) * kKS, j0, lp, lq);
     }
     if (!wait_mma(c)) return false;
     asm volatile("tcgen05.fence::after_thread_sync;");
