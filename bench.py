@@ -41,7 +41,7 @@ for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
 METRIC = "eigh/s (batch n≤128) & n=4096 time at 1e-13 resid: FP32+refine vs FP64 GPU"
 # DRAM bytes (read + write) of the refinement in one step of the 1024-matrix
 # workload (ncu dram__bytes_read.sum + dram__bytes_write.sum)
-REFINE_DRAM_BYTES_PER_1024 = 685.5e6
+REFINE_DRAM_BYTES_PER_1024 = 1367.8e6
 BATCH = 4096
 NLO, NHI = 8, 128
 SEED = 2
@@ -101,7 +101,8 @@ def refine_roofline(achieved, peak, batch, fp32):
     (same order distribution), from an ncu capture, scaled by the matrix
     count; the algorithmic bytes are ~20 sum(n^2) = 0.48 GB per step, the
     rest is the per-matrix double-float scratch of the refinement (56 n^2
-    bytes) that does not stay in L2."""
+    bytes) and the products' slice scratch (224 KB per CTA, rewritten for
+    every product), which do not stay in L2."""
     return {"kernel": "k_solve_refine", "bound": "tensor", "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
             "traffic": REFINE_DRAM_BYTES_PER_1024 * batch / 1024 if REFINE_DRAM_BYTES_PER_1024 else None,
