@@ -74,9 +74,10 @@ struct OzCfg {
   static constexpr size_t kSmem = kStages * kStageBytes;
   static constexpr int kDrainCols = BN / (kDrainWarps / 4);
   // kind::f16 instruction descriptor: F32 accumulate, bf16 A and B, both
-  // K-major, N = BN, M = kBM
-  static constexpr uint32_t kIdesc =
-      (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+  // K-major, M = kBM, N = nn
+  __host__ __device__ static constexpr uint32_t idesc(int nn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+  }
   static_assert(S * BN <= 512, "level accumulators exceed the TMEM columns");
   static_assert(kSmem + 1024 <= 232448, "stage ring exceeds shared memory");
 };
@@ -282,20 +283,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_gemm(const GemmArgs g) {
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t a0 = make_desc(smem_u32(sm + st * stB));
           const uint64_t b0 = a0 + (uint64_t)(kAAll >> 4);
+          // A slice s times B slices t = 1 .. kMaxLevel - s at once: those
+          // are adjacent BN-row blocks of the stage (one K-major operand of
+          // BN (kMaxLevel - s) rows in the same layout, split at the MMA's
+          // N <= 256) and their levels s + 1 .. kMaxLevel adjacent BN-column
+          // accumulators: A is read once per group instead of once per pair
 #pragma unroll
           for (int ks = 0; ks < kKS / 16; ks++)  // K = 16 per instruction: 2 K-core matrices = 256 B
 #pragma unroll
-            for (int s = 1; s <= Cfg::S; s++)
+            for (int s = 1; s <= Cfg::S; s++) {
+              // s = 1 reaches every level first and starts the group's
+              // accumulators from zero
+              const uint32_t accumulate = (qq == 0 && ks == 0 && s == 1) ? 0u : 1u;
+              constexpr int kMaxT = 256 / kBN;  // B slices per MMA (N <= 256)
 #pragma unroll
-              for (int t = 1; t <= Cfg::S; t++) {
-                if (s + t > kMaxLevel) continue;
-                // in this order (s = 1 first) the group's first MMA into
-                // level s + t has s = 1 and starts the accumulator from zero
-                const uint32_t accumulate = (qq == 0 && ks == 0 && s == 1) ? 0u : 1u;
-                mma_f16(tmem + (uint32_t)((s + t - 2) * kBN),
+              for (int t0 = 1; t0 <= Cfg::S; t0 += kMaxT) {
+                const int nt = kMaxLevel - s - t0 + 1;  // slices t0 .. kMaxLevel - s left
+                if (nt <= 0) continue;
+                const int cnt = nt < kMaxT ? nt : kMaxT;
+                mma_f16(tmem + (uint32_t)((s + t0 - 2) * kBN),
                         a0 + (uint64_t)(((s - 1) * kABlock + ks * 256) >> 4),
-                        b0 + (uint64_t)(((t - 1) * kBBlock + ks * 256) >> 4), Cfg::kIdesc, accumulate);
+                        b0 + (uint64_t)(((t0 - 1) * kBBlock + ks * 256) >> 4), Cfg::idesc(cnt * kBN), accumulate);
               }
+            }
           mma_commit(&empty_bar[st]);  // stage buffer reusable once these MMAs finish
         }
         mma_commit(&drain_full);  // the group's accumulators are complete
