@@ -89,6 +89,7 @@ cudaError_t ensure_init() {
     if ((e = chase_kernels_init()) != cudaSuccess) g_init_err = e;
     if ((e = apply_kernels_init()) != cudaSuccess) g_init_err = e;
     if ((e = refine_kernels_init()) != cudaSuccess) g_init_err = e;
+    if ((e = adjoint_kernels_init()) != cudaSuccess) g_init_err = e;
   });
   return g_init_err;
 }

@@ -206,6 +206,20 @@ GLA_DEV void col_exps(int n, const T* __restrict__ M, int* out) {
   __syncthreads();
 }
 
+// Scale exponents of the rows of an n x n column-major array: out[i] =
+// exp_of(max_j |hi(M(i, j))|), one thread per row (consecutive threads read
+// consecutive rows of a column); all threads of the CTA, ends with a barrier.
+template <class T>
+GLA_DEV void row_exps(int n, const T* __restrict__ M, int* out) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    float m = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < n; j++) m = fmaxf(m, fabsf(hi_of(M[(size_t)j * n + i])));
+    out[i] = exp_of(m);
+  }
+  __syncthreads();
+}
+
 // Slab staging: a warp fills whole 8 x 8 core matrices (each lane one row
 // and two consecutive k: 128 contiguous bytes per warp and slice, free of
 // bank conflicts). P's 128 x 32 slab is 64 core matrices (8 per warp), Q's
