@@ -134,7 +134,7 @@ struct gla_plan_s {
   int* pin_pending = nullptr;
   df64* d_adj = nullptr;  // adjoint workspace (allocated by the first gla_plan_adjoint)
   double* h_adj = nullptr;  // device staging of gla_plan_adjoint_host
-  double* d_adj_large = nullptr;  // adjoint workspace of the orders above GLA_MAX_SMALL_N
+  LargeAdjoint* adj_large = nullptr;  // adjoint context of the orders above GLA_MAX_SMALL_N
   // orders above GLA_MAX_SMALL_N: solved one at a time by the large path
   std::vector<int> large_idx;           // batch indices, in batch order
   std::map<int, LargeCtx*> large_ctx;   // one context per distinct order
@@ -428,7 +428,7 @@ int gla_plan_destroy(gla_plan_t p) {
   cudaFreeHost(p->pin_pending);
   cudaFree(p->d_adj);
   cudaFree(p->h_adj);
-  cudaFree(p->d_adj_large);
+  large_adjoint_destroy(p->adj_large);
   for (auto& kv : p->large_ctx) large_destroy(kv.second);
   for (auto& kv : p->large_ref) refine_large_destroy(kv.second);
   cudaFreeHost(p->h_large_info);
@@ -889,7 +889,10 @@ int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const doubl
   if (!p->large_idx.empty()) {  // larger orders: three FP64 GEMMs each, one shared workspace
     int nl = 0;
     for (int b : p->large_idx) nl = std::max(nl, (int)p->n[b]);
-    if (!p->d_adj_large) GLA_CUDA(cache_alloc(&p->d_adj_large, sizeof(double) * large_adjoint_workspace_elems(nl)));
+    if (!p->adj_large) {
+      int rc = large_adjoint_create(&p->adj_large, nl);
+      if (rc) return rc;
+    }
     for (int b : p->large_idx) {
       const int nb = (int)p->n[b];
       int64_t aoff = 0, woff = 0;
@@ -897,8 +900,8 @@ int gla_plan_adjoint(gla_plan_t p, const double* w, const double* V, const doubl
         aoff += p->n[q] * p->n[q];
         woff += p->n[q];
       }
-      GLA_CUDA(large_adjoint(nb, w + woff, V + aoff, nb, wbar + woff, Vbar + aoff, nb, Abar + aoff, nb, gr,
-                             p->d_adj_large, st));
+      GLA_CUDA(large_adjoint(p->adj_large, nb, w + woff, V + aoff, nb, wbar + woff, Vbar + aoff, nb, Abar + aoff, nb,
+                             gr, st));
     }
   }
   return 0;

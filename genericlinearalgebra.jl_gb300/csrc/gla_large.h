@@ -69,12 +69,15 @@ cudaError_t oz_slice_rows(OzWork* w, const float* hi, const float* lo, long long
 bool oz_fits(const OzWork* w, int m, int n, int K);
 
 // ---- adjoint of one large eigen-decomposition (large_adjoint.cu):
-// Abar = V (diag(wbar) + sym(F o (V' Vbar))) V', FP64; ws holds
-// large_adjoint_workspace_elems(n) doubles.
-size_t large_adjoint_workspace_elems(int n);
-cudaError_t large_adjoint(int n, const double* w, const double* V, long long ldv, const double* wbar,
-                          const double* Vbar, long long ldvb, double* Abar, long long lda, double gap_rel,
-                          double* ws, cudaStream_t st);
+// Abar = V (diag(wbar) + sym(F o (V' Vbar))) V' for orders up to nmax of
+// the context (its tensor-core slice buffers and float-pair planes,
+// ~70 n^2 bytes).
+struct LargeAdjoint;
+int large_adjoint_create(LargeAdjoint** out, int nmax);
+void large_adjoint_destroy(LargeAdjoint* a);
+cudaError_t large_adjoint(LargeAdjoint* a, int n, const double* w, const double* V, long long ldv,
+                          const double* wbar, const double* Vbar, long long ldvb, double* Abar, long long lda,
+                          double gap_rel, cudaStream_t st);
 
 // ---- stage plans (one order, one working precision)
 struct SytrdPlan;

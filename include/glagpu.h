@@ -181,12 +181,14 @@ int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, voi
  * Output Abar (packed like A, full symmetric matrices):
  *     Abar = V (diag(wbar) + sym(F o (V' Vbar))) V',  sym(X) = (X + X')/2,
  *     F_ij = 1/(w_j - w_i) when |w_j - w_i| > gap_rel * max|w|, else 0.
- * gap_rel <= 0 selects 1e-10. Orders <= GLA_MAX_SMALL_N: one CTA per
- * matrix, products in double-float arithmetic (~1e-14). Larger orders: three
- * FP64 GEMMs per matrix (V'Vbar, V S, (V S) V'). The first call allocates the
- * adjoint workspace (32 bytes per arena element, plus 16 n^2 bytes for the
- * largest order above GLA_MAX_SMALL_N); later calls allocate nothing.
- * Asynchronous on `stream`.
+ * gap_rel <= 0 selects 1e-10. The three products (V'Vbar, V S, (V S) V')
+ * run to double-float accuracy (~2^-47 relative to the row and column
+ * maxima) on the tensor cores: one CTA per matrix for orders <=
+ * GLA_MAX_SMALL_N, three tensor-core GEMMs per matrix above. The first call
+ * allocates the adjoint workspace (32 bytes per arena element, plus about
+ * 70 n^2 bytes for the largest order above GLA_MAX_SMALL_N); later calls
+ * allocate nothing. A bounded tensor-core wait that ran out leaves the
+ * matrix's Abar NaN. Asynchronous on `stream`.
  */
 int gla_plan_adjoint(gla_plan_t plan, const double* w, const double* V, const double* wbar, const double* Vbar,
                      double* Abar, double gap_rel, void* stream);

@@ -213,7 +213,7 @@ def test_large_deterministic(G, precision, n):
 
 
 def test_large_adjoint_vs_analytic(G):
-    # orders above the one-CTA bound: three FP64 GEMMs; mixed with small orders
+    # orders above the one-CTA bound: three tensor-core GEMMs; mixed with small orders
     import torch
     from helpers import analytic_adjoint
     rng = np.random.default_rng(41)
