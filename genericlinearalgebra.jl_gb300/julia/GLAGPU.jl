@@ -327,7 +327,7 @@ end
     eigen_adjoint(E, wbar, Vbar; gap_rel = 0.0) -> Abar
 
 Reverse-mode adjoint of `E = eigen(A)` for a real symmetric `A`
-(gla_plan_adjoint_host; one CTA for n <= $(GLA_MAX_SMALL_N), three FP64 GEMMs
+(gla_plan_adjoint_host; one CTA for n <= $(GLA_MAX_SMALL_N), three tensor-core GEMMs
 above): the full symmetric cotangent
 `V (diag(wbar) + sym(F .* (V'Vbar))) V'` with `F_ij = 1/(w_j - w_i)` above
 the gap threshold. `nothing` stands for a zero cotangent.
