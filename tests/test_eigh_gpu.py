@@ -2,8 +2,8 @@
 against the CPU oracle on the same seeded inputs, plus the reference's own
 known-answer cases (test/eigenselfadjoint.jl).
 
-Tolerances (stated per spec: eigenvalues to a relative tolerance,
-eigenvectors by residual, orthogonality and sign-normalised comparison):
+Tolerances (eigenvalues to a relative tolerance, eigenvectors by residual,
+orthogonality and sign-normalised comparison):
   FP64        |w - w_oracle| <= 8 n eps64 ||A||, residual and ||V'V - I|| <= 1e-13,
               vectors within 100 n eps ||A|| / gap of the oracle's
   FP32        |w - w_oracle32| <= 8 n eps32 ||A||, residual, orthogonality <= 32 n eps32
