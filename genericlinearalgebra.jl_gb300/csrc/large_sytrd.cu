@@ -23,7 +23,11 @@
 //     with this column's terms plus its norm partial.
 // Each phase issues all of its global loads before its first reduction:
 // on GB300 an L2 round trip costs about a microsecond and is the unit of
-// cost at the small trailing orders.
+// cost at the small trailing orders. Phase B's rows are split over the CTAs
+// once per panel (rows k0 + 1 .. n - 1; a row above the current column's s
+// is idle), so each CTA computes V and W for the same rows in every column
+// of the panel and keeps them in shared memory for the rank-2 corrections
+// of the later columns, instead of reading them back from L2.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -200,6 +204,10 @@ GLA_DEV void own_rows(int s, int n, int& lo, int& hi) {
   hi = min(n, lo + R);
 }
 
+// Rows per CTA of phase B in the panel starting at column k0 (the split of
+// rows k0 + 1 .. n - 1, fixed for the panel).
+GLA_DEV __host__ int panel_rows(int k0, int n, int G) { return (n - k0 - 1 + G - 1) / G; }
+
 // Dot-product unit kinds, in work-list order after the SYMV units.
 constexpr int kDotA = 0;  // sum_r a_r A[r, s]        (cross term of v'A_t v)
 constexpr int kDotV = 1;  // sum_r a_r V[r, q], q < c
@@ -216,6 +224,14 @@ __global__ void __launch_bounds__(kPT, 1) k_sytrd_panel(const SytrdArgs<T> a) {
   __shared__ T sdotV[kSytrdNB], sdotW[kSytrdNB], sVs[kSytrdNB], sWs[kSytrdNB];
   __shared__ int sust[kMaxTC + 1];
   __shared__ T sscal[4];
+  // this CTA's V and W rows of the panel (rows lo0 .. lo0 + R0 - 1, columns
+  // 0 .. nbp - 1), dynamic shared memory
+  extern __shared__ __align__(16) unsigned char vw_raw[];
+  T* sVr = reinterpret_cast<T*>(vw_raw);
+  const int R0 = panel_rows(a.k0, n, G);
+  T* sWr = sVr + (size_t)R0 * kSytrdNB;
+  const int lo0 = min(n, a.k0 + 1 + g * R0), hi0 = min(n, lo0 + R0);
+  for (int i = tid; i < 2 * R0 * kSytrdNB; i += kPT) sVr[i] = T(0);
   int rb = 0;
   unsigned bar_target = a.bar_base;
   for (int i = tid; i <= a.nTC; i += kPT) sust[i] = a.ustart[i];
@@ -281,15 +297,15 @@ __global__ void __launch_bounds__(kPT, 1) k_sytrd_panel(const SytrdArgs<T> a) {
     const int ndch = (m + kDotRows - 1) / kDotRows;
     const int Js = s / kTW;
     const int nchs = (n - Js * kTW + kRC - 1) / kRC;
-    int lo, hi;
-    own_rows(s, n, lo, hi);
-    const int R = hi - lo;
+    const int R = R0;
     int tpr = 1;
     while (tpr < 32 && tpr * 2 * R <= kPT) tpr *= 2;
     const int sub = tid % tpr;
-    const int i = lo + tid / tpr;
-    const bool act = i < hi;
+    const int rl = tid / tpr;  // this thread's row of the CTA's panel rows
+    const int i = lo0 + rl;
+    const bool act = i < hi0 && i >= s;
     const int ii = act ? i : s;  // idle threads read row s (always in range)
+    const int rc = rl < R ? rl : R - 1;  // (idle threads: any cached row)
     // (1) every load of the phase, independent of the reductions
     T red[4] = {T(0), T(0), T(0), T(0)};  // sigma, a'A_t a, sum a_r A[r,s], y_s raw
     for (int t = tid; t < G; t += kPT) {
@@ -372,7 +388,7 @@ __global__ void __launch_bounds__(kPT, 1) k_sytrd_panel(const SytrdArgs<T> a) {
     // (3) own rows
     T y = T(0), xn = T(0);
     for (int q = sub; q < c; q += tpr) {
-      const T vq = a.V[ii + (long long)q * ldv], wq = a.W[ii + (long long)q * ldv];
+      const T vq = sVr[(size_t)rc * kSytrdNB + q], wq = sWr[(size_t)rc * kSytrdNB + q];
       const T pv = fma(scale, sdotV[q], sVs[q]), qv = fma(scale, sdotW[q], sWs[q]);
       y -= vq * qv + wq * pv;
       xn += vq * sWs[q] + wq * sVs[q];
@@ -390,6 +406,8 @@ __global__ void __launch_bounds__(kPT, 1) k_sytrd_panel(const SytrdArgs<T> a) {
     if (act && sub == 0) {
       a.V[ii + (long long)c * ldv] = vi;
       a.W[ii + (long long)c * ldv] = wi;
+      sVr[(size_t)rl * kSytrdNB + c] = vi;
+      sWr[(size_t)rl * kSytrdNB + c] = wi;
       if (ii > s) A[ii + (long long)j * ld] = vi;
       if (update_next) {
         // A[s, s] is read by every CTA in this phase: its new value goes to d[s]
@@ -521,7 +539,8 @@ cudaError_t sytrd_run(SytrdPlan& sp, T* A, long long lda, T* d, T* e, T* tau, cu
     a.bar_base = bar_base;
     bar_base += 2u * (unsigned)nbp * (unsigned)sp.G;  // barriers per launch: 1 + nbp + (nbp - 1)
     void* args[] = {(void*)&a};
-    err = cudaLaunchCooperativeKernel((const void*)k_sytrd_panel<T>, dim3(sp.G), dim3(kPT), args, 0, st);
+    err = cudaLaunchCooperativeKernel((const void*)k_sytrd_panel<T>, dim3(sp.G), dim3(kPT), args,
+                                      2 * (size_t)panel_rows(k0, n, sp.G) * kSytrdNB * sizeof(T), st);
     if (err != cudaSuccess) return err;
     const int t = k0 + nbp;
     if (t < n - 1) {  // trailing update A[t:, t:] -= V W' + W V' (lower tiles)
@@ -561,9 +580,14 @@ cudaError_t sytrd_plan_create(SytrdPlan** out, int n, bool f64, bool tc) {
   int dev = 0, nsm = 0, per = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err == cudaSuccess) err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (err == cudaSuccess)
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per, f64 ? (const void*)k_sytrd_panel<double> : (const void*)k_sytrd_panel<float>, kPT, 0);
+  // phase B's V / W row cache: 2 rows-per-CTA x kSytrdNB values. The limit
+  // is a property of the kernel, shared by every plan: always the largest
+  // order's, so that a plan made later never lowers it below an earlier
+  // plan's launches.
+  const void* kfn = f64 ? (const void*)k_sytrd_panel<double> : (const void*)k_sytrd_panel<float>;
+  const int vwbytes = 2 * panel_rows(0, kMaxTC * kTW, std::max(nsm, 1)) * kSytrdNB * (f64 ? 8 : 4);
+  if (err == cudaSuccess) err = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, vwbytes);
+  if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfn, kPT, vwbytes);
   if (err == cudaSuccess && per < 1) err = cudaErrorCooperativeLaunchTooLarge;
   if (err != cudaSuccess) {
     delete sp;
