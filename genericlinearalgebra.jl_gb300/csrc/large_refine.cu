@@ -31,13 +31,13 @@
 // afterwards when an update moved an eigenvalue past a neighbour); a cluster whose C_J is
 // already diagonal to 1e-15 ||A|| is not rotated (an FP32 rotation would
 // bring back 1e-7 non-orthogonality). When nothing was rotated and the
-// corrections are below 1e-7 (or at their rounding floor), one last
+// corrections are below 2e-7 (or at their rounding floor), one last
 // "polishing" iteration forms the full double-float Gram matrix and uses the
 // symmetric form E = R/2 + sym(T)/(lam_j - lam_i): the residual form
 // recovers r_ij only to ~u ||A|| / gap_ij, the symmetric form to u. The
 // polish forms X E in double-float on the tensor cores and skips rotations
 // that are rounding noise at tight gaps; when the orthogonality defect it
-// started from exceeded 3e-8 (tight clusters rotated shortly before), one
+// started from exceeded 1e-7 (tight clusters rotated shortly before), one
 // more symmetric step X <- X (I + R/2) squares the remaining ~d^2 away.
 #include <cuda_runtime.h>
 
@@ -677,13 +677,14 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
       r->rotated += (int)rs.size();
       if (polish) {
         // the polish corrects the orthogonality defect d it started from to
-        // first order, leaving ~3/4 d^2: above d = 3e-8 (tight clusters
+        // first order, leaving ~3/4 d^2 (7.5e-15 at d = 1e-7, far inside the
+        // 1e-13 target): above d = 1e-7 (tight clusters
         // rotated by FP32 Rayleigh-Ritz solutions shortly before) one more
         // symmetric step X <- X (I + R/2) squares it again; both products on
         // the tensor cores in double-float. The residual moves by
         // (lam_j - lam_i) r_ij / 2, negligible where the defect sits (pairs
         // at tight gaps).
-        if (hs[1] > 3e-8f) {
+        if (hs[1] > 1e-7f) {
           RF_CUDA(oz_slice(r->ozx, true, r->Xhi, r->Xlo, n, n, n, 7, st));
           RF_CUDA(oz_slice(r->oz, false, r->Xhi, r->Xlo, n, n, n, 7, st));
           RF_CUDA(oz_gemm2(r->ozx, r->oz, n, n, n, r->Ghi, r->Glo, n, true, st));
@@ -703,14 +704,15 @@ int refine_large_run(RefineLarge* r, const double* A, long long lda, bool lower,
         break;
       }
       // the eigenvectors have (nearly) converged: nothing rotated, and the
-      // corrections are below 1e-7 (the polishing iteration, quadratically
-      // convergent, leaves ~emax^2 ||A|| in the residual) or have stopped
+      // corrections are below 2e-7 (the polishing iteration, quadratically
+      // convergent, leaves ~emax^2 ||A|| = 4e-14 ||A|| in the residual, inside
+      // the 1e-13 target) or have stopped
       // falling (the rounding floor of the residual form, u ||A|| / gap, at
       // the tightest gaps). One more iteration with the full Gram matrix then
       // restores orthogonality to working accuracy (the residual form
       // recovers r_ij only to ~u ||A|| / gap_ij).
       const double emax = hs[0];
-      if (rs.empty() && (emax < 1e-7 || (emax < 1e-5 && emax > 0.25 * emax_prev))) polish = true;
+      if (rs.empty() && (emax < 2e-7 || (emax < 1e-5 && emax > 0.25 * emax_prev))) polish = true;
       emax_prev = emax;
       // keep the columns in ascending order (cluster updates can move an
       // eigenvalue past a neighbour that was not in its cluster)
