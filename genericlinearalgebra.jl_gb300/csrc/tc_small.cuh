@@ -23,15 +23,18 @@
 // MMA's canonical no-swizzle K-major layout (oz_prims.cuh), one thread
 // issues the MMAs (per K = 16 step one per slice of P, see idesc_n) and
 // commits to an mbarrier, and the CTA loads the next slab's values into
-// registers while they run; after the last slab the eight warps drain the levels with
-// tcgen05.ld (warp w reads TMEM lanes 32 (w % 4) .. +31, columns 16 (w / 4)
-// .. +15), combine them and call the store functor.
+// registers while they run; after the last slab the eight warps drain the
+// levels with tcgen05.ld (warp w reads TMEM lanes 32 (w % 4) .. +31,
+// columns 16 (w / 4) .. +15), combine them and call the store functor.
+// With a per-CTA global scratch (the persistent kernel), P's slabs are
+// sliced only in the first pass and stored there by bulk copies; later
+// passes bring them back with bulk copies and slice only Q's slab.
 //
 // Every mbarrier wait is bounded: a wait that runs out sets the error word
 // and the CTA's abort flag, no further MMA is issued by the CTA, and the
 // caller sees `false` (the matrix is then reported as not converged).
-// teardown() waits (bounded) for every MMA the CTA issued before it frees
-// the TMEM.
+// teardown() waits (bounded) for every bulk copy and MMA the CTA issued
+// before it frees the TMEM.
 #pragma once
 #include <cuda_bf16.h>
 
