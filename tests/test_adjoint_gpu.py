@@ -161,3 +161,28 @@ def test_forward_and_adjoint_in_one_graph(G, precision):
         assert torch.equal(Abar, Abar2)
     gp.close()
     ref.close()
+
+
+def test_adjoint_tensor_core_products_all_orders(G):
+    # the batched adjoint's tensor-core products at every slab and pass
+    # boundary of the order (1 .. 128, the 32-column passes, a 1e6 scaling):
+    # the kernel's Abar against the closed form on the same (w, V)
+    import torch
+    from helpers import goe
+    ns = [1, 2, 3, 17, 31, 32, 33, 63, 64, 65, 96, 127, 128]
+    mats = [goe(n, 300 + n) * (1e6 if n == 65 else 1.0) for n in ns]
+    plan = G.Plan(ns)
+    w, V = solve(G, plan, mats)
+    rng = np.random.default_rng(5)
+    wbar = torch.tensor(rng.standard_normal(plan.w_elems), device="cuda")
+    Vbar = torch.tensor(rng.standard_normal(plan.a_elems), device="cuda")
+    Abar = torch.empty_like(V)
+    plan.adjoint(w, V, wbar, Vbar, Abar)
+    ws, Vs = plan.unpack(w.cpu().numpy(), V.cpu().numpy())
+    wbs, Vbs = plan.unpack(wbar.cpu().numpy(), Vbar.cpu().numpy())
+    _, Abs = plan.unpack(w.cpu().numpy(), Abar.cpu().numpy())
+    for wg, Vg, wb, Vb, Ab in zip(ws, Vs, wbs, Vbs, Abs):
+        ref = analytic_adjoint(Vg, wg, wb, Vb, gap_rel=1e-10)
+        assert np.all(np.isfinite(Ab))
+        assert np.linalg.norm(Ab - ref) <= 1e-11 * max(np.linalg.norm(ref), 1e-300)
+        assert np.array_equal(Ab, Ab.T)
