@@ -157,7 +157,8 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
   __shared__ unsigned brk_mask[kRT / 32];
   __shared__ double gred[kRT / 32];
   __shared__ double gmin_s, lmax_s;
-  __shared__ int expA[TC ? kSmallMaxN : 1], expX[TC ? kSmallMaxN : 1], expY[TC ? kSmallMaxN : 1];
+  // scale exponents: A's rows, and the columns of [Y | X] (X's at expQ + n)
+  __shared__ int expA[TC ? kSmallMaxN : 1], expQ[TC ? 2 * kSmallMaxN : 1];
   float* Bsf = reinterpret_cast<float*>(Bs2);
   const SmallDesc dsc = descs[mid];
   const int n = dsc.n, tid = threadIdx.x;
@@ -210,6 +211,7 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
       const df64* Xc = X;
       auto xk = [&](int k, int j) { return it == 0 ? df_make(X0[(size_t)j * n + k], 0.f) : Xc[(size_t)j * n + k]; };
       auto xt = [&](int i, int k) { return it == 0 ? df_make(X0[(size_t)i * n + k], 0.f) : Xc[(size_t)i * n + k]; };
+      int* expX = expQ + n;
       if (it == 0)
         tcs::col_exps(n, X0, expX);
       else
@@ -217,22 +219,28 @@ GLA_DEV void refine_body(int mid, const SmallDesc* __restrict__ descs, const dou
       tcs::gemm(
           *tcx, n, expA, expX, [&](int i, int k) { return A2[(size_t)k * n + i]; }, xk,
           [&](int i, int j, df64 v) { Y[(size_t)j * n + i] = v; }, false);
-      tcs::col_exps(n, Y, expY);
+      tcs::col_exps(n, Y, expQ);
+      // [S | X'X] = X' [Y | X] as one product (X' sliced once): columns j < n
+      // give S, columns n + j give X'X; upper triangles, mirrored
       tcs::gemm(
-          *tcx, n, expX, expY, xt, [&](int k, int j) { return Y[(size_t)j * n + k]; },
+          *tcx, n, 2 * n, expX, expQ, xt,
+          [&](int k, int j) { return j < n ? Y[(size_t)j * n + k] : xk(k, j - n); },
           [&](int i, int j, df64 v) {
-            Sd[(size_t)j * n + i] = v;
-            Sd[(size_t)i * n + j] = v;
+            if (j < n) {
+              if (i <= j) {
+                Sd[(size_t)j * n + i] = v;
+                Sd[(size_t)i * n + j] = v;
+              }
+            } else {
+              const int jj = j - n;
+              if (i <= jj) {
+                const df64 r = df_add(df_make(i == jj ? 1.f : 0.f, 0.f), df_neg(v));
+                Rd[(size_t)jj * n + i] = r;
+                Rd[(size_t)i * n + jj] = r;
+              }
+            }
           },
-          true);
-      tcs::gemm(
-          *tcx, n, expX, expX, xt, xk,
-          [&](int i, int j, df64 v) {
-            const df64 r = df_add(df_make(i == j ? 1.f : 0.f, 0.f), df_neg(v));
-            Rd[(size_t)j * n + i] = r;
-            Rd[(size_t)i * n + j] = r;
-          },
-          true);
+          false);
       if (!tcs::ok(*tcx)) break;  // a tensor-core wait ran out: reported as not converged
       cS = Sd;
       cR = Rd;

@@ -240,9 +240,10 @@ struct SlabRegs {
 GLA_DEV int cm_row(int cm, int lane) { return ((cm >> 2) << 3) + (lane >> 2); }
 GLA_DEV int cm_k(int cm, int lane) { return ((cm & 3) << 3) + ((lane & 3) << 1); }
 
-// rows: the rows of P this pass needs (the rest are zero slices).
+// rows: the rows of P this pass needs (the rest are zero slices); nc: the
+// columns of Q.
 template <class LP, class LQ>
-GLA_DEV void slab_load(SlabRegs& g, int n, int rows, int k0, int j0, const LP& lp, const LQ& lq) {
+GLA_DEV void slab_load(SlabRegs& g, int n, int nc, int rows, int k0, int j0, const LP& lp, const LQ& lq) {
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const df64 zero = df_make(0.f, 0.f);
 #pragma unroll
@@ -256,13 +257,13 @@ GLA_DEV void slab_load(SlabRegs& g, int n, int rows, int k0, int j0, const LP& l
   for (int t = 0; t < kQPairs; t++) {
     const int cm = wid + 8 * t;
     const int j = j0 + cm_row(cm, lane), k = k0 + cm_k(cm, lane);
-    g.q[t][0] = (j < n && k < n) ? lq(k, j) : zero;
-    g.q[t][1] = (j < n && k + 1 < n) ? lq(k + 1, j) : zero;
+    g.q[t][0] = (j < nc && k < n) ? lq(k, j) : zero;
+    g.q[t][1] = (j < nc && k + 1 < n) ? lq(k + 1, j) : zero;
   }
 }
 
 // doP = false: Q's slab only (P's comes from the cache).
-GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int rows, int j0, const int* ea, const int* eb,
+GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int nc, int rows, int j0, const int* ea, const int* eb,
                         bool doP) {
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* sa = c.slabs;
@@ -286,7 +287,7 @@ GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int rows, int j0
     const int cc = cm_row(cm, lane), kk = cm_k(cm, lane);
     const int j = j0 + cc;
     unsigned char* dst = sb + oz::tile_off(cc, kk);
-    if (j < n) {
+    if (j < nc) {
       slice7x2(g.q[t][0], g.q[t][1], eb[j], dst, kBBlk);
     } else {
 #pragma unroll
@@ -301,19 +302,19 @@ GLA_DEV void slab_slice(const SlabRegs& g, const Ctx& c, int n, int rows, int j0
 // such is the most accurate). upper: only i <= j is stored. Returns false
 // when the CTA has aborted (C is then incomplete).
 template <class LP, class LQ, class ST>
-GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, const LQ& lq, const ST& store,
+GLA_DEV bool gemm(Ctx& c, int n, int nc, const int* ea, const int* eb, const LP& lp, const LQ& lq, const ST& store,
                   bool upper) {
   const int tid = threadIdx.x;
   if (c.sh->abort) return false;
   const int nks = (n + kKS - 1) / kKS;
   // the P cache pays from the second pass on (n > 32)
-  const bool cache = c.pcache != nullptr && n > kNT;
+  const bool cache = c.pcache != nullptr && nc > kNT;
   SlabRegs g;
-  for (int j0 = 0; j0 < n; j0 += kNT) {
+  for (int j0 = 0; j0 < nc; j0 += kNT) {
     const bool from_cache = cache && j0 > 0;
     // P rows sliced: all; or (upper, no cache) the stored i <= j < j0 + 32
     const int rows = (upper && !cache) ? min(n, j0 + kNT) : n;
-    slab_load(g, n, from_cache ? 0 : rows, 0, j0, lp, lq);
+    slab_load(g, n, nc, from_cache ? 0 : rows, 0, j0, lp, lq);
     if (from_cache && j0 == kNT && tid == 0) bulk_wait_all();  // pass 0's stores have landed
     for (int q = 0; q < nks; q++) {
       // the MMAs of the previous slab read the buffers (and, in pass 0 with
@@ -329,7 +330,7 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
           oz::mbar_expect_tx(&c.sh->ldbar, (uint32_t)kPSlab);
           oz::bulk_g2s(c.slabs, c.pcache + (size_t)q * kPSlab, (uint32_t)kPSlab, &c.sh->ldbar);
         }
-        slab_slice(g, c, n, rows, j0, ea, eb, false);
+        slab_slice(g, c, nc, rows, j0, ea, eb, false);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const bool landed = oz::mbar_wait(&c.sh->ldbar, c.ldphase, c.err);
         c.ldphase ^= 1;
@@ -338,7 +339,7 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
         if (c.sh->abort) return false;
         if (tid == 0) c.sh->ld_pending = 0;
       } else {
-        slab_slice(g, c, n, rows, j0, ea, eb, true);
+        slab_slice(g, c, nc, rows, j0, ea, eb, true);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
       }
@@ -361,7 +362,7 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
         if (cache && !from_cache) bulk_s2g(c.pcache + (size_t)q * kPSlab, c.slabs, (uint32_t)kPSlab);
       }
       // the next slab's loads overlap these MMAs
-      if (q + 1 < nks) slab_load(g, n, from_cache ? 0 : rows, (q + 1) * kKS, j0, lp, lq);
+      if (q + 1 < nks) slab_load(g, n, nc, from_cache ? 0 : rows, (q + 1) * kKS, j0, lp, lq);
     }
     if (!wait_mma(c)) return false;
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -392,7 +393,7 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
 #pragma unroll
         for (int u = 0; u < 16; u++) {
           const int j = j0 + half * 16 + u;
-          if (j >= n || (upper && r > j)) continue;
+          if (j >= nc || (upper && r > j)) continue;
           float ah, al;
           two_sum(ph[u], pl[u], ah, al);
           const int e = er + eb[j];
@@ -404,6 +405,13 @@ GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, con
     __syncthreads();  // the accumulators are free for the next pass
   }
   return true;
+}
+
+// C = P Q with Q square (nc = n).
+template <class LP, class LQ, class ST>
+GLA_DEV bool gemm(Ctx& c, int n, const int* ea, const int* eb, const LP& lp, const LQ& lq, const ST& store,
+                  bool upper) {
+  return gemm(c, n, n, ea, eb, lp, lq, store, upper);
 }
 
 }  // namespace tcs
