@@ -41,7 +41,7 @@ for _p in (ROOT, PKG, os.path.join(ROOT, "tests")):
 METRIC = "eigh/s (batch n≤128) & n=4096 time at 1e-13 resid: FP32+refine vs FP64 GPU"
 # DRAM bytes (read + write) of the refinement in one step of the 1024-matrix
 # workload (ncu dram__bytes_read.sum + dram__bytes_write.sum)
-REFINE_DRAM_BYTES_PER_1024 = 1367.8e6
+REFINE_DRAM_BYTES_PER_1024 = 1233.8e6
 BATCH = 4096
 NLO, NHI = 8, 128
 SEED = 2
