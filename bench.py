@@ -386,6 +386,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     el_e2e = ev0.elapsed_time(ev1) * 1e-3
+    # chunks the host execute overlapped its copies with (it also copies the
+    # 24-byte chase state of every matrix out, to find the matrices finished
+    # after their chunk's copy)
+    e2e_chunks, e2e_pipelined = plan.host_pipeline()
     plan.close()
     el_e2e = max_over_ranks(torch, el_e2e, ws, dev)
     peak = measured_dgemm_tflops(torch) if rank == 0 else None
@@ -448,7 +452,10 @@ def run_ours(args):
             "cpu_lapack": lapack,
             "e2e": {"value": ws * len(ns) * args.steps / el_e2e, "unit": "eigh/s",
                     "h2d_bytes_per_step": int(A64.nbytes),
-                    "d2h_bytes_per_step": int(8 * nA + 8 * nW + 4 * len(ns))},
+                    "d2h_bytes_per_step": int(8 * nA + 8 * nW + 4 * len(ns) + (24 * len(ns) if e2e_pipelined else 0)),
+                    "pipeline": {"chunks": e2e_chunks if e2e_pipelined else 0,
+                                 "how": "copies of one chunk of matrices overlap the solve of another"
+                                        if e2e_pipelined else "whole batch copied in, solved, copied out"}},
             "clocks": results["f32_refined"]["clocks"],
             "gpu_launches": int(G["launches_per_step"] * args.steps),  # the timed graph replays
             "paths": {k: {kk: vv for kk, vv in v.items() if kk != "clocks"} for k, v in results.items()},

@@ -49,6 +49,7 @@ constexpr int kHdrPerN = 3;     // header-log capacity per pass, in units of n
 constexpr int kAsyncPasses = 2;     // chase passes enqueued without a host check
 constexpr int kGraphPasses = 4;     // chase passes of a capture-safe (GLA_FLAG_GRAPH) execute
 constexpr int kMaxBuckets = 8;      // size buckets of width 16 over (0, 128]
+constexpr int kMaxChunks = 4;       // host-execute pipeline: chunks of the batch
 
 #define GLA_CUDA(x)                                  \
   do {                                               \
@@ -156,6 +157,19 @@ struct gla_plan_s {
   bool persistent = false;
   int persist_grid = 0;
   int* d_next = nullptr;  // its work counter
+  // gla_plan_execute_host of a persistent plan on pinned host buffers: the
+  // batch as contiguous runs of matrices ("chunks"), so that the copy of
+  // chunk c + 1's A and of chunk c - 1's w and V overlap the solve of chunk c
+  int nchunks = 0;                        // 0: no pipeline
+  int64_t chunk_b[kMaxChunks + 1] = {};   // chunk c: batch indices chunk_b[c] .. chunk_b[c + 1] - 1
+  int64_t chunk_a[kMaxChunks + 1] = {};   // its A / V elements from chunk_a[c]
+  int64_t chunk_w[kMaxChunks + 1] = {};   // its w elements from chunk_w[c]
+  int chunk_start[kMaxChunks + 1] = {};   // its work items: d_chunk_order[chunk_start[c] ..]
+  int* d_chunk_order = nullptr;           // each chunk's work items, orders descending
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_in[kMaxChunks] = {}, ev_solved[kMaxChunks] = {}, ev_out = nullptr;
+  ChaseState* h_cst = nullptr;            // pinned: the chase states after the persistent launches
+  bool last_pipelined = false;            // the last gla_plan_execute_host used the pipeline
   cudaEvent_t tev[kMaxBuckets][GLA_NUM_PHASES][2] = {};
   bool tused[kMaxBuckets][GLA_NUM_PHASES] = {};
   void mark(int b, int phase, int end, cudaStream_t st) {
@@ -333,6 +347,36 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   // the tensor-core products' slice scratch, one per persistent CTA (orders above 32 only)
   const bool pcache = p->persistent && p->refine_tc && p->nmax > 32;
   const size_t o_pcache = carve(pcache ? (size_t)p->persist_grid * refine_pcache_bytes() : 0);
+  // host-execute pipeline: one chunk per three matrices of every persistent
+  // CTA (two chunks at least, kMaxChunks at most), split at equal A bytes
+  std::vector<int> chunk_order;
+  if (p->persistent && p->large_idx.empty() && !p->graph && !p->timing) {
+    const int nc = std::min(kMaxChunks, p->nwork / std::max(1, 3 * p->persist_grid));
+    if (nc >= 2) {
+      p->nchunks = nc;
+      int64_t b = 0, a = 0, wo = 0;
+      for (int c = 1; c <= nc; c++) {
+        const int64_t target = aoff * c / nc;
+        while (b < batch && (c == nc || a < target)) {
+          a += n[b] * n[b];
+          wo += n[b];
+          b++;
+        }
+        p->chunk_b[c] = b;
+        p->chunk_a[c] = a;
+        p->chunk_w[c] = wo;
+      }
+      for (int c = 0; c < nc; c++) {
+        p->chunk_start[c] = (int)chunk_order.size();
+        for (int64_t i = p->chunk_b[c]; i < p->chunk_b[c + 1]; i++)
+          if (n[i] >= 1) chunk_order.push_back((int)i);
+        std::stable_sort(chunk_order.begin() + p->chunk_start[c], chunk_order.end(),
+                         [&](int x, int y) { return n[x] > n[y]; });
+      }
+      p->chunk_start[nc] = (int)chunk_order.size();
+    }
+  }
+  const size_t o_corder = carve(sizeof(int) * chunk_order.size());
   p->ws_bytes = off;
   err = cudaMalloc((void**)&p->ws, p->ws_bytes);
   if (err != cudaSuccess) {
@@ -355,17 +399,30 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   p->d_vtmp = (jobz == 'N' && refined) ? (void*)(w + o_vtmp) : nullptr;
   p->d_qtmp = p->stein ? (void*)(w + o_qtmp) : nullptr;
   p->d_next = (int*)(w + o_next);
+  p->d_chunk_order = (int*)(w + o_corder);
   if (refined) refine_carve(&p->rw, w + o_ref, aoff, woff, batch);
   if (refined) p->rw.pcache = pcache ? (unsigned char*)(w + o_pcache) : nullptr;
   if (batch) err = cudaMemcpy(p->d_desc, desc.data(), sizeof(SmallDesc) * batch, cudaMemcpyHostToDevice);
   if (err == cudaSuccess && !perm_bucket.empty())
     err = cudaMemcpy(p->d_perm_bucket, perm_bucket.data(), sizeof(int) * perm_bucket.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && !chunk_order.empty())
+    err = cudaMemcpy(p->d_chunk_order, chunk_order.data(), sizeof(int) * chunk_order.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMemset(p->d_scale, 0, sizeof(int) * std::max<int64_t>(batch, 1));
   if (err == cudaSuccess) err = cudaMallocHost((void**)&p->pin_pending, sizeof(int) * kMaxBuckets);
   if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
   for (Bucket& bk : p->buckets) {
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&bk.stream, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&bk.join, cudaEventDisableTiming);
+  }
+  if (p->nchunks) {
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->s_in, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->s_out, cudaStreamNonBlocking);
+    for (int c = 0; c < p->nchunks; c++) {
+      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_in[c], cudaEventDisableTiming);
+      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_solved[c], cudaEventDisableTiming);
+    }
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaMallocHost((void**)&p->h_cst, sizeof(ChaseState) * batch);
   }
   if (err == cudaSuccess && !p->large_idx.empty())
     err = cudaMallocHost((void**)&p->h_large_info, sizeof(int) * p->large_idx.size());
@@ -416,6 +473,14 @@ int gla_plan_destroy(gla_plan_t p) {
     if (bk.join) cudaEventDestroy(bk.join);
   }
   if (p->fork) cudaEventDestroy(p->fork);
+  if (p->s_in) cudaStreamDestroy(p->s_in);
+  if (p->s_out) cudaStreamDestroy(p->s_out);
+  for (int c = 0; c < kMaxChunks; c++) {
+    if (p->ev_in[c]) cudaEventDestroy(p->ev_in[c]);
+    if (p->ev_solved[c]) cudaEventDestroy(p->ev_solved[c]);
+  }
+  if (p->ev_out) cudaEventDestroy(p->ev_out);
+  cudaFreeHost(p->h_cst);
   for (int b = 0; b < kMaxBuckets; b++)
     for (int ph = 0; ph < GLA_NUM_PHASES; ph++)
       for (int k = 0; k < 2; k++)
@@ -588,6 +653,20 @@ int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cuda
   return 0;
 }
 
+// The persistent launch over `count` matrices of the work list `order`
+// (orders descending).
+int persistent_solve(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st, const int* order,
+                     int count) {
+  GLA_CUDA(cudaMemsetAsync(p->d_next, 0, sizeof(int), st));
+  GLA_CUDA(launch_solve_refine(&p->rw, count, p->nmax, std::min(p->persist_grid, count), st, p->d_desc, order,
+                               p->d_next, (const double*)A, p->uplo == 'L', (float*)p->d_d, (float*)p->d_e,
+                               (float*)p->d_x32, info, p->d_cst, p->d_scale, (float*)p->d_w32, (float*)p->d_qtmp,
+                               (double*)Vout, (double*)w, p->d_stats, p->refine_tc));
+  return 0;
+}
+
+int persistent_finish(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st);
+
 // The orders <= 128 of an FP32 + refinement plan with the in-kernel FP32
 // solver: one persistent launch solves and refines every matrix it can
 // (largest first, from a work counter); the QL chase, rotation replay and
@@ -596,15 +675,18 @@ int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cuda
 // plans; otherwise a full rotation log is finished by further host-checked
 // passes.
 int execute_persistent(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st) {
+  p->mark(0, GLA_PHASE_TRIDIAG, 0, st);
+  if (int rc = persistent_solve(p, A, w, Vout, info, st, p->d_perm_bucket, p->nwork)) return rc;
+  p->mark(0, GLA_PHASE_TRIDIAG, 1, st);
+  return persistent_finish(p, A, w, Vout, info, st);
+}
+
+// The chase, rotation-replay and refinement launches over the whole work
+// list that finish the matrices the persistent launches left (they return
+// at once for the others).
+int persistent_finish(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st) {
   const int lower = p->uplo == 'L';
   const int n = p->nwork;
-  GLA_CUDA(cudaMemsetAsync(p->d_next, 0, sizeof(int), st));
-  p->mark(0, GLA_PHASE_TRIDIAG, 0, st);
-  GLA_CUDA(launch_solve_refine(&p->rw, n, p->nmax, p->persist_grid, st, p->d_desc, p->d_perm_bucket, p->d_next,
-                               (const double*)A, lower, (float*)p->d_d, (float*)p->d_e, (float*)p->d_x32, info,
-                               p->d_cst, p->d_scale, (float*)p->d_w32, (float*)p->d_qtmp, (double*)Vout, (double*)w,
-                               p->d_stats, p->refine_tc));
-  p->mark(0, GLA_PHASE_TRIDIAG, 1, st);
   const int npass = p->graph ? kGraphPasses : kAsyncPasses;
   auto pass = [&]() -> int {
     GLA_CUDA(cudaMemsetAsync(p->d_pending, 0, sizeof(int), st));
@@ -767,6 +849,97 @@ int ensure_staging(gla_plan_t p) {
   }
   return 0;
 }
+
+// Page-locked host memory (registered or allocated by CUDA): copies from
+// and to it run asynchronously.
+bool host_pinned(const void* ptr) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// gla_plan_execute_host of a persistent plan, pipelined over its chunks:
+// chunk c's A goes in on s_in, its persistent launch waits for it on the
+// caller's stream, and its w and V come out on s_out while the next chunk
+// is solved. The launches that finish the matrices the persistent kernel
+// left (the QL chase and its replay, refinement) run once at the end over
+// the whole batch, as in execute_persistent; those matrices, known from
+// the chase states copied after the last persistent launch, are copied out
+// again afterwards. Results are those of gla_plan_execute.
+int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host,
+                           cudaStream_t st) {
+  const size_t ioe = p->io_elem();
+  const bool wantv = p->jobz == 'V';
+  void* Vout = wantv ? p->h_V : p->d_vtmp;
+  char* dA = static_cast<char*>(p->h_A);
+  char* dW = static_cast<char*>(p->h_w);
+  char* dV = static_cast<char*>(p->h_V);
+  const char* hA = static_cast<const char*>(A_host);
+  char* hW = static_cast<char*>(w_host);
+  char* hV = static_cast<char*>(V_host);
+  p->last_stream = st;
+  p->last_passes = 0;
+  for (int b = 0; b < kMaxBuckets; b++)
+    for (int ph = 0; ph < GLA_NUM_PHASES; ph++) p->tused[b][ph] = false;
+  GLA_CUDA(cudaEventRecord(p->fork, st));
+  GLA_CUDA(cudaStreamWaitEvent(p->s_in, p->fork, 0));
+  GLA_CUDA(cudaStreamWaitEvent(p->s_out, p->fork, 0));
+  for (int c = 0; c < p->nchunks; c++) {
+    const size_t a0 = ioe * p->chunk_a[c], ab = ioe * (p->chunk_a[c + 1] - p->chunk_a[c]);
+    if (ab) GLA_CUDA(cudaMemcpyAsync(dA + a0, hA + a0, ab, cudaMemcpyHostToDevice, p->s_in));
+    GLA_CUDA(cudaEventRecord(p->ev_in[c], p->s_in));
+  }
+  GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
+  GLA_CUDA(cudaMemsetAsync(p->h_info, 0, sizeof(int) * p->batch, st));
+  GLA_CUDA(cudaMemsetAsync(p->rw.err, 0, sizeof(int), st));
+  for (int c = 0; c < p->nchunks; c++) {
+    GLA_CUDA(cudaStreamWaitEvent(st, p->ev_in[c], 0));
+    if (int rc = persistent_solve(p, p->h_A, p->h_w, Vout, p->h_info, st, p->d_chunk_order + p->chunk_start[c],
+                                  p->chunk_start[c + 1] - p->chunk_start[c]))
+      return rc;
+    GLA_CUDA(cudaEventRecord(p->ev_solved[c], st));
+    GLA_CUDA(cudaStreamWaitEvent(p->s_out, p->ev_solved[c], 0));
+    const size_t w0 = ioe * p->chunk_w[c], wb = ioe * (p->chunk_w[c + 1] - p->chunk_w[c]);
+    const size_t a0 = ioe * p->chunk_a[c], ab = ioe * (p->chunk_a[c + 1] - p->chunk_a[c]);
+    if (wb) GLA_CUDA(cudaMemcpyAsync(hW + w0, dW + w0, wb, cudaMemcpyDeviceToHost, p->s_out));
+    if (wantv && ab) GLA_CUDA(cudaMemcpyAsync(hV + a0, dV + a0, ab, cudaMemcpyDeviceToHost, p->s_out));
+  }
+  GLA_CUDA(cudaMemcpyAsync(p->h_cst, p->d_cst, sizeof(ChaseState) * p->batch, cudaMemcpyDeviceToHost, st));
+  if (int rc = persistent_finish(p, p->h_A, p->h_w, Vout, p->h_info, st)) return rc;
+  GLA_CUDA(cudaMemcpyAsync(info_host, p->h_info, sizeof(int) * p->batch, cudaMemcpyDeviceToHost, st));
+  GLA_CUDA(cudaEventRecord(p->ev_out, p->s_out));
+  GLA_CUDA(cudaStreamWaitEvent(st, p->ev_out, 0));
+  GLA_CUDA(cudaStreamSynchronize(st));
+  // the matrices finished after their chunk's copy
+  std::vector<int64_t> late;
+  for (int64_t b = 0; b < p->batch; b++)
+    if (p->n[b] >= 1 && p->h_cst[b].applied != kRefinedInKernel) late.push_back(b);
+  if (late.size() > 64) {
+    GLA_CUDA(cudaMemcpyAsync(hW, dW, ioe * p->w_elems, cudaMemcpyDeviceToHost, st));
+    if (wantv) GLA_CUDA(cudaMemcpyAsync(hV, dV, ioe * p->a_elems, cudaMemcpyDeviceToHost, st));
+  } else if (!late.empty()) {
+    size_t k = 0;
+    int64_t aoff = 0, woff = 0;
+    for (int64_t b = 0; b < p->batch && k < late.size(); b++) {
+      const int64_t nb = p->n[b];
+      if (b == late[k]) {
+        GLA_CUDA(cudaMemcpyAsync(hW + ioe * woff, dW + ioe * woff, ioe * nb, cudaMemcpyDeviceToHost, st));
+        if (wantv)
+          GLA_CUDA(cudaMemcpyAsync(hV + ioe * aoff, dV + ioe * aoff, ioe * nb * nb, cudaMemcpyDeviceToHost, st));
+        k++;
+      }
+      aoff += nb * nb;
+      woff += nb;
+    }
+  }
+  if (!late.empty()) GLA_CUDA(cudaStreamSynchronize(st));
+  int bad = 0;
+  for (int64_t b = 0; b < p->batch; b++) bad += info_host[b] != 0;
+  return bad;
+}
 }  // namespace
 
 extern "C" {
@@ -781,6 +954,9 @@ int gla_plan_execute_host(gla_plan_t p, const void* A_host, void* w_host, void* 
   cudaStream_t st = (cudaStream_t)stream;
   const size_t ioe = p->io_elem();
   if (int rs = ensure_staging(p)) return rs;
+  p->last_pipelined =
+      p->nchunks && host_pinned(A_host) && host_pinned(w_host) && (p->jobz != 'V' || host_pinned(V_host));
+  if (p->last_pipelined) return execute_host_pipelined(p, A_host, w_host, V_host, info_host, st);
   GLA_CUDA(cudaMemcpyAsync(p->h_A, A_host, ioe * p->a_elems, cudaMemcpyHostToDevice, st));
   int rc = plan_execute(p, p->h_A, p->h_w, p->h_V, p->h_info, st);
   if (rc) return rc;
@@ -970,6 +1146,15 @@ int gla_plan_stats(gla_plan_t p, int64_t* rotations, int64_t* sweeps, int* passe
   if (rotations) *rotations = c[GLA_COUNTER_ROTATIONS];
   if (sweeps) *sweeps = c[GLA_COUNTER_SWEEPS];
   if (passes) *passes = (int)c[GLA_COUNTER_PASSES];
+  return 0;
+}
+
+int gla_plan_host_pipeline(gla_plan_t p, int* chunks, int* last_pipelined) {
+  if (!p) return -1;
+  if (!chunks) return -2;
+  if (!last_pipelined) return -3;
+  *chunks = p->nchunks;
+  *last_pipelined = p->last_pipelined ? 1 : 0;
   return 0;
 }
 

@@ -237,6 +237,13 @@ class Plan:
                                                _stream_ptr(stream) if stream is not None else None)
         return _lib.check(rc, "gla_plan_execute_host")
 
+    def host_pipeline(self):
+        """(chunks, last_pipelined): the chunks execute_host overlaps its copies
+        with (0: never), and whether its last call did."""
+        c, u = C.c_int(0), C.c_int(0)
+        _lib.check(_lib.load().gla_plan_host_pipeline(self._h, C.byref(c), C.byref(u)))
+        return c.value, bool(u.value)
+
     def adjoint(self, w, V, wbar, Vbar, Abar, gap_rel=0.0, stream=None):
         """Abar = V (diag(wbar) + sym(F o V'Vbar)) V' for every matrix (torch CUDA
         arenas, FP64, packed like execute's outputs). Asynchronous."""

@@ -64,6 +64,7 @@ SIGNATURES = {
     "gla_plan_arena_sizes": ([_vp, C.POINTER(_i64), C.POINTER(_i64)], _int),
     "gla_plan_execute": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
     "gla_plan_execute_host": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
+    "gla_plan_host_pipeline": ([_vp, C.POINTER(_int), C.POINTER(_int)], _int),
     "gla_plan_execute_eigen2": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
     "gla_plan_execute_eigen2_host": ([_vp, _vp, _vp, _vp, _vp, _vp], _int),
     "gla_plan_stats": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_int)], _int),

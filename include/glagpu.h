@@ -168,10 +168,18 @@ int gla_plan_execute_eigen2_host(gla_plan_t plan, const void* A_host, void* w_ho
 /*
  * Same, from and to HOST buffers: copies A in, runs, copies w, V and info
  * out, and synchronizes `stream` before returning. Uses plan-owned device
- * buffers (allocated on first use). Pinned host memory is fastest.
+ * buffers (allocated on first use). Pinned host memory is fastest: for an
+ * GLA_PREC_F32_REFINED plan of orders <= GLA_MAX_SMALL_N whose batch fills
+ * the device several times over, with A, w and V (jobz 'V') in page-locked
+ * memory, the batch is solved in up to four contiguous chunks and the
+ * copies of one chunk overlap the solve of the next (same results).
  */
 int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, void* V_host, int* info_host,
                           void* stream);
+/* The number of chunks gla_plan_execute_host pipelines this plan over (0:
+ * never), and whether its last call did (1) or copied all of A in before
+ * the solve and all of w and V out after it (0). */
+int gla_plan_host_pipeline(gla_plan_t plan, int* chunks, int* last_pipelined);
 
 /*
  * Adjoint of the plan's eigen-decomposition (reverse mode; the kernel behind
