@@ -156,17 +156,19 @@ struct gla_plan_s {
   // one persistent launch (k_solve_refine) instead of per-bucket pipelines
   bool persistent = false;
   int persist_grid = 0;
-  int* d_next = nullptr;  // its work counter
+  int* d_next = nullptr;  // its work counters (one per chunk of the host-execute pipeline)
   // gla_plan_execute_host of a persistent plan on pinned host buffers: the
   // batch as contiguous runs of matrices ("chunks"), so that the copy of
-  // chunk c + 1's A and of chunk c - 1's w and V overlap the solve of chunk c
+  // chunk c + 1's A and of chunk c - 1's w and V overlap the solve of chunk
+  // c; consecutive chunks are solved on two alternating streams, so that the
+  // next chunk's CTAs take the SMs the last matrices of a chunk leave idle
   int nchunks = 0;                        // 0: no pipeline
   int64_t chunk_b[kMaxChunks + 1] = {};   // chunk c: batch indices chunk_b[c] .. chunk_b[c + 1] - 1
   int64_t chunk_a[kMaxChunks + 1] = {};   // its A / V elements from chunk_a[c]
   int64_t chunk_w[kMaxChunks + 1] = {};   // its w elements from chunk_w[c]
   int chunk_start[kMaxChunks + 1] = {};   // its work items: d_chunk_order[chunk_start[c] ..]
   int* d_chunk_order = nullptr;           // each chunk's work items, orders descending
-  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaStream_t s_in = nullptr, s_out = nullptr, s_odd = nullptr;  // s_odd: the odd chunks' solves
   cudaEvent_t ev_in[kMaxChunks] = {}, ev_solved[kMaxChunks] = {}, ev_out = nullptr;
   ChaseState* h_cst = nullptr;            // pinned: the chase states after the persistent launches
   bool last_pipelined = false;            // the last gla_plan_execute_host used the pipeline
@@ -330,7 +332,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   const size_t o_w32 = carve(refined ? 4 * woff : 0);
   const size_t o_vtmp = carve((jobz == 'N' && refined) ? 8 * aoff : 0);
   const size_t o_qtmp = carve(p->stein ? 4 * aoff : 0);
-  const size_t o_next = carve(sizeof(int));
+  const size_t o_next = carve(sizeof(int) * kMaxChunks);
   size_t refine_bytes = refined ? refine_workspace_bytes(aoff, woff, batch) : 0;
   const size_t o_ref = carve(refine_bytes);
   cudaError_t err = cudaSuccess;
@@ -344,14 +346,11 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     }
     p->persist_grid = std::max(1, std::min(2 * nsm, p->nwork));
   }
-  // the tensor-core products' slice scratch, one per persistent CTA (orders above 32 only)
-  const bool pcache = p->persistent && p->refine_tc && p->nmax > 32;
-  const size_t o_pcache = carve(pcache ? (size_t)p->persist_grid * refine_pcache_bytes() : 0);
-  // host-execute pipeline: one chunk per three matrices of every persistent
-  // CTA (two chunks at least, kMaxChunks at most), split at equal A bytes
+  // host-execute pipeline: one chunk per matrix of every persistent CTA
+  // (two chunks at least, kMaxChunks at most), split at equal A bytes
   std::vector<int> chunk_order;
   if (p->persistent && p->large_idx.empty() && !p->graph && !p->timing) {
-    const int nc = std::min(kMaxChunks, p->nwork / std::max(1, 3 * p->persist_grid));
+    const int nc = std::min(kMaxChunks, p->nwork / std::max(1, p->persist_grid));
     if (nc >= 2) {
       p->nchunks = nc;
       int64_t b = 0, a = 0, wo = 0;
@@ -377,6 +376,12 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
     }
   }
   const size_t o_corder = carve(sizeof(int) * chunk_order.size());
+  // the tensor-core products' slice scratch, one per persistent CTA (orders
+  // above 32 only); a second set for the pipeline's odd chunks, whose CTAs
+  // run beside the even chunks' with the same block indices
+  const bool pcache = p->persistent && p->refine_tc && p->nmax > 32;
+  const size_t pcache_set = pcache ? (size_t)p->persist_grid * refine_pcache_bytes() : 0;
+  const size_t o_pcache = carve((p->nchunks ? 2 : 1) * pcache_set);
   p->ws_bytes = off;
   err = cudaMalloc((void**)&p->ws, p->ws_bytes);
   if (err != cudaSuccess) {
@@ -417,6 +422,7 @@ int gla_plan_create(gla_plan_t* plan_out, int precision, char jobz, char uplo, i
   if (p->nchunks) {
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->s_in, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->s_out, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&p->s_odd, cudaStreamNonBlocking);
     for (int c = 0; c < p->nchunks; c++) {
       if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_in[c], cudaEventDisableTiming);
       if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->ev_solved[c], cudaEventDisableTiming);
@@ -475,6 +481,7 @@ int gla_plan_destroy(gla_plan_t p) {
   if (p->fork) cudaEventDestroy(p->fork);
   if (p->s_in) cudaStreamDestroy(p->s_in);
   if (p->s_out) cudaStreamDestroy(p->s_out);
+  if (p->s_odd) cudaStreamDestroy(p->s_odd);
   for (int c = 0; c < kMaxChunks; c++) {
     if (p->ev_in[c]) cudaEventDestroy(p->ev_in[c]);
     if (p->ev_solved[c]) cudaEventDestroy(p->ev_solved[c]);
@@ -654,12 +661,13 @@ int execute_large(gla_plan_t p, const void* A, void* w, void* V, int* info, cuda
 }
 
 // The persistent launch over `count` matrices of the work list `order`
-// (orders descending).
+// (orders descending), with work counter `next` and the refinement
+// scratch `rw` (its slice scratch is per block index).
 int persistent_solve(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st, const int* order,
-                     int count) {
-  GLA_CUDA(cudaMemsetAsync(p->d_next, 0, sizeof(int), st));
-  GLA_CUDA(launch_solve_refine(&p->rw, count, p->nmax, std::min(p->persist_grid, count), st, p->d_desc, order,
-                               p->d_next, (const double*)A, p->uplo == 'L', (float*)p->d_d, (float*)p->d_e,
+                     int count, int* next, const RefineWork* rw) {
+  GLA_CUDA(cudaMemsetAsync(next, 0, sizeof(int), st));
+  GLA_CUDA(launch_solve_refine(rw, count, p->nmax, std::min(p->persist_grid, count), st, p->d_desc, order, next,
+                               (const double*)A, p->uplo == 'L', (float*)p->d_d, (float*)p->d_e,
                                (float*)p->d_x32, info, p->d_cst, p->d_scale, (float*)p->d_w32, (float*)p->d_qtmp,
                                (double*)Vout, (double*)w, p->d_stats, p->refine_tc));
   return 0;
@@ -676,7 +684,7 @@ int persistent_finish(gla_plan_t p, const void* A, void* w, void* Vout, int* inf
 // passes.
 int execute_persistent(gla_plan_t p, const void* A, void* w, void* Vout, int* info, cudaStream_t st) {
   p->mark(0, GLA_PHASE_TRIDIAG, 0, st);
-  if (int rc = persistent_solve(p, A, w, Vout, info, st, p->d_perm_bucket, p->nwork)) return rc;
+  if (int rc = persistent_solve(p, A, w, Vout, info, st, p->d_perm_bucket, p->nwork, p->d_next, &p->rw)) return rc;
   p->mark(0, GLA_PHASE_TRIDIAG, 1, st);
   return persistent_finish(p, A, w, Vout, info, st);
 }
@@ -862,13 +870,16 @@ bool host_pinned(const void* ptr) {
 }
 
 // gla_plan_execute_host of a persistent plan, pipelined over its chunks:
-// chunk c's A goes in on s_in, its persistent launch waits for it on the
-// caller's stream, and its w and V come out on s_out while the next chunk
-// is solved. The launches that finish the matrices the persistent kernel
-// left (the QL chase and its replay, refinement) run once at the end over
-// the whole batch, as in execute_persistent; those matrices, known from
-// the chase states copied after the last persistent launch, are copied out
-// again afterwards. Results are those of gla_plan_execute.
+// chunk c's A goes in on s_in; its persistent launch waits for it, on the
+// caller's stream for even c and on s_odd for odd c, with its own work
+// counter (and, for odd c, the second set of slice scratch), so that it
+// starts on the SMs the previous chunk's last matrices leave idle; its w
+// and V come out on s_out while later chunks are solved. The launches that
+// finish the matrices the persistent kernel left (the QL chase and its
+// replay, refinement) run once at the end over the whole batch, as in
+// execute_persistent; those matrices, known from the chase states copied
+// after the last persistent launch, are copied out again afterwards.
+// Results are those of gla_plan_execute.
 int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host,
                            cudaStream_t st) {
   const size_t ioe = p->io_elem();
@@ -887,6 +898,8 @@ int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void*
   GLA_CUDA(cudaEventRecord(p->fork, st));
   GLA_CUDA(cudaStreamWaitEvent(p->s_in, p->fork, 0));
   GLA_CUDA(cudaStreamWaitEvent(p->s_out, p->fork, 0));
+  RefineWork rw_odd = p->rw;
+  if (rw_odd.pcache) rw_odd.pcache += (size_t)p->persist_grid * refine_pcache_bytes();
   for (int c = 0; c < p->nchunks; c++) {
     const size_t a0 = ioe * p->chunk_a[c], ab = ioe * (p->chunk_a[c + 1] - p->chunk_a[c]);
     if (ab) GLA_CUDA(cudaMemcpyAsync(dA + a0, hA + a0, ab, cudaMemcpyHostToDevice, p->s_in));
@@ -895,18 +908,24 @@ int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void*
   GLA_CUDA(cudaMemsetAsync(p->d_stats, 0, sizeof(unsigned long long) * 4, st));
   GLA_CUDA(cudaMemsetAsync(p->h_info, 0, sizeof(int) * p->batch, st));
   GLA_CUDA(cudaMemsetAsync(p->rw.err, 0, sizeof(int), st));
+  // the memsets above come before every chunk's launch
+  GLA_CUDA(cudaEventRecord(p->fork, st));
+  GLA_CUDA(cudaStreamWaitEvent(p->s_odd, p->fork, 0));
   for (int c = 0; c < p->nchunks; c++) {
-    GLA_CUDA(cudaStreamWaitEvent(st, p->ev_in[c], 0));
-    if (int rc = persistent_solve(p, p->h_A, p->h_w, Vout, p->h_info, st, p->d_chunk_order + p->chunk_start[c],
-                                  p->chunk_start[c + 1] - p->chunk_start[c]))
+    cudaStream_t cs = (c & 1) ? p->s_odd : st;
+    GLA_CUDA(cudaStreamWaitEvent(cs, p->ev_in[c], 0));
+    if (int rc = persistent_solve(p, p->h_A, p->h_w, Vout, p->h_info, cs, p->d_chunk_order + p->chunk_start[c],
+                                  p->chunk_start[c + 1] - p->chunk_start[c], p->d_next + c,
+                                  (c & 1) ? &rw_odd : &p->rw))
       return rc;
-    GLA_CUDA(cudaEventRecord(p->ev_solved[c], st));
+    GLA_CUDA(cudaEventRecord(p->ev_solved[c], cs));
     GLA_CUDA(cudaStreamWaitEvent(p->s_out, p->ev_solved[c], 0));
     const size_t w0 = ioe * p->chunk_w[c], wb = ioe * (p->chunk_w[c + 1] - p->chunk_w[c]);
     const size_t a0 = ioe * p->chunk_a[c], ab = ioe * (p->chunk_a[c + 1] - p->chunk_a[c]);
     if (wb) GLA_CUDA(cudaMemcpyAsync(hW + w0, dW + w0, wb, cudaMemcpyDeviceToHost, p->s_out));
     if (wantv && ab) GLA_CUDA(cudaMemcpyAsync(hV + a0, dV + a0, ab, cudaMemcpyDeviceToHost, p->s_out));
   }
+  for (int c = 1; c < p->nchunks; c += 2) GLA_CUDA(cudaStreamWaitEvent(st, p->ev_solved[c], 0));
   GLA_CUDA(cudaMemcpyAsync(p->h_cst, p->d_cst, sizeof(ChaseState) * p->batch, cudaMemcpyDeviceToHost, st));
   if (int rc = persistent_finish(p, p->h_A, p->h_w, Vout, p->h_info, st)) return rc;
   GLA_CUDA(cudaMemcpyAsync(info_host, p->h_info, sizeof(int) * p->batch, cudaMemcpyDeviceToHost, st));
