@@ -168,11 +168,13 @@ int gla_plan_execute_eigen2_host(gla_plan_t plan, const void* A_host, void* w_ho
 /*
  * Same, from and to HOST buffers: copies A in, runs, copies w, V and info
  * out, and synchronizes `stream` before returning. Uses plan-owned device
- * buffers (allocated on first use). Pinned host memory is fastest: for an
- * GLA_PREC_F32_REFINED plan of orders <= GLA_MAX_SMALL_N whose batch fills
- * the device several times over, with A, w and V (jobz 'V') in page-locked
- * memory, the batch is solved in up to four contiguous chunks and the
- * copies of one chunk overlap the solve of the next (same results).
+ * buffers (allocated on first use). Pinned host memory is fastest: for a
+ * GLA_PREC_F32_REFINED plan of orders <= GLA_MAX_SMALL_N (none larger)
+ * holding at least two matrices per CTA of its persistent launch (two CTAs
+ * per SM), without GLA_FLAG_GRAPH or GLA_FLAG_TIMING, and with A, w and V
+ * (jobz 'V') in page-locked memory, the batch is solved in two to four
+ * contiguous chunks and the copies of one chunk overlap the solve of
+ * another (same results, bit for bit).
  */
 int gla_plan_execute_host(gla_plan_t plan, const void* A_host, void* w_host, void* V_host, int* info_host,
                           void* stream);
