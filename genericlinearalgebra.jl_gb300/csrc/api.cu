@@ -880,8 +880,7 @@ bool host_pinned(const void* ptr) {
 // execute_persistent; those matrices, known from the chase states copied
 // after the last persistent launch, are copied out again afterwards.
 // Results are those of gla_plan_execute.
-int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host,
-                           cudaStream_t st) {
+int pipelined_body(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host, cudaStream_t st) {
   const size_t ioe = p->io_elem();
   const bool wantv = p->jobz == 'V';
   void* Vout = wantv ? p->h_V : p->d_vtmp;
@@ -958,6 +957,18 @@ int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void*
   int bad = 0;
   for (int64_t b = 0; b < p->batch; b++) bad += info_host[b] != 0;
   return bad;
+}
+
+int execute_host_pipelined(gla_plan_t p, const void* A_host, void* w_host, void* V_host, int* info_host,
+                           cudaStream_t st) {
+  const int rc = pipelined_body(p, A_host, w_host, V_host, info_host, st);
+  if (rc < 0) {  // an error: none of this call's copies or solves stays in flight
+    cudaStreamSynchronize(p->s_in);
+    cudaStreamSynchronize(p->s_odd);
+    cudaStreamSynchronize(p->s_out);
+    cudaStreamSynchronize(st);
+  }
+  return rc;
 }
 }  // namespace
 
