@@ -43,6 +43,20 @@ def test_band_tridiagonal_and_back_transform(n, b):
     assert len(refl) == sum(1 for _ in M.sb2st_tasks(n, b))
 
 
+@pytest.mark.parametrize("n,b,nb", [(97, 8, 8), (130, 16, 5), (200, 32, 32), (129, 64, 16)])
+def test_blocked_q2_matches_reflector_order(n, b, nb):
+    # the compact-WY grouping of the bulge-chase reflectors gives Q2 Z as
+    # the reflectors applied one by one in program order (applying a sweep
+    # block's groups with t descending instead is off by O(1))
+    A = goe(n, 950 + n)
+    B, _ = M.sy2sb(A, b)
+    _, refl = M.sb2st(B, b)
+    Z = np.linalg.qr(np.random.default_rng(n).standard_normal((n, n)))[0]
+    X1 = M.q2_apply(refl, Z)
+    X2 = M.q2_apply_blocked(refl, Z, b, nb)
+    assert np.abs(X1 - X2).max() <= 1e-13
+
+
 def test_graded_and_already_banded_input():
     # rows scaled over six orders of magnitude, and a matrix that is already
     # tridiagonal (every reflector is the identity: tau = 0)

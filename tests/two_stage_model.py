@@ -135,6 +135,43 @@ def q2_apply(refl, Z):
     return Z
 
 
+def q2_apply_blocked(refl, Z, b, nb):
+    """Q2 Z with the reflectors grouped in compact-WY blocks: group (J, t)
+    holds task t of sweeps J .. J + nb - 1 (nb <= b), rows J + 1 + t b ..
+    J + nb + t b + b - 1, one (b + nb - 1) x nb block V and nb x nb T.
+    Groups are applied for J descending and, within J, t ascending, each as
+    I - V T V' (its sweeps descending). Two reflectors whose order this
+    changes against q2_apply act on disjoint rows (nb <= b), so the result
+    is the same up to rounding; each group is one GEMM pair over all of Z's
+    columns instead of nb rank-1 updates."""
+    assert nb <= b
+    Z = np.array(Z, dtype=float)
+    n = Z.shape[0]
+    by = {}
+    for j, t, r0, v, tau in refl:
+        by[(j, t)] = (r0, v, tau)
+    nsweep = max(j for j, _, _, _, _ in refl) + 1 if refl else 0
+    for J in reversed(range(0, nsweep, nb)):
+        ts = sorted({t for (j, t) in by if J <= j < J + nb})
+        for t in ts:
+            members = [(j,) + by[(j, t)] for j in range(J, min(J + nb, nsweep)) if (j, t) in by]
+            lo = min(r0 for _, r0, _, _ in members)
+            hi = max(r0 + len(v) for _, r0, v, _ in members)
+            k = len(members)
+            V = np.zeros((hi - lo, k))
+            taus = np.zeros(k)
+            for c, (_, r0, v, tau) in enumerate(members):  # sweeps ascending
+                V[r0 - lo:r0 - lo + len(v), c] = v
+                taus[c] = tau
+            T = np.zeros((k, k))
+            for c in range(k):
+                T[c, c] = taus[c]
+                if c:
+                    T[:c, c] = -taus[c] * T[:c, :c] @ (V[:, :c].T @ V[:, c])
+            Z[lo:hi] -= V @ (T @ (V.T @ Z[lo:hi]))
+    return Z
+
+
 def critical_path(n, b):
     """(tasks, critical path in tasks, widest step) of the bulge chase with
     unit-time tasks, each after every earlier task whose lo .. hi - 1
