@@ -174,13 +174,22 @@ def q2_apply_blocked(refl, Z, b, nb):
 
 def critical_path(n, b):
     """(tasks, critical path in tasks, widest step) of the bulge chase with
-    unit-time tasks, each after every earlier task whose lo .. hi - 1
-    overlaps its own: the latency floor of a GPU schedule of the sweeps."""
-    last = np.zeros(n, dtype=np.int64)
+    unit-time tasks, each after every earlier task that touched one of the
+    lower-band entries it touches: the latency floor of a GPU schedule of
+    the sweeps. Task (j, t) reads and writes rows r0 .. r1 - 1, columns
+    c .. r1 - 1 (c the column it annihilates: its left update and the
+    diagonal block) and rows r1 .. r1 + b - 1, columns r0 .. r1 - 1 (its
+    right update, which fills the bulge)."""
+    last = np.zeros((n, n), dtype=np.int64)
     count, width = 0, {}
-    for _, _, _, _, lo, hi in sb2st_tasks(n, b):
-        s = int(last[lo:hi].max())
-        last[lo:hi] = s + 1
+    for j, t, r0, r1, _, _ in sb2st_tasks(n, b):
+        c = j if t == 0 else r0 - b
+        r2 = min(n, r1 + b)
+        s = int(last[r0:r1, c:r1].max())
+        if r2 > r1:
+            s = max(s, int(last[r1:r2, r0:r1].max()))
+            last[r1:r2, r0:r1] = s + 1
+        last[r0:r1, c:r1] = s + 1
         count += 1
         width[s] = width.get(s, 0) + 1
     return count, int(last.max()), max(width.values()) if width else 0
