@@ -36,6 +36,25 @@ def test_python_binding_covers_header():
     assert set(_lib.SIGNATURES) == set(header_symbols())
 
 
+def test_python_signatures_match_prototypes():
+    # the ctypes table against the header: argument count and each type's
+    # size and kind (pointers as c_void_p, POINTER(...) or c_char_p)
+    from glagpu import _lib
+    from test_julia_glue import prototypes
+    scalars = {"int": ctypes.c_int, "int64_t": ctypes.c_int64, "size_t": ctypes.c_size_t,
+               "double": ctypes.c_double, "float": ctypes.c_float, "char": ctypes.c_char}
+    for name, (cret, ctypes_) in prototypes().items():
+        args, ret = _lib.SIGNATURES[name]
+        assert len(args) == len(ctypes_), name
+        for c, t in zip(ctypes_ + [cret], list(args) + [ret]):
+            c = c.replace("const ", "").strip()
+            if c.endswith("*") or c == "gla_plan_t":
+                assert t in (ctypes.c_void_p, ctypes.c_char_p) or t.__name__.startswith("LP_"), (name, c, t)
+            else:
+                assert ctypes.sizeof(t) == ctypes.sizeof(scalars[c]), (name, c, t)
+                assert (t in (ctypes.c_float, ctypes.c_double)) == (c in ("float", "double")), (name, c, t)
+
+
 def test_host_only_calls(lib):
     lib.gla_version.restype = ctypes.c_int
     assert lib.gla_version() == 100

@@ -19,6 +19,7 @@ def prototypes():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
     src = re.sub(r"//[^\n]*", " ", src)
+    src = re.sub(r"(?m)^\s*#.*$", " ", src)  # preprocessor lines
     out = {}
     for ret, name, params in re.findall(r"([A-Za-z_][\w\s\*]*?)\b(gla_\w+)\s*\(([^)]*)\)\s*;", src):
         types = []
