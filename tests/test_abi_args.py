@@ -73,3 +73,36 @@ def test_single_matrix_drivers_reject_each_argument(lib):
     assert lib.gla_dsyev(b"V", b"L", 4, vp(8), 3, vp(8), ctypes.byref(info), None) == -5  # lda < n
     assert lib.gla_dsyev_static(b"V", b"L", 200, vp(8), 200, vp(8), ctypes.byref(info), None) == -2001
     assert lib.gla_dstev(b"X", 4, None, None, None, 4, 0, ctypes.byref(info), None) == -1
+
+
+def test_other_entry_points_reject_each_argument(lib):
+    p = ctypes.c_void_p(64)
+    info = ctypes.c_int(0)
+    # complex and quaternion Hermitian (their real embeddings are of order 2n and 4n)
+    assert lib.gla_zheev(b"X", b"L", 4, p, 4, p, p, 4, ctypes.byref(info), None) == -1
+    assert lib.gla_zheev(b"V", b"X", 4, p, 4, p, p, 4, ctypes.byref(info), None) == -2
+    assert lib.gla_zheev(b"V", b"L", -1, p, 4, p, p, 4, ctypes.byref(info), None) == -3
+    assert lib.gla_zheev(b"V", b"L", 9000, p, 9000, p, p, 9000, ctypes.byref(info), None) == -3  # 2n > GLA_MAX_N
+    assert lib.gla_zheev(b"V", b"L", 4, p, 3, p, p, 4, ctypes.byref(info), None) == -5
+    assert lib.gla_zheev(b"V", b"L", 4, p, 4, p, p, 3, ctypes.byref(info), None) == -8
+    assert lib.gla_qheev(b"X", b"L", 4, p, 4, p, p, 4, ctypes.byref(info), None) == -1
+    assert lib.gla_qheev(b"V", b"L", 5000, p, 5000, p, p, 5000, ctypes.byref(info), None) == -3  # 4n > GLA_MAX_N
+    # symtri! and its EigenQ products
+    assert lib.gla_dsytrd(b"X", 4, p, 4, p, p, p, None) == -1
+    assert lib.gla_dsytrd(b"L", -1, p, 4, p, p, p, None) == -2
+    assert lib.gla_dsytrd(b"L", 4, p, 3, p, p, p, None) == -4
+    assert lib.gla_dormtr(b"X", b"L", b"N", 4, 4, p, 4, p, p, 4, None) == -1
+    assert lib.gla_dormtr(b"L", b"X", b"N", 4, 4, p, 4, p, p, 4, None) == -2
+    assert lib.gla_dormtr(b"L", b"L", b"X", 4, 4, p, 4, p, p, 4, None) == -3
+    assert lib.gla_dormtr(b"L", b"L", b"N", -1, 4, p, 4, p, p, 4, None) == -4
+    # spectrum slicing: an empty index range (iu = il - 1) is a no-op
+    assert lib.gla_numnegevals(-1, p, p, 2, p, p, None) == -1
+    assert lib.gla_numnegevals(4, p, p, -1, p, p, None) == -4
+    assert lib.gla_dstebz(4, p, p, 0, 2, 0.0, p, None) == -4
+    assert lib.gla_dstebz(4, p, p, 1, 5, 0.0, p, None) == -5
+    assert lib.gla_dstebz(4, p, p, 3, 2, 0.0, p, None) == 0
+    # the GEMMs: sizes, and the 16-byte alignment the TMA tensor maps need
+    assert lib.gla_sgemm_3xtf32(-1, 4, 4, 1.0, p, 4, p, 4, 0.0, p, 4, None) == -1
+    assert lib.gla_sgemm_3xtf32(4, 4, 4, 1.0, ctypes.c_void_p(66), 4, p, 4, 0.0, p, 4, None) == -5
+    assert lib.gla_sgemm_3xtf32(4, 4, 4, 1.0, p, 3, p, 4, 0.0, p, 4, None) == -6
+    assert lib.gla_gemm_df(-1, 4, 4, p, p, 4, p, p, 4, p, p, 4, None) == -1
